@@ -1,0 +1,765 @@
+// gbfe_core.cu -- handles, uploads and the FP64 cellwise operator apply.
+//
+// The apply Y = P^T (sum_c G_c^T A_c G_c) P X of
+// ksdft/KohnShamOperatorContextFE.t.cpp:1326-1443 runs as three kernels on
+// the context's stream:
+//   1. k_p2c            X[r] = inh_r + sum_j w_rj X[c_j]        (constraint rows)
+//   2. k_cell_apply_f64 per cell: gather X[ids] into shared memory, then
+//                       Yc = A_c^T Xc (the reference's column-major
+//                       C(m x nd) = Xc(m x nd) * A_c(nd x nd)), written to a
+//                       cell-wise scratch buffer
+//   3. k_assemble       per dof: sum of its cell slots in ascending cell order,
+//                       plus w * (row sum) for every constraint row that names
+//                       it as a parent (distributeChildToParent), rows -> 0.
+// No float atomics anywhere: every output element has exactly one writer and a
+// fixed summation order, so results are bitwise reproducible run to run.
+#include "gbfe_internal.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+using namespace gbfe;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_p2c(T *__restrict__ x, uint32_t m, uint32_t n_rows, const uint32_t *__restrict__ row_ids,
+                      const uint32_t *__restrict__ row_sizes, const uint32_t *__restrict__ col_ids,
+                      const uint32_t *__restrict__ row_acc, const double *__restrict__ col_vals,
+                      const double *__restrict__ inh) {
+  const uint64_t total = (uint64_t)n_rows * m;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = (uint32_t)(t / m), v = (uint32_t)(t - (uint64_t)i * m);
+    T val = (T)inh[i];
+    const uint32_t a = row_acc[i], s = row_sizes[i];
+    for (uint32_t j = 0; j < s; ++j) val += (T)col_vals[a + j] * x[(uint64_t)col_ids[a + j] * m + v];
+    x[(uint64_t)row_ids[i] * m + v] = val;
+  }
+}
+
+// Constraint rows are zeroed and parents collect w * x[row] in row order.
+template <class T>
+__global__ void k_c2p_inplace(T *__restrict__ x, uint32_t m, uint64_t n_dofs, const uint32_t *__restrict__ par_ptr,
+                              const uint32_t *__restrict__ par_row, const double *__restrict__ par_w) {
+  const uint64_t total = n_dofs * m;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = t / m;
+    const uint32_t v = (uint32_t)(t - i * m);
+    const uint32_t b = par_ptr[i], e = par_ptr[i + 1];
+    if (b == e) continue;
+    T acc = x[t];
+    for (uint32_t q = b; q < e; ++q) acc += (T)par_w[q] * x[(uint64_t)par_row[q] * m + v];
+    x[t] = acc;
+  }
+}
+
+template <class T>
+__global__ void k_zero_rows(T *__restrict__ x, uint32_t m, uint32_t n_rows, const uint32_t *__restrict__ row_ids) {
+  const uint64_t total = (uint64_t)n_rows * m;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = (uint32_t)(t / m), v = (uint32_t)(t - (uint64_t)i * m);
+    x[(uint64_t)row_ids[i] * m + v] = (T)0;
+  }
+}
+
+// FP64 cell product.  grid = (cells, vector tiles, row splits); block = 256.
+// Shared memory: Xs[nd][mtc] for this cell's vector tile.
+__global__ void __launch_bounds__(256) k_cell_apply_f64(
+    const double *__restrict__ X, uint32_t m, const uint32_t *__restrict__ ids,
+    const uint32_t *__restrict__ cell_off, const uint64_t *__restrict__ mat_off,
+    const double *__restrict__ mats, double *__restrict__ Yc, uint32_t mt, uint32_t jsplit) {
+  extern __shared__ double Xs[];
+  const uint32_t c = blockIdx.x;
+  const uint32_t v0 = blockIdx.y * mt;
+  const uint32_t mtc = min(mt, m - v0);
+  const uint32_t off = cell_off[c];
+  const uint32_t nd = cell_off[c + 1] - off;
+  const double *__restrict__ A = mats + mat_off[c];
+  const uint32_t nin = nd * mtc;
+  for (uint32_t idx = threadIdx.x; idx < nin; idx += blockDim.x) {
+    const uint32_t k = idx / mtc, v = idx - k * mtc;
+    Xs[idx] = X[(uint64_t)ids[off + k] * m + v0 + v];
+  }
+  __syncthreads();
+  const uint32_t jper = (nd + jsplit - 1) / jsplit;
+  const uint32_t j0 = blockIdx.z * jper;
+  const uint32_t j1 = min(nd, j0 + jper);
+  if (j0 >= j1) return;
+  const uint32_t nout = (j1 - j0) * mtc;
+  for (uint32_t o = threadIdx.x; o < nout; o += blockDim.x) {
+    const uint32_t jj = o / mtc, v = o - jj * mtc;
+    const uint32_t j = j0 + jj;
+    const double *__restrict__ Aj = A + (uint64_t)nd * j;  // column j of A_c
+    double acc0 = 0.0, acc1 = 0.0;
+    uint32_t k = 0;
+    for (; k + 1 < nd; k += 2) {
+      acc0 = fma(__ldg(Aj + k), Xs[k * mtc + v], acc0);
+      acc1 = fma(__ldg(Aj + k + 1), Xs[(k + 1) * mtc + v], acc1);
+    }
+    if (k < nd) acc0 = fma(__ldg(Aj + k), Xs[k * mtc + v], acc0);
+    Yc[(uint64_t)(off + j) * m + v0 + v] = acc0 + acc1;
+  }
+}
+
+// Assembly with the constraint epilogue fused in.  One thread per (dof, vec).
+template <class TC, class TY>
+__global__ void k_assemble(const TC *__restrict__ Yc, uint32_t m, uint64_t n_dofs,
+                           const uint32_t *__restrict__ slot_ptr, const uint32_t *__restrict__ slot,
+                           const uint8_t *__restrict__ is_row, const uint32_t *__restrict__ par_ptr,
+                           const uint32_t *__restrict__ par_row, const double *__restrict__ par_w,
+                           TY *__restrict__ Y) {
+  const uint64_t total = n_dofs * m;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = t / m;
+    const uint32_t v = (uint32_t)(t - i * m);
+    if (is_row && is_row[i]) {
+      Y[t] = (TY)0;
+      continue;
+    }
+    TY acc = (TY)0;
+    for (uint32_t p = slot_ptr[i], e = slot_ptr[i + 1]; p < e; ++p) acc = acc + (TY)Yc[(uint64_t)slot[p] * m + v];
+    if (par_ptr) {
+      for (uint32_t q = par_ptr[i], qe = par_ptr[i + 1]; q < qe; ++q) {
+        const uint32_t r = par_row[q];
+        TY sr = (TY)0;
+        for (uint32_t p = slot_ptr[r], e = slot_ptr[r + 1]; p < e; ++p) sr = sr + (TY)Yc[(uint64_t)slot[p] * m + v];
+        acc += (TY)par_w[q] * sr;
+      }
+    }
+    Y[t] = acc;
+  }
+}
+
+// Diagonal operator with the constraint epilogue fused in.
+template <class T>
+__global__ void k_diag_apply(const T *__restrict__ X, uint32_t m, uint64_t n_dofs, const double *__restrict__ d,
+                             const uint8_t *__restrict__ is_row, const uint32_t *__restrict__ par_ptr,
+                             const uint32_t *__restrict__ par_row, const double *__restrict__ par_w,
+                             T *__restrict__ Y) {
+  const uint64_t total = n_dofs * m;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = t / m;
+    const uint32_t v = (uint32_t)(t - i * m);
+    if (is_row && is_row[i]) {
+      Y[t] = (T)0;
+      continue;
+    }
+    T acc = (T)d[i] * X[t];
+    if (par_ptr) {
+      for (uint32_t q = par_ptr[i], qe = par_ptr[i + 1]; q < qe; ++q) {
+        const uint32_t r = par_row[q];
+        acc += (T)par_w[q] * ((T)d[r] * X[(uint64_t)r * m + v]);
+      }
+    }
+    Y[t] = acc;
+  }
+}
+
+template <class TS, class TD>
+__global__ void k_convert(const TS *__restrict__ s, TD *__restrict__ d, uint64_t n) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x)
+    d[t] = (TD)s[t];
+}
+
+template <class T>
+__global__ void k_fill(T *__restrict__ d, uint64_t n, T v) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x)
+    d[t] = v;
+}
+
+unsigned stride_grid(gbfe_ctx *ctx, uint64_t n, unsigned block = 256) {
+  uint64_t g = (n + block - 1) / block;
+  const uint64_t cap = (uint64_t)ctx->sm_count * 16;
+  if (g > cap) g = cap;
+  return (unsigned)(g ? g : 1);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// internal API
+// ---------------------------------------------------------------------------
+namespace gbfe {
+
+void constraints_p2c(gbfe_ctx *ctx, const gbfe_cons *c, gbfe_mv *x) {
+  if (!c || c->n_rows == 0 || x->m == 0) return;
+  const uint64_t n = (uint64_t)c->n_rows * x->m;
+  if (c->pure_dirichlet) {
+    if (x->dtype == GBFE_F64)
+      k_zero_rows<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(x->d.p, x->m, c->n_rows, c->row_ids.p);
+    else
+      k_zero_rows<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(x->f.p, x->m, c->n_rows, c->row_ids.p);
+  } else {
+    if (x->dtype == GBFE_F64)
+      k_p2c<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(x->d.p, x->m, c->n_rows, c->row_ids.p,
+                                                                   c->row_sizes.p, c->col_ids.p, c->row_acc.p,
+                                                                   c->col_vals.p, c->inh.p);
+    else
+      k_p2c<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(x->f.p, x->m, c->n_rows, c->row_ids.p,
+                                                                  c->row_sizes.p, c->col_ids.p, c->row_acc.p,
+                                                                  c->col_vals.p, c->inh.p);
+  }
+  check_launch(ctx, "p2c");
+}
+
+static void constraints_c2p(gbfe_ctx *ctx, const gbfe_cons *c, gbfe_mv *x) {
+  if (!c || c->n_rows == 0 || x->m == 0) return;
+  const uint64_t n = x->count();
+  if (!c->pure_dirichlet) {
+    if (x->dtype == GBFE_F64)
+      k_c2p_inplace<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(x->d.p, x->m, x->mesh->n_dofs,
+                                                                           c->par_ptr.p, c->par_row.p, c->par_w.p);
+    else
+      k_c2p_inplace<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(x->f.p, x->m, x->mesh->n_dofs,
+                                                                          c->par_ptr.p, c->par_row.p, c->par_w.p);
+    check_launch(ctx, "c2p");
+  }
+  const uint64_t nr = (uint64_t)c->n_rows * x->m;
+  if (x->dtype == GBFE_F64)
+    k_zero_rows<double><<<stride_grid(ctx, nr), 256, 0, ctx->stream>>>(x->d.p, x->m, c->n_rows, c->row_ids.p);
+  else
+    k_zero_rows<float><<<stride_grid(ctx, nr), 256, 0, ctx->stream>>>(x->f.p, x->m, c->n_rows, c->row_ids.p);
+  check_launch(ctx, "zero_rows");
+}
+
+static void cell_apply_f64(const gbfe_op *op, gbfe_mv *X, double *Yc) {
+  gbfe_mesh *me = op->mesh;
+  gbfe_ctx *ctx = me->ctx;
+  const uint32_t m = X->m;
+  const size_t smem_cap = 96 * 1024;
+  uint32_t mt = (uint32_t)std::min<size_t>(m, smem_cap / (sizeof(double) * me->nd_max));
+  if (mt == 0) throw Error(GBFE_ERR_ARG, "cell too large for the FP64 apply");
+  const uint32_t vt = (m + mt - 1) / mt;
+  mt = (m + vt - 1) / vt;  // balance vector tiles
+  uint64_t base = (uint64_t)me->n_cells * vt;
+  uint32_t jsplit = 1;
+  const uint64_t target = (uint64_t)ctx->sm_count * 12;
+  while (base * jsplit < target && jsplit * 8 < me->nd_min) jsplit *= 2;
+  const size_t smem = sizeof(double) * (size_t)me->nd_max * mt;
+  static bool attr_set = false;
+  if (!attr_set) {
+    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+    attr_set = true;
+  }
+  dim3 grid(me->n_cells, vt, jsplit);
+  k_cell_apply_f64<<<grid, 256, smem, ctx->stream>>>(X->d.p, m, me->ids.p, me->cell_off.p, me->mat_off.p,
+                                                     op->mats.p, Yc, mt, jsplit);
+  check_launch(ctx, "cell_apply_f64");
+}
+
+void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
+  gbfe_mesh *me = op->mesh;
+  gbfe_ctx *ctx = me->ctx;
+  GBFE_REQUIRE(X->mesh == me && Y->mesh == me, "apply: vectors belong to a different mesh");
+  GBFE_REQUIRE(X->m == Y->m, "apply: X and Y have different numbers of vectors");
+  GBFE_REQUIRE(X->dtype == Y->dtype, "apply: X and Y have different precisions");
+  GBFE_REQUIRE(X != Y, "apply: X and Y must be distinct");
+  const uint32_t m = X->m;
+  if (m == 0) return;
+  const gbfe_cons *c = op->cons;
+  const bool has_par = c && !c->pure_dirichlet;
+  const uint64_t n = (uint64_t)me->n_dofs * m;
+
+  if (op->kind == OP_JACOBI) {
+    if (X->dtype == GBFE_F64)
+      k_diag_apply<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->d.p, m, me->n_dofs, op->diag.p, nullptr,
+                                                                         nullptr, nullptr, nullptr, Y->d.p);
+    else
+      k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->f.p, m, me->n_dofs, op->diag.p, nullptr,
+                                                                        nullptr, nullptr, nullptr, Y->f.p);
+    check_launch(ctx, "jacobi_apply");
+    return;
+  }
+  constraints_p2c(ctx, c, X);
+  if (op->kind == OP_DIAG) {
+    const uint8_t *isr = c ? c->is_row.p : nullptr;
+    if (X->dtype == GBFE_F64)
+      k_diag_apply<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+          X->d.p, m, me->n_dofs, op->diag.p, isr, has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr,
+          has_par ? c->par_w.p : nullptr, Y->d.p);
+    else
+      k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+          X->f.p, m, me->n_dofs, op->diag.p, isr, has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr,
+          has_par ? c->par_w.p : nullptr, Y->f.p);
+    check_launch(ctx, "diag_apply");
+    return;
+  }
+  // cell operator
+  if (X->dtype == GBFE_F32) {
+    apply_cell_mixed(op, X, Y);
+    return;
+  }
+  op->cellbuf.ensure((size_t)me->total_cell_dofs * m);
+  cell_apply_f64(op, X, op->cellbuf.p);
+  const uint8_t *isr = c ? c->is_row.p : nullptr;
+  k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+      op->cellbuf.p, m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr, has_par ? c->par_ptr.p : nullptr,
+      has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->d.p);
+  check_launch(ctx, "assemble_f64");
+}
+
+// assembly entry used by the mixed path (FP32 cell buffer -> FP32 Y)
+void assemble_f32(const gbfe_op *op, const float *Yc, gbfe_mv *Y) {
+  gbfe_mesh *me = op->mesh;
+  gbfe_ctx *ctx = me->ctx;
+  const gbfe_cons *c = op->cons;
+  const bool has_par = c && !c->pure_dirichlet;
+  const uint64_t n = (uint64_t)me->n_dofs * Y->m;
+  const uint8_t *isr = c ? c->is_row.p : nullptr;
+  k_assemble<float, float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+      Yc, Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr, has_par ? c->par_ptr.p : nullptr,
+      has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->f.p);
+  check_launch(ctx, "assemble_f32");
+}
+
+void convert_mv(gbfe_ctx *ctx, const gbfe_mv *src, gbfe_mv *dst) {
+  const uint64_t n = src->count();
+  if (src->dtype == dst->dtype) {
+    GBFE_CUDA(cudaMemcpyAsync(dst->ptr(), src->ptr(), n * (src->dtype == GBFE_F64 ? 8 : 4),
+                              cudaMemcpyDeviceToDevice, ctx->stream));
+    return;
+  }
+  if (src->dtype == GBFE_F64)
+    k_convert<double, float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(src->d.p, dst->f.p, n);
+  else
+    k_convert<float, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(src->f.p, dst->d.p, n);
+  check_launch(ctx, "convert");
+}
+
+void fill_mv(gbfe_ctx *ctx, gbfe_mv *x, double v) {
+  const uint64_t n = x->count();
+  if (!n) return;
+  if (x->dtype == GBFE_F64)
+    k_fill<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(x->d.p, n, v);
+  else
+    k_fill<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(x->f.p, n, (float)v);
+  check_launch(ctx, "fill");
+}
+
+}  // namespace gbfe
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int gbfe_ctx_create(int device, gbfe_ctx **out) {
+  if (!out) return GBFE_ERR_ARG;
+  *out = nullptr;
+  gbfe_ctx *ctx = nullptr;
+  try {
+    ctx = new gbfe_ctx();
+  } catch (...) {
+    return GBFE_ERR_ALLOC;
+  }
+  int rc = gbfe_guard(ctx, [&] {
+    int n = 0;
+    GBFE_CUDA(cudaGetDeviceCount(&n));
+    GBFE_REQUIRE(device >= 0 && device < n, "no such CUDA device");
+    GBFE_CUDA(cudaSetDevice(device));
+    int major = 0, minor = 0;
+    GBFE_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device));
+    GBFE_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device));
+    GBFE_REQUIRE(major == 10 && minor == 3, "libgbfe is built for sm_103a (GB300) only");
+    ctx->device = device;
+    GBFE_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
+    GBFE_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+    ctx->stream = ctx->own_stream;
+    GBFE_CUBLAS(cublasCreate(&ctx->cublas));
+    GBFE_CUBLAS(cublasSetStream(ctx->cublas, ctx->stream));
+    GBFE_CUBLAS(cublasSetPointerMode(ctx->cublas, CUBLAS_POINTER_MODE_HOST));
+    GBFE_CUSOLVER(cusolverDnCreate(&ctx->cusolver));
+    GBFE_CUSOLVER(cusolverDnSetStream(ctx->cusolver, ctx->stream));
+  });
+  if (rc != GBFE_OK) {
+    std::string msg = ctx->last_error;
+    gbfe_ctx_destroy(ctx);
+    fprintf(stderr, "gbfe_ctx_create: %s\n", msg.c_str());
+    return rc;
+  }
+  *out = ctx;
+  return GBFE_OK;
+}
+
+int gbfe_ctx_destroy(gbfe_ctx *ctx) {
+  if (!ctx) return GBFE_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->red.reset();
+  ctx->small.reset();
+  ctx->info.reset();
+  ctx->lwork.reset();
+  if (ctx->cusolver) cusolverDnDestroy(ctx->cusolver);
+  if (ctx->cublas) cublasDestroy(ctx->cublas);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return GBFE_OK;
+}
+
+int gbfe_last_error(const gbfe_ctx *ctx, char *buf, size_t len) {
+  if (!ctx || !buf || !len) return GBFE_ERR_ARG;
+  snprintf(buf, len, "%s", ctx->last_error.c_str());
+  return GBFE_OK;
+}
+
+int gbfe_ctx_set_stream(gbfe_ctx *ctx, void *stream) {
+  if (!ctx) return GBFE_ERR_ARG;
+  return gbfe_guard(ctx, [&] {
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    GBFE_CUBLAS(cublasSetStream(ctx->cublas, ctx->stream));
+    GBFE_CUSOLVER(cusolverDnSetStream(ctx->cusolver, ctx->stream));
+  });
+}
+
+int gbfe_ctx_synchronize(gbfe_ctx *ctx) {
+  if (!ctx) return GBFE_ERR_ARG;
+  return gbfe_guard(ctx, [&] { GBFE_CUDA(cudaStreamSynchronize(ctx->stream)); });
+}
+
+int gbfe_ctx_kernel_launches(const gbfe_ctx *ctx, uint64_t *count) {
+  if (!ctx || !count) return GBFE_ERR_ARG;
+  *count = ctx->launches;
+  return GBFE_OK;
+}
+
+int gbfe_mesh_upload(gbfe_ctx *ctx, uint32_t n_cells, const uint32_t *nd_per_cell, const uint32_t *cell_dof_ids,
+                     uint64_t n_dofs, gbfe_mesh **out) {
+  if (!ctx || !out) return GBFE_ERR_ARG;
+  *out = nullptr;
+  gbfe_mesh *me = nullptr;
+  int rc = gbfe_guard(ctx, [&] {
+    GBFE_REQUIRE(n_cells > 0 && nd_per_cell && cell_dof_ids && n_dofs > 0, "mesh_upload: empty mesh");
+    GBFE_REQUIRE(n_dofs < 0xffffffffULL, "mesh_upload: n_dofs must fit in uint32 (size_type)");
+    me = new gbfe_mesh();
+    me->ctx = ctx;
+    me->n_dofs = n_dofs;
+    me->n_cells = n_cells;
+    me->h_nd.assign(nd_per_cell, nd_per_cell + n_cells);
+    me->h_cell_off.resize(n_cells + 1);
+    me->h_mat_off.resize(n_cells + 1);
+    me->h_cell_off[0] = 0;
+    me->h_mat_off[0] = 0;
+    uint64_t tot = 0, totm = 0;
+    me->nd_max = 0;
+    me->nd_min = 0xffffffffu;
+    for (uint32_t c = 0; c < n_cells; ++c) {
+      const uint32_t nd = nd_per_cell[c];
+      GBFE_REQUIRE(nd > 0, "mesh_upload: cell with zero dofs");
+      tot += nd;
+      totm += (uint64_t)nd * nd;
+      GBFE_REQUIRE(tot < 0xffffffffULL, "mesh_upload: too many cell dofs for uint32 offsets");
+      me->h_cell_off[c + 1] = (uint32_t)tot;
+      me->h_mat_off[c + 1] = totm;
+      me->nd_max = std::max(me->nd_max, nd);
+      me->nd_min = std::min(me->nd_min, nd);
+    }
+    me->total_cell_dofs = tot;
+    me->total_mat = totm;
+    // dof -> slots transpose (counting sort keeps ascending slot order)
+    std::vector<uint32_t> cnt(n_dofs + 1, 0);
+    for (uint64_t p = 0; p < tot; ++p) {
+      const uint32_t g = cell_dof_ids[p];
+      GBFE_REQUIRE(g < n_dofs, "mesh_upload: dof id out of range");
+      cnt[g + 1]++;
+    }
+    for (uint64_t i = 0; i < n_dofs; ++i) cnt[i + 1] += cnt[i];
+    std::vector<uint32_t> slot(tot), pos(cnt.begin(), cnt.end() - 1);
+    for (uint64_t p = 0; p < tot; ++p) slot[pos[cell_dof_ids[p]]++] = (uint32_t)p;
+    // size bins (distinct nd values), cells grouped by bin in ascending cell order
+    std::vector<uint32_t> nds(me->h_nd);
+    std::sort(nds.begin(), nds.end());
+    nds.erase(std::unique(nds.begin(), nds.end()), nds.end());
+    me->bin_nd = nds;
+    std::vector<uint32_t> bcells;
+    bcells.reserve(n_cells);
+    for (uint32_t b = 0; b < nds.size(); ++b) {
+      me->bin_begin.push_back((uint32_t)bcells.size());
+      for (uint32_t c = 0; c < n_cells; ++c)
+        if (me->h_nd[c] == nds[b]) bcells.push_back(c);
+    }
+    me->bin_begin.push_back((uint32_t)bcells.size());
+    cudaStream_t s = ctx->stream;
+    me->ids.upload(cell_dof_ids, tot, s);
+    me->nd.upload(nd_per_cell, n_cells, s);
+    me->cell_off.upload(me->h_cell_off.data(), n_cells + 1, s);
+    me->mat_off.upload(me->h_mat_off.data(), n_cells + 1, s);
+    me->slot_ptr.upload(cnt.data(), n_dofs + 1, s);
+    me->slot.upload(slot.data(), tot, s);
+    me->bin_cells.upload(bcells.data(), bcells.size(), s);
+    GBFE_CUDA(cudaStreamSynchronize(s));
+  });
+  if (rc != GBFE_OK) {
+    delete me;
+    return rc;
+  }
+  *out = me;
+  return GBFE_OK;
+}
+
+int gbfe_mesh_destroy(gbfe_mesh *mesh) {
+  if (!mesh) return GBFE_OK;
+  cudaStreamSynchronize(mesh->ctx->stream);
+  delete mesh;
+  return GBFE_OK;
+}
+
+int gbfe_constraints_upload(gbfe_mesh *mesh, uint32_t n_rows, const uint32_t *row_ids, const uint32_t *row_sizes,
+                            const uint32_t *col_ids, const uint32_t *row_acc, const double *col_values,
+                            const double *inhomogeneities, gbfe_cons **out) {
+  if (!mesh || !out) return GBFE_ERR_ARG;
+  *out = nullptr;
+  gbfe_ctx *ctx = mesh->ctx;
+  gbfe_cons *c = nullptr;
+  int rc = gbfe_guard(ctx, [&] {
+    GBFE_REQUIRE(n_rows == 0 || (row_ids && row_sizes && row_acc && inhomogeneities),
+                 "constraints_upload: null array");
+    c = new gbfe_cons();
+    c->mesh = mesh;
+    c->n_rows = n_rows;
+    const uint64_t N = mesh->n_dofs;
+    std::vector<uint8_t> is_row(N, 0);
+    uint64_t nnz = 0;
+    for (uint32_t i = 0; i < n_rows; ++i) {
+      GBFE_REQUIRE(row_ids[i] < N, "constraints_upload: row id out of range");
+      GBFE_REQUIRE(!is_row[row_ids[i]], "constraints_upload: duplicate constraint row");
+      is_row[row_ids[i]] = 1;
+      nnz = std::max<uint64_t>(nnz, (uint64_t)row_acc[i] + row_sizes[i]);
+      if (row_sizes[i] != 0 || inhomogeneities[i] != 0.0) c->pure_dirichlet = false;
+    }
+    GBFE_REQUIRE(nnz == 0 || (col_ids && col_values), "constraints_upload: null column arrays");
+    c->nnz = nnz;
+    // transpose: parent column -> (row dof, weight) in ascending constraint-row order
+    std::vector<uint32_t> cnt(N + 1, 0);
+    for (uint32_t i = 0; i < n_rows; ++i)
+      for (uint32_t j = 0; j < row_sizes[i]; ++j) {
+        const uint32_t col = col_ids[row_acc[i] + j];
+        GBFE_REQUIRE(col < N, "constraints_upload: column id out of range");
+        GBFE_REQUIRE(!is_row[col], "constraints_upload: constraints are not closed (a column is a constrained row)");
+        cnt[col + 1]++;
+      }
+    for (uint64_t i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
+    const uint64_t tnnz = cnt[N];
+    std::vector<uint32_t> prow(tnnz), pos(cnt.begin(), cnt.end() - 1);
+    std::vector<double> pw(tnnz);
+    for (uint32_t i = 0; i < n_rows; ++i)
+      for (uint32_t j = 0; j < row_sizes[i]; ++j) {
+        const uint32_t col = col_ids[row_acc[i] + j];
+        const uint32_t q = pos[col]++;
+        prow[q] = row_ids[i];
+        pw[q] = col_values[row_acc[i] + j];
+      }
+    cudaStream_t s = ctx->stream;
+    if (n_rows) {
+      c->row_ids.upload(row_ids, n_rows, s);
+      c->row_sizes.upload(row_sizes, n_rows, s);
+      c->row_acc.upload(row_acc, n_rows, s);
+      c->inh.upload(inhomogeneities, n_rows, s);
+    }
+    if (nnz) {
+      c->col_ids.upload(col_ids, nnz, s);
+      c->col_vals.upload(col_values, nnz, s);
+    }
+    c->is_row.upload(is_row.data(), N, s);
+    if (!c->pure_dirichlet) {
+      c->par_ptr.upload(cnt.data(), N + 1, s);
+      if (tnnz) {
+        c->par_row.upload(prow.data(), tnnz, s);
+        c->par_w.upload(pw.data(), tnnz, s);
+      } else {
+        c->par_row.alloc(1);
+        c->par_w.alloc(1);
+      }
+    }
+    GBFE_CUDA(cudaStreamSynchronize(s));
+  });
+  if (rc != GBFE_OK) {
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return GBFE_OK;
+}
+
+int gbfe_constraints_destroy(gbfe_cons *cons) {
+  if (!cons) return GBFE_OK;
+  cudaStreamSynchronize(cons->mesh->ctx->stream);
+  delete cons;
+  return GBFE_OK;
+}
+
+int gbfe_constraints_distribute_parent_to_child(const gbfe_cons *cons, gbfe_mv *x) {
+  if (!cons || !x) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = cons->mesh->ctx;
+  return gbfe_guard(ctx, [&] {
+    GBFE_REQUIRE(x->mesh == cons->mesh, "p2c: vector on another mesh");
+    constraints_p2c(ctx, cons, x);
+  });
+}
+
+int gbfe_constraints_distribute_child_to_parent(const gbfe_cons *cons, gbfe_mv *x) {
+  if (!cons || !x) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = cons->mesh->ctx;
+  return gbfe_guard(ctx, [&] {
+    GBFE_REQUIRE(x->mesh == cons->mesh, "c2p: vector on another mesh");
+    constraints_c2p(ctx, cons, x);
+  });
+}
+
+int gbfe_cellmat_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *mats, int prec_flags, gbfe_op **out) {
+  if (!mesh || !out) return GBFE_ERR_ARG;
+  *out = nullptr;
+  gbfe_op *op = nullptr;
+  int rc = gbfe_guard(mesh->ctx, [&] {
+    GBFE_REQUIRE(mats, "cellmat_upload: null matrices");
+    GBFE_REQUIRE(!cons || cons->mesh == mesh, "cellmat_upload: constraints on another mesh");
+    op = new gbfe_op();
+    op->mesh = mesh;
+    op->cons = cons;
+    op->kind = OP_CELL;
+    op->prec = prec_flags | GBFE_PREC_FP64;
+    op->mats.upload(mats, mesh->total_mat, mesh->ctx->stream);
+    if (prec_flags & GBFE_PREC_MIXED) build_mixed_mats(op);
+    GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
+  });
+  if (rc != GBFE_OK) {
+    delete op;
+    return rc;
+  }
+  *out = op;
+  return GBFE_OK;
+}
+
+static int diag_upload_impl(gbfe_mesh *mesh, const gbfe_cons *cons, const double *diag, int kind, gbfe_op **out) {
+  if (!mesh || !out) return GBFE_ERR_ARG;
+  *out = nullptr;
+  gbfe_op *op = nullptr;
+  int rc = gbfe_guard(mesh->ctx, [&] {
+    GBFE_REQUIRE(diag, "diag_upload: null diagonal");
+    GBFE_REQUIRE(!cons || cons->mesh == mesh, "diag_upload: constraints on another mesh");
+    op = new gbfe_op();
+    op->mesh = mesh;
+    op->cons = cons;
+    op->kind = kind;
+    if (kind == OP_JACOBI) {
+      std::vector<double> inv(mesh->n_dofs);
+      for (uint64_t i = 0; i < mesh->n_dofs; ++i) inv[i] = 1.0 / diag[i];
+      op->diag.upload(inv.data(), mesh->n_dofs, mesh->ctx->stream);
+      GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
+    } else {
+      op->diag.upload(diag, mesh->n_dofs, mesh->ctx->stream);
+      GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
+    }
+  });
+  if (rc != GBFE_OK) {
+    delete op;
+    return rc;
+  }
+  *out = op;
+  return GBFE_OK;
+}
+
+int gbfe_diag_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *diag, gbfe_op **out) {
+  return diag_upload_impl(mesh, cons, diag, OP_DIAG, out);
+}
+
+int gbfe_jacobi_upload(gbfe_mesh *mesh, const double *diagonal, gbfe_op **out) {
+  return diag_upload_impl(mesh, nullptr, diagonal, OP_JACOBI, out);
+}
+
+int gbfe_op_destroy(gbfe_op *op) {
+  if (!op) return GBFE_OK;
+  cudaStreamSynchronize(op->mesh->ctx->stream);
+  delete op;
+  return GBFE_OK;
+}
+
+int gbfe_mv_create(gbfe_mesh *mesh, uint32_t m, int dtype, gbfe_mv **out) {
+  if (!mesh || !out) return GBFE_ERR_ARG;
+  *out = nullptr;
+  gbfe_mv *mv = nullptr;
+  int rc = gbfe_guard(mesh->ctx, [&] {
+    GBFE_REQUIRE(dtype == GBFE_F64 || dtype == GBFE_F32, "mv_create: dtype must be GBFE_F64 or GBFE_F32");
+    mv = new gbfe_mv();
+    mv->mesh = mesh;
+    mv->m = m;
+    mv->dtype = dtype;
+    const size_t n = mv->count();
+    if (dtype == GBFE_F64) {
+      mv->d.alloc(n);
+      if (n) GBFE_CUDA(cudaMemsetAsync(mv->d.p, 0, n * 8, mesh->ctx->stream));
+    } else {
+      mv->f.alloc(n);
+      if (n) GBFE_CUDA(cudaMemsetAsync(mv->f.p, 0, n * 4, mesh->ctx->stream));
+    }
+  });
+  if (rc != GBFE_OK) {
+    delete mv;
+    return rc;
+  }
+  *out = mv;
+  return GBFE_OK;
+}
+
+int gbfe_mv_destroy(gbfe_mv *mv) {
+  if (!mv) return GBFE_OK;
+  cudaStreamSynchronize(mv->mesh->ctx->stream);
+  delete mv;
+  return GBFE_OK;
+}
+
+int gbfe_mv_copy_in(gbfe_mv *mv, const void *host) {
+  if (!mv || !host) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = mv->mesh->ctx;
+  return gbfe_guard(ctx, [&] {
+    const size_t bytes = mv->count() * (mv->dtype == GBFE_F64 ? 8 : 4);
+    if (bytes) GBFE_CUDA(cudaMemcpyAsync(mv->ptr(), host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int gbfe_mv_copy_out(const gbfe_mv *mv, void *host) {
+  if (!mv || !host) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = mv->mesh->ctx;
+  return gbfe_guard(ctx, [&] {
+    const size_t bytes = mv->count() * (mv->dtype == GBFE_F64 ? 8 : 4);
+    if (bytes) GBFE_CUDA(cudaMemcpyAsync(host, mv->ptr(), bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int gbfe_mv_copy(const gbfe_mv *src, gbfe_mv *dst) {
+  if (!src || !dst) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = src->mesh->ctx;
+  return gbfe_guard(ctx, [&] {
+    GBFE_REQUIRE(src->mesh == dst->mesh && src->m == dst->m, "mv_copy: shape mismatch");
+    convert_mv(ctx, src, dst);
+  });
+}
+
+int gbfe_mv_set_value(gbfe_mv *mv, double value) {
+  if (!mv) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = mv->mesh->ctx;
+  return gbfe_guard(ctx, [&] { fill_mv(ctx, mv, value); });
+}
+
+int gbfe_mv_device_ptr(const gbfe_mv *mv, void **ptr) {
+  if (!mv || !ptr) return GBFE_ERR_ARG;
+  *ptr = mv->ptr();
+  return GBFE_OK;
+}
+
+int gbfe_apply(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
+  if (!op || !X || !Y) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = op->mesh->ctx;
+  return gbfe_guard(ctx, [&] { apply_op(op, X, Y); });
+}
+
+}  // extern "C"

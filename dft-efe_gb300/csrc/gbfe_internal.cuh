@@ -1,0 +1,217 @@
+// gbfe_internal.cuh -- device-resident state behind the C ABI in include/gbfe.h.
+//
+// HBM layout (all device buffers owned by the handle that created them):
+//   mesh:  ids[sum nd]        cell-major cell->dof ids (uint32)
+//          cell_off[C+1]      prefix sum of nd (uint32)
+//          mat_off[C+1]       prefix sum of nd^2 (uint64)
+//          slot_ptr[N+1], slot[sum nd]
+//                             dof -> cell-slot transpose, slots of a dof in
+//                             ascending (cell, local index) order, which is the
+//                             order the reference's serial scatter adds them
+//                             (FECellWiseDataOperations.t.cpp:87-151)
+//   cons:  the reference CSR arrays + the column->row transpose
+//          par_ptr[N+1], par_row[nnz], par_w[nnz] (rows of each parent column in
+//          ascending constraint-row order, the order distributeChildToParent
+//          adds them) + is_row[N] flags
+//   op:    mats f64[sum nd^2] col-major per cell; optional split-BF16 hi/lo
+//          copies; or diag f64[N]
+//   mv:    data[N][m] row-major, vector index fastest
+#pragma once
+#include <cuda_runtime.h>
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+#include <cuda_bf16.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include <stdexcept>
+
+#include "../../include/gbfe.h"
+
+namespace gbfe {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define GBFE_CUDA(call)                                                                      \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      throw ::gbfe::Error(e_ == cudaErrorMemoryAllocation ? GBFE_ERR_ALLOC : GBFE_ERR_CUDA,  \
+                          std::string(#call) + ": " + cudaGetErrorString(e_));               \
+  } while (0)
+
+#define GBFE_CUBLAS(call)                                                                    \
+  do {                                                                                       \
+    cublasStatus_t s_ = (call);                                                              \
+    if (s_ != CUBLAS_STATUS_SUCCESS)                                                         \
+      throw ::gbfe::Error(GBFE_ERR_CUDA, std::string(#call) + ": cublas status " +           \
+                                             std::to_string((int)s_));                      \
+  } while (0)
+
+#define GBFE_CUSOLVER(call)                                                                  \
+  do {                                                                                       \
+    cusolverStatus_t s_ = (call);                                                            \
+    if (s_ != CUSOLVER_STATUS_SUCCESS)                                                       \
+      throw ::gbfe::Error(GBFE_ERR_CUDA, std::string(#call) + ": cusolver status " +         \
+                                             std::to_string((int)s_));                      \
+  } while (0)
+
+#define GBFE_REQUIRE(cond, msg)                                                              \
+  do {                                                                                       \
+    if (!(cond)) throw ::gbfe::Error(GBFE_ERR_ARG, msg);                                     \
+  } while (0)
+
+// owning device buffer
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count == n && p) return;
+    reset();
+    if (count) GBFE_CUDA(cudaMalloc(&p, sizeof(T) * count));
+    n = count;
+  }
+  // grow-only scratch
+  void ensure(size_t count) {
+    if (count > n) alloc(count);
+  }
+  void upload(const T *h, size_t count, cudaStream_t s) {
+    alloc(count);
+    if (count) GBFE_CUDA(cudaMemcpyAsync(p, h, sizeof(T) * count, cudaMemcpyHostToDevice, s));
+  }
+};
+
+}  // namespace gbfe
+
+struct gbfe_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  cublasHandle_t cublas = nullptr;
+  cusolverDnHandle_t cusolver = nullptr;
+  std::string last_error;
+  uint64_t launches = 0;
+  int sm_count = 0;
+  // shared scratch
+  gbfe::DBuf<double> red;    // reduction partials
+  gbfe::DBuf<double> small;  // m x m work matrices
+  gbfe::DBuf<int> info;
+  gbfe::DBuf<double> lwork;
+};
+
+struct gbfe_mesh {
+  gbfe_ctx *ctx = nullptr;
+  uint64_t n_dofs = 0;
+  uint32_t n_cells = 0;
+  uint32_t nd_max = 0;
+  uint32_t nd_min = 0;
+  uint64_t total_cell_dofs = 0;  // sum nd
+  uint64_t total_mat = 0;        // sum nd^2
+  std::vector<uint32_t> h_nd;
+  std::vector<uint32_t> h_cell_off;
+  std::vector<uint64_t> h_mat_off;
+  gbfe::DBuf<uint32_t> ids, cell_off, slot_ptr, slot, nd;
+  gbfe::DBuf<uint64_t> mat_off;
+  // size bins for variable-nd meshes: cells sorted by nd, grouped
+  std::vector<uint32_t> bin_nd;       // nd of each bin
+  std::vector<uint32_t> bin_begin;    // offset into bin_cells
+  gbfe::DBuf<uint32_t> bin_cells;     // cell ids grouped by bin
+};
+
+struct gbfe_cons {
+  gbfe_mesh *mesh = nullptr;
+  uint32_t n_rows = 0;
+  uint64_t nnz = 0;
+  bool pure_dirichlet = true;  // every row has 0 columns and 0 inhomogeneity
+  gbfe::DBuf<uint32_t> row_ids, row_sizes, col_ids, row_acc;
+  gbfe::DBuf<double> col_vals, inh;
+  gbfe::DBuf<uint32_t> par_ptr, par_row;
+  gbfe::DBuf<double> par_w;
+  gbfe::DBuf<uint8_t> is_row;
+};
+
+enum OpKind { OP_CELL = 0, OP_DIAG = 1, OP_JACOBI = 2 };
+
+struct gbfe_op {
+  gbfe_mesh *mesh = nullptr;
+  const gbfe_cons *cons = nullptr;
+  int kind = OP_CELL;
+  int prec = GBFE_PREC_FP64;
+  gbfe::DBuf<double> mats;            // f64 col-major per cell
+  gbfe::DBuf<__nv_bfloat16> mats_hi;  // split-BF16 high part, tile layout
+  gbfe::DBuf<__nv_bfloat16> mats_lo;  // split-BF16 low part
+  gbfe::DBuf<float> mats_f32;         // FP32 copy for the SIMT mixed apply
+  gbfe::DBuf<double> diag;
+  mutable gbfe::DBuf<double> cellbuf;  // per-apply cell-wise result scratch (f64)
+  mutable gbfe::DBuf<float> cellbuf_f32;
+};
+
+struct gbfe_mv {
+  gbfe_mesh *mesh = nullptr;
+  uint32_t m = 0;
+  int dtype = GBFE_F64;
+  gbfe::DBuf<double> d;
+  gbfe::DBuf<float> f;
+  size_t count() const { return (size_t)mesh->n_dofs * m; }
+  void *ptr() const { return dtype == GBFE_F64 ? (void *)d.p : (void *)f.p; }
+};
+
+namespace gbfe {
+
+inline unsigned grid_for(uint64_t n, unsigned block) {
+  uint64_t g = (n + block - 1) / block;
+  if (g > 0x7fffffffULL) g = 0x7fffffffULL;
+  return (unsigned)(g ? g : 1);
+}
+
+inline void count_launch(gbfe_ctx *ctx, uint64_t n = 1) { ctx->launches += n; }
+inline void check_launch(gbfe_ctx *ctx, const char *name) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw Error(GBFE_ERR_CUDA, std::string(name) + ": " + cudaGetErrorString(e));
+  count_launch(ctx);
+}
+
+// ---- internal entry points shared between translation units
+void constraints_p2c(gbfe_ctx *ctx, const gbfe_cons *c, gbfe_mv *x);
+void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
+void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
+void build_mixed_mats(gbfe_op *op);
+
+// vector kernels (solvers)
+void axpby(gbfe_ctx *ctx, size_t n, double a, const gbfe_mv *x, double b, const gbfe_mv *y, gbfe_mv *z);
+void col_dots(gbfe_ctx *ctx, const gbfe_mv *x, const gbfe_mv *y, double *host_out);
+
+}  // namespace gbfe
+
+// catch-all wrapper for the C ABI
+template <class F>
+static inline int gbfe_guard(gbfe_ctx *ctx, F &&f) {
+  try {
+    f();
+    return GBFE_OK;
+  } catch (const gbfe::Error &e) {
+    if (ctx) ctx->last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    if (ctx) ctx->last_error = "host allocation failed";
+    return GBFE_ERR_ALLOC;
+  } catch (const std::exception &e) {
+    if (ctx) ctx->last_error = e.what();
+    return GBFE_ERR_ARG;
+  }
+}

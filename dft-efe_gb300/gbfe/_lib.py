@@ -1,0 +1,113 @@
+"""ctypes binding of libgbfe.so (the C ABI declared in include/gbfe.h).
+
+There is no fallback: if the CUDA library is missing or cannot be loaded the
+import of the compute API fails with a clear error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libgbfe.so"
+
+GBFE_OK = 0
+STATUS_NAMES = {
+    0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_ALLOC", 4: "ERR_NOT_ORTHONORMALIZABLE",
+    5: "ERR_LAPACK", 6: "ERR_NOT_CONVERGED", 7: "ERR_DIVERGED", 8: "ERR_TIMEOUT", 9: "ERR_CANCELLED",
+}
+GBFE_F64, GBFE_F32 = 0, 1
+GBFE_PREC_FP64, GBFE_PREC_MIXED = 1, 2
+
+p = C.c_void_p
+u32, u64, i32, f64 = C.c_uint32, C.c_uint64, C.c_int, C.c_double
+pu32, pf64 = C.POINTER(C.c_uint32), C.POINTER(C.c_double)
+
+
+class KSParams(C.Structure):
+    _fields_ = [
+        ("degree", u32), ("max_passes", u32), ("n_wanted", u32), ("filter_precision", i32),
+        ("residual_tol", f64), ("wanted_lower", f64), ("wanted_upper", f64), ("unwanted_upper", f64),
+        ("use_lanczos", i32), ("lanczos_steps", u32), ("lanczos_seed", u64), ("fixed_passes", i32),
+    ]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "gbfe_ctx_create": (i32, [i32, C.POINTER(p)]),
+    "gbfe_ctx_destroy": (i32, [p]),
+    "gbfe_last_error": (i32, [p, C.c_char_p, C.c_size_t]),
+    "gbfe_ctx_set_stream": (i32, [p, p]),
+    "gbfe_ctx_synchronize": (i32, [p]),
+    "gbfe_ctx_kernel_launches": (i32, [p, C.POINTER(u64)]),
+    "gbfe_mesh_upload": (i32, [p, u32, p, p, u64, C.POINTER(p)]),
+    "gbfe_mesh_destroy": (i32, [p]),
+    "gbfe_constraints_upload": (i32, [p, u32, p, p, p, p, p, p, C.POINTER(p)]),
+    "gbfe_constraints_destroy": (i32, [p]),
+    "gbfe_constraints_distribute_parent_to_child": (i32, [p, p]),
+    "gbfe_constraints_distribute_child_to_parent": (i32, [p, p]),
+    "gbfe_cellmat_upload": (i32, [p, p, p, i32, C.POINTER(p)]),
+    "gbfe_diag_upload": (i32, [p, p, p, C.POINTER(p)]),
+    "gbfe_jacobi_upload": (i32, [p, p, C.POINTER(p)]),
+    "gbfe_op_destroy": (i32, [p]),
+    "gbfe_mv_create": (i32, [p, u32, i32, C.POINTER(p)]),
+    "gbfe_mv_destroy": (i32, [p]),
+    "gbfe_mv_copy_in": (i32, [p, p]),
+    "gbfe_mv_copy_out": (i32, [p, p]),
+    "gbfe_mv_copy": (i32, [p, p]),
+    "gbfe_mv_set_value": (i32, [p, f64]),
+    "gbfe_mv_device_ptr": (i32, [p, C.POINTER(p)]),
+    "gbfe_mv_l2_norms": (i32, [p, p]),
+    "gbfe_mv_dots": (i32, [p, p, p]),
+    "gbfe_apply": (i32, [p, p, p]),
+    "gbfe_residual_chebyshev_filter": (i32, [p, p, p, p, p, u32, f64, f64, f64, i32, p]),
+    "gbfe_chebyshev_filter": (i32, [p, p, p, u32, f64, f64, f64, p]),
+    "gbfe_cholesky_gram_schmidt": (i32, [p, p, p]),
+    "gbfe_rayleigh_ritz": (i32, [p, p, p, p]),
+    "gbfe_eigen_residual_norms": (i32, [p, p, p, p, p]),
+    "gbfe_chfsi_pass": (i32, [p, p, p, p, p, u32, f64, f64, f64, i32]),
+    "gbfe_ks_eigen_solve": (i32, [p, p, p, p, C.POINTER(KSParams), p, p, C.POINTER(u32)]),
+    "gbfe_lanczos_bounds": (i32, [p, p, p, u32, u64, p]),
+    "gbfe_cg_solve": (i32, [p, p, p, p, u32, f64, f64, f64, C.POINTER(u32), p]),
+}
+
+_lib = None
+
+
+def exported_symbols() -> list[str]:
+    return list(SIGNATURES)
+
+
+def load(path: Path | None = None) -> C.CDLL:
+    """Load libgbfe.so and declare every entry point.  Raises if it is absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    lp = Path(path) if path else LIB_PATH
+    if not lp.exists():
+        raise ImportError(f"libgbfe.so not built at {lp}; run gbfe.build.build() (no CPU fallback exists)")
+    lib = C.CDLL(str(lp))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class GBFEError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+        self.status = STATUS_NAMES.get(code, str(code))
+
+
+def check(rc: int, ctx_handle=None, what: str = "") -> None:
+    if rc == GBFE_OK:
+        return
+    msg = what
+    if ctx_handle:
+        buf = C.create_string_buffer(1024)
+        load().gbfe_last_error(ctx_handle, buf, 1024)
+        msg = f"{what}: {buf.value.decode(errors='replace')}"
+    raise GBFEError(rc, msg)

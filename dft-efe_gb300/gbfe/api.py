@@ -1,0 +1,354 @@
+"""Host-side mirror of the reference operator / solver interface on top of the
+C ABI.  Class and method names follow dft-efe so that calling code reads like
+the reference's own:
+
+=============================================  ==========================================================
+this module                                    reference
+=============================================  ==========================================================
+``LinAlgOpContext``                            ``linearAlgebra/LinAlgOpContext.h:148-176``
+``FEBasisManager``                             ``basis/FEBasisManager.h`` (cell->dof map + constraints)
+``MultiVector``                                ``linearAlgebra/MultiVector.h:133`` ([N][m], vector fastest)
+``KohnShamOperatorContextFE.apply``            ``ksdft/KohnShamOperatorContextFE.t.cpp:1326-1443``
+``CFEOverlapOperatorContext.apply``            ``basis/CFEOverlapOperatorContext.t.cpp:539-641``
+``CFEOverlapInverseOpContextGLL.apply``        ``basis/CFEOverlapInverseOpContextGLL.t.cpp:499-560``
+``LaplaceOperatorContextFE.apply``             ``electrostatics/LaplaceOperatorContextFE.t.cpp:397-467``
+``PreconditionerJacobi.apply``                 ``linearAlgebra/PreconditionerJacobi.t.cpp:56-80``
+``ResidualChebyshevFilterGEP``                 ``linearAlgebra/ChebyshevFilter.t.cpp:242-444``
+``ChebyshevFilter``                            ``linearAlgebra/ChebyshevFilter.t.cpp:39-135``
+``OrthonormalizationFunctions``                ``linearAlgebra/OrthonormalizationFunctions.t.cpp:153-431``
+``RayleighRitzEigenSolver``                    ``linearAlgebra/RayleighRitzEigenSolver.t.cpp:67-302``
+``ChebyshevFilteredEigenSolver``               ``linearAlgebra/ChebyshevFilteredEigenSolver.t.cpp:194-437``
+``KohnShamEigenSolver``                        ``ksdft/KohnShamEigenSolver.t.cpp:214-684``
+``CGLinearSolver``                             ``linearAlgebra/CGLinearSolver.t.cpp:68-313``
+=============================================  ==========================================================
+
+Every compute call goes to libgbfe.so on the GPU; nothing here computes on the
+CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import GBFE_F32, GBFE_F64, GBFE_PREC_FP64, GBFE_PREC_MIXED, GBFEError, KSParams, check
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class LinAlgOpContext:
+    """One CUDA device, one stream, cuBLAS/cuSOLVER handles."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        rc = self.lib.gbfe_ctx_create(device, C.byref(h))
+        if rc != 0:
+            raise GBFEError(rc, f"gbfe_ctx_create(device={device}) failed")
+        self.h = h
+
+    def synchronize(self) -> None:
+        check(self.lib.gbfe_ctx_synchronize(self.h), self.h, "synchronize")
+
+    def kernel_launches(self) -> int:
+        n = C.c_uint64()
+        check(self.lib.gbfe_ctx_kernel_launches(self.h, C.byref(n)), self.h, "launch count")
+        return int(n.value)
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(self.lib.gbfe_ctx_set_stream(self.h, C.c_void_p(stream_ptr or 0)), self.h, "set_stream")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.gbfe_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class FEBasisManager:
+    """Cell->dof map and constraints on the device."""
+
+    def __init__(self, ctx: LinAlgOpContext, nd_per_cell: np.ndarray, cell_dof_ids: np.ndarray, n_dofs: int,
+                 constraints=None):
+        self.ctx = ctx
+        lib = ctx.lib
+        self._nd = np.ascontiguousarray(nd_per_cell, dtype=np.uint32)
+        self._ids = np.ascontiguousarray(cell_dof_ids, dtype=np.uint32)
+        self.n_dofs = int(n_dofs)
+        self.n_cells = int(self._nd.size)
+        h = C.c_void_p()
+        check(lib.gbfe_mesh_upload(ctx.h, self.n_cells, _ptr(self._nd), _ptr(self._ids), self.n_dofs, C.byref(h)),
+              ctx.h, "mesh_upload")
+        self.h = h
+        self.cons_h = None
+        if constraints is not None:
+            self.set_constraints(constraints)
+
+    @classmethod
+    def from_problem(cls, ctx: LinAlgOpContext, prob) -> "FEBasisManager":
+        return cls(ctx, prob.nd_per_cell, prob.cell_dof_ids, prob.n_dofs, prob.constraints)
+
+    def set_constraints(self, cons) -> None:
+        lib = self.ctx.lib
+        arrs = [np.ascontiguousarray(a, dtype=t) for a, t in (
+            (cons.row_ids, np.uint32), (cons.row_sizes, np.uint32), (cons.col_ids, np.uint32),
+            (cons.row_acc, np.uint32), (cons.col_values, np.float64), (cons.inhomogeneities, np.float64))]
+        self._cons_arrays = arrs
+        h = C.c_void_p()
+        check(lib.gbfe_constraints_upload(self.h, int(arrs[0].size), *[_ptr(a) for a in arrs], C.byref(h)),
+              self.ctx.h, "constraints_upload")
+        self.cons_h = h
+
+    def distributeParentToChild(self, X: "MultiVector") -> None:
+        check(self.ctx.lib.gbfe_constraints_distribute_parent_to_child(self.cons_h, X.h), self.ctx.h, "p2c")
+
+    def distributeChildToParent(self, X: "MultiVector") -> None:
+        check(self.ctx.lib.gbfe_constraints_distribute_child_to_parent(self.cons_h, X.h), self.ctx.h, "c2p")
+
+
+class MultiVector:
+    """Device block vector, row-major [n_dofs][m] (vector index fastest)."""
+
+    def __init__(self, basis: FEBasisManager, num_vectors: int, dtype=np.float64, init: Optional[np.ndarray] = None):
+        self.basis = basis
+        self.ctx = basis.ctx
+        self.m = int(num_vectors)
+        self.dtype = np.dtype(dtype)
+        code = GBFE_F64 if self.dtype == np.float64 else GBFE_F32
+        if self.dtype not in (np.float64, np.float32):
+            raise ValueError("MultiVector dtype must be float64 or float32")
+        h = C.c_void_p()
+        check(self.ctx.lib.gbfe_mv_create(basis.h, self.m, code, C.byref(h)), self.ctx.h, "mv_create")
+        self.h = h
+        if init is not None:
+            self.copy_from(init)
+
+    @property
+    def shape(self):
+        return (self.basis.n_dofs, self.m)
+
+    def copy_from(self, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=self.dtype).reshape(self.shape)
+        check(self.ctx.lib.gbfe_mv_copy_in(self.h, _ptr(a)), self.ctx.h, "mv_copy_in")
+
+    def numpy(self) -> np.ndarray:
+        out = np.empty(self.shape, dtype=self.dtype)
+        check(self.ctx.lib.gbfe_mv_copy_out(self.h, _ptr(out)), self.ctx.h, "mv_copy_out")
+        return out
+
+    def copy_to(self, other: "MultiVector") -> None:
+        check(self.ctx.lib.gbfe_mv_copy(self.h, other.h), self.ctx.h, "mv_copy")
+
+    def setValue(self, v: float) -> None:
+        check(self.ctx.lib.gbfe_mv_set_value(self.h, float(v)), self.ctx.h, "mv_set_value")
+
+    def l2Norms(self) -> np.ndarray:
+        out = np.empty(self.m)
+        check(self.ctx.lib.gbfe_mv_l2_norms(self.h, _ptr(out)), self.ctx.h, "l2Norms")
+        return out
+
+    def dot(self, other: "MultiVector") -> np.ndarray:
+        out = np.empty(self.m)
+        check(self.ctx.lib.gbfe_mv_dots(self.h, other.h, _ptr(out)), self.ctx.h, "dots")
+        return out
+
+    def device_ptr(self) -> int:
+        v = C.c_void_p()
+        check(self.ctx.lib.gbfe_mv_device_ptr(self.h, C.byref(v)), self.ctx.h, "device_ptr")
+        return int(v.value or 0)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.ctx.lib.gbfe_mv_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OperatorContext:
+    """``apply(X, Y, updateGhostX=False, updateGhostY=False)``; ghosts are no-ops on one GPU."""
+
+    h = None
+    ctx: LinAlgOpContext
+
+    def apply(self, X: MultiVector, Y: MultiVector, updateGhostX: bool = False, updateGhostY: bool = False) -> None:
+        check(self.ctx.lib.gbfe_apply(self.h, X.h, Y.h), self.ctx.h, "apply")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.ctx.lib.gbfe_op_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CellMatrixOperatorContext(OperatorContext):
+    def __init__(self, basis: FEBasisManager, cell_matrices: np.ndarray, mixed: bool = False,
+                 use_constraints: bool = True):
+        self.basis, self.ctx = basis, basis.ctx
+        mats = np.ascontiguousarray(cell_matrices, dtype=np.float64)
+        h = C.c_void_p()
+        flags = GBFE_PREC_FP64 | (GBFE_PREC_MIXED if mixed else 0)
+        cons = basis.cons_h if use_constraints else None
+        check(self.ctx.lib.gbfe_cellmat_upload(basis.h, cons, _ptr(mats), flags, C.byref(h)), self.ctx.h,
+              "cellmat_upload")
+        self.h = h
+        self.mixed = mixed
+
+
+class KohnShamOperatorContextFE(CellMatrixOperatorContext):
+    """H = sum over cells of the Hamiltonian cell matrices (local part)."""
+
+
+class CFEOverlapOperatorContext(CellMatrixOperatorContext):
+    """Consistent (Gauss) overlap M."""
+
+
+class LaplaceOperatorContextFE(CellMatrixOperatorContext):
+    """K = int grad N_i . grad N_j."""
+
+
+class CFEOverlapInverseOpContextGLL(OperatorContext):
+    """Y = M_GLL^{-1} X with constraints; takes the assembled GLL-lumped diagonal."""
+
+    def __init__(self, basis: FEBasisManager, m_gll_diagonal: np.ndarray):
+        self.basis, self.ctx = basis, basis.ctx
+        inv = np.ascontiguousarray(1.0 / np.asarray(m_gll_diagonal, dtype=np.float64))
+        h = C.c_void_p()
+        check(self.ctx.lib.gbfe_diag_upload(basis.h, basis.cons_h, _ptr(inv), C.byref(h)), self.ctx.h, "diag_upload")
+        self.h = h
+
+
+class DiagonalOperatorContext(OperatorContext):
+    """Y = d o X with constraints (lumped overlap or any diagonal operator)."""
+
+    def __init__(self, basis: FEBasisManager, diagonal: np.ndarray, use_constraints: bool = True):
+        self.basis, self.ctx = basis, basis.ctx
+        d = np.ascontiguousarray(diagonal, dtype=np.float64)
+        h = C.c_void_p()
+        check(self.ctx.lib.gbfe_diag_upload(basis.h, basis.cons_h if use_constraints else None, _ptr(d), C.byref(h)),
+              self.ctx.h, "diag_upload")
+        self.h = h
+
+
+class PreconditionerJacobi(OperatorContext):
+    """Y = diag^{-1} o X (no constraints), reciprocal taken from ``diagonal``."""
+
+    def __init__(self, basis: FEBasisManager, diagonal: np.ndarray):
+        self.basis, self.ctx = basis, basis.ctx
+        d = np.ascontiguousarray(diagonal, dtype=np.float64)
+        h = C.c_void_p()
+        check(self.ctx.lib.gbfe_jacobi_upload(basis.h, _ptr(d), C.byref(h)), self.ctx.h, "jacobi_upload")
+        self.h = h
+
+
+def ResidualChebyshevFilterGEP(A, B, BInv, eigenvalues: Sequence[float], X: MultiVector, polynomialDegree: int,
+                               wantedSpectrumLowerBound: float, wantedSpectrumUpperBound: float,
+                               unWantedSpectrumUpperBound: float, Y: MultiVector, mixed: bool = False) -> None:
+    ev = np.ascontiguousarray(eigenvalues, dtype=np.float64)
+    check(A.ctx.lib.gbfe_residual_chebyshev_filter(A.h, B.h, BInv.h, _ptr(ev), X.h, int(polynomialDegree),
+                                                   float(wantedSpectrumLowerBound), float(wantedSpectrumUpperBound),
+                                                   float(unWantedSpectrumUpperBound),
+                                                   GBFE_F32 if mixed else GBFE_F64, Y.h), A.ctx.h, "residual filter")
+
+
+def ChebyshevFilter(A, BInv, eigenSubspaceGuess: MultiVector, polynomialDegree: int, wantedSpectrumLowerBound: float,
+                    wantedSpectrumUpperBound: float, unWantedSpectrumUpperBound: float,
+                    filteredSubspace: MultiVector) -> None:
+    check(A.ctx.lib.gbfe_chebyshev_filter(A.h, BInv.h, eigenSubspaceGuess.h, int(polynomialDegree),
+                                          float(wantedSpectrumLowerBound), float(wantedSpectrumUpperBound),
+                                          float(unWantedSpectrumUpperBound), filteredSubspace.h), A.ctx.h, "filter")
+
+
+class OrthonormalizationFunctions:
+    @staticmethod
+    def CholeskyGramSchmidt(X: MultiVector, orthogonalizedX: MultiVector, B) -> None:
+        check(B.ctx.lib.gbfe_cholesky_gram_schmidt(B.h, X.h, orthogonalizedX.h), B.ctx.h, "CholeskyGramSchmidt")
+
+
+class RayleighRitzEigenSolver:
+    @staticmethod
+    def solve(A, X: MultiVector, eigenVectors: MultiVector) -> np.ndarray:
+        ev = np.empty(X.m)
+        check(A.ctx.lib.gbfe_rayleigh_ritz(A.h, X.h, _ptr(ev), eigenVectors.h), A.ctx.h, "RayleighRitz")
+        return ev
+
+
+def eigen_residual_norms(A, B, X: MultiVector, eigenvalues) -> np.ndarray:
+    ev = np.ascontiguousarray(eigenvalues, dtype=np.float64)
+    out = np.empty(X.m)
+    check(A.ctx.lib.gbfe_eigen_residual_norms(A.h, B.h, X.h, _ptr(ev), _ptr(out)), A.ctx.h, "residual norms")
+    return out
+
+
+class ChebyshevFilteredEigenSolver:
+    def __init__(self, wantedSpectrumLowerBound: float, wantedSpectrumUpperBound: float,
+                 unWantedSpectrumUpperBound: float, polynomialDegree: int, mixed: bool = False):
+        self.wl, self.wu, self.uu = wantedSpectrumLowerBound, wantedSpectrumUpperBound, unWantedSpectrumUpperBound
+        self.degree, self.mixed = int(polynomialDegree), mixed
+
+    def solve(self, A, eigenValues: np.ndarray, eigenVectors: MultiVector, B, BInv) -> np.ndarray:
+        ev = np.ascontiguousarray(eigenValues, dtype=np.float64).copy()
+        check(A.ctx.lib.gbfe_chfsi_pass(A.h, B.h, BInv.h, eigenVectors.h, _ptr(ev), self.degree, self.wl, self.wu,
+                                        self.uu, GBFE_F32 if self.mixed else GBFE_F64), A.ctx.h, "chfsi pass")
+        return ev
+
+
+def lanczos_bounds(A, B, BInv, steps: int = 20, seed: int = 7) -> np.ndarray:
+    out = np.empty(3)
+    check(A.ctx.lib.gbfe_lanczos_bounds(A.h, B.h, BInv.h, int(steps), int(seed), _ptr(out)), A.ctx.h, "lanczos")
+    return out
+
+
+class KohnShamEigenSolver:
+    def __init__(self, n_wanted: int, degree: int, max_passes: int, residual_tol: float = 1e-6, mixed: bool = False,
+                 bounds: Optional[Sequence[float]] = None, lanczos_steps: int = 20, lanczos_seed: int = 7,
+                 fixed_passes: bool = False):
+        self.p = KSParams()
+        self.p.degree, self.p.max_passes, self.p.n_wanted = int(degree), int(max_passes), int(n_wanted)
+        self.p.filter_precision = GBFE_F32 if mixed else GBFE_F64
+        self.p.residual_tol = float(residual_tol)
+        if bounds is not None:
+            self.p.use_lanczos = 0
+            self.p.wanted_lower, self.p.wanted_upper, self.p.unwanted_upper = map(float, bounds)
+        else:
+            self.p.use_lanczos = 1
+        self.p.lanczos_steps, self.p.lanczos_seed = int(lanczos_steps), int(lanczos_seed)
+        self.p.fixed_passes = 1 if fixed_passes else 0
+
+    def solve(self, H, X: MultiVector, M, MInv, eigenvalues: Optional[np.ndarray] = None):
+        ev = np.zeros(X.m) if eigenvalues is None else np.ascontiguousarray(eigenvalues, dtype=np.float64).copy()
+        res = np.empty(X.m)
+        passes = C.c_uint32()
+        rc = H.ctx.lib.gbfe_ks_eigen_solve(H.h, M.h, MInv.h, X.h, C.byref(self.p), _ptr(ev), _ptr(res),
+                                           C.byref(passes))
+        return rc, ev, res, int(passes.value)
+
+
+class CGLinearSolver:
+    def __init__(self, maxIter: int, absoluteTol: float, relativeTol: float, divergenceTol: float):
+        self.maxIter, self.absTol, self.relTol, self.divTol = int(maxIter), absoluteTol, relativeTol, divergenceTol
+
+    def solve(self, A, PC, b: MultiVector, x: MultiVector):
+        iters = C.c_uint32()
+        rn = np.empty(b.m)
+        rc = A.ctx.lib.gbfe_cg_solve(A.h, PC.h, b.h, x.h, self.maxIter, float(self.absTol), float(self.relTol),
+                                     float(self.divTol), C.byref(iters), _ptr(rn))
+        return rc, int(iters.value), rn

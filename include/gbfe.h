@@ -1,0 +1,211 @@
+/*
+ * gbfe.h -- C ABI of the GB300 FE-operator / ChFSI library (libgbfe.so).
+ *
+ * One process, one GPU.  Every entry point returns an int status
+ * (GBFE_OK == 0); the message of the last failure on a context is read with
+ * gbfe_last_error().  No C++ exception crosses this boundary.
+ *
+ * Data layouts are the reference's (dft-efe):
+ *   - block vectors ("MultiVector") are row-major [n_dofs][m], vector index
+ *     fastest (linearAlgebra/MultiVector.h:133, data()[iDof*m + iVec]);
+ *   - cell dof ids are cell-major and flat (basis/FEBasisManager.h,
+ *     locallyOwnedCellLocalDofIdsBegin), size_type = uint32;
+ *   - cell matrices are column-major nd_c x nd_c, cells concatenated
+ *     (ksdft/KohnShamOperatorContextFE.h:141-155, d_hamiltonianInAllCells);
+ *   - constraints are the CSR arrays of basis/ConstraintsInternal.h
+ *     (rowConstraintsIdsLocal, rowConstraintsSizes, columnConstraintsIdsLocal,
+ *     columnConstraintsAccumulated, columnConstraintsValues,
+ *     constraintsInhomogenities).
+ */
+#ifndef GBFE_H
+#define GBFE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (mirror linearAlgebra/LinearAlgebraTypes.h error enums) */
+enum {
+  GBFE_OK = 0,
+  GBFE_ERR_ARG = 1,            /* invalid argument / contract violation       */
+  GBFE_ERR_CUDA = 2,           /* CUDA runtime / library failure              */
+  GBFE_ERR_ALLOC = 3,          /* device allocation failed / over budget      */
+  GBFE_ERR_NOT_ORTHONORMALIZABLE = 4, /* Cholesky-GS: globalSize < m or
+                                   near-zero L diagonal
+                                   (OrthonormalizationFunctions.t.cpp:274-306) */
+  GBFE_ERR_LAPACK = 5,         /* potrf / trtri / syevd failure               */
+  GBFE_ERR_NOT_CONVERGED = 6,  /* CG FAILED_TO_CONVERGE, KS_MAX_PASS_ERROR     */
+  GBFE_ERR_DIVERGED = 7,       /* CG RESIDUAL_DIVERGENCE                      */
+  GBFE_ERR_TIMEOUT = 8,        /* a bounded device wait gave up               */
+  GBFE_ERR_CANCELLED = 9       /* serving request cancelled                   */
+};
+
+enum { GBFE_F64 = 0, GBFE_F32 = 1 };
+
+/* cell-matrix precision variants an operator carries */
+enum {
+  GBFE_PREC_FP64 = 1,          /* FP64 matrices (always present)               */
+  GBFE_PREC_MIXED = 2          /* + split-BF16 hi/lo copies for the FP32 path   */
+};
+
+typedef struct gbfe_ctx gbfe_ctx;
+typedef struct gbfe_mesh gbfe_mesh;
+typedef struct gbfe_cons gbfe_cons;
+typedef struct gbfe_op gbfe_op;
+typedef struct gbfe_mv gbfe_mv;
+
+/* ---- lifecycle ------------------------------------------------------------
+ * Replaces the LinAlgOpContext<DEVICE> / BlasQueue / LapackQueue bundle
+ * (linearAlgebra/LinAlgOpContext.h:148-176). */
+int gbfe_ctx_create(int device, gbfe_ctx **out);
+int gbfe_ctx_destroy(gbfe_ctx *ctx);
+int gbfe_last_error(const gbfe_ctx *ctx, char *buf, size_t len);
+/* cudaStream_t as void*; NULL selects the context's own stream */
+int gbfe_ctx_set_stream(gbfe_ctx *ctx, void *stream);
+int gbfe_ctx_synchronize(gbfe_ctx *ctx);
+/* number of kernels this context has launched so far */
+int gbfe_ctx_kernel_launches(const gbfe_ctx *ctx, uint64_t *count);
+
+/* ---- mesh: cell -> dof map ------------------------------------------------
+ * Replaces FEBasisManager::nLocallyOwnedCells / nLocallyOwnedCellDofs /
+ * locallyOwnedCellLocalDofIdsBegin (basis/FEBasisManager.h) as consumed by
+ * KohnShamOperatorContextFE.t.cpp:1334-1356. */
+int gbfe_mesh_upload(gbfe_ctx *ctx, uint32_t n_cells, const uint32_t *nd_per_cell,
+                     const uint32_t *cell_dof_ids, uint64_t n_dofs, gbfe_mesh **out);
+int gbfe_mesh_destroy(gbfe_mesh *mesh);
+
+/* ---- constraints ------------------------------------------------------------
+ * Replaces ConstraintsLocal<...,DEVICE> built from CFEConstraintsLocalDealii
+ * (basis/CFEConstraintsLocalDealii.t.cpp:360-460, ConstraintsInternal.h).
+ * The constraint set must be closed (no column is itself a constrained row). */
+int gbfe_constraints_upload(gbfe_mesh *mesh, uint32_t n_rows, const uint32_t *row_ids,
+                            const uint32_t *row_sizes, const uint32_t *col_ids,
+                            const uint32_t *row_acc, const double *col_values,
+                            const double *inhomogeneities, gbfe_cons **out);
+int gbfe_constraints_destroy(gbfe_cons *cons);
+/* ConstraintsInternal<DEVICE>::constraintsDistributeParentToChild
+ * (basis/ConstraintsInternal.cpp:37-107; .cu:39) */
+int gbfe_constraints_distribute_parent_to_child(const gbfe_cons *cons, gbfe_mv *x);
+/* ConstraintsInternal<DEVICE>::constraintsDistributeChildToParent
+ * (basis/ConstraintsInternal.cpp:112-170; .cu:85) -- deterministic, no atomics */
+int gbfe_constraints_distribute_child_to_parent(const gbfe_cons *cons, gbfe_mv *x);
+
+/* ---- operators --------------------------------------------------------------
+ * Cell-matrix operator: KohnShamOperatorContextFE (H), CFEOverlapOperatorContext
+ * (consistent M) and LaplaceOperatorContextFE (K) all reduce to this
+ * (KohnShamOperatorContextFE.t.cpp:1326-1443, CFEOverlapOperatorContext.t.cpp:
+ * 587-640, LaplaceOperatorContextFE.t.cpp:397-467).  `cons` may be NULL.
+ * `prec_flags` is a mask of GBFE_PREC_*. */
+int gbfe_cellmat_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *mats,
+                        int prec_flags, gbfe_op **out);
+/* Diagonal operator with constraints: CFEOverlapInverseOpContextGLL
+ * (CFEOverlapInverseOpContextGLL.t.cpp:528-559) or the lumped
+ * CFEOverlapOperatorContext (:546-582).  `diag` holds the diagonal entries
+ * (already inverted for an inverse operator). */
+int gbfe_diag_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *diag, gbfe_op **out);
+/* Jacobi preconditioner: Y = diagInv o X, no constraints
+ * (linearAlgebra/PreconditionerJacobi.t.cpp:23-80; the reciprocal is taken
+ * here from `diagonal` exactly as the reference constructor does). */
+int gbfe_jacobi_upload(gbfe_mesh *mesh, const double *diagonal, gbfe_op **out);
+int gbfe_op_destroy(gbfe_op *op);
+
+/* ---- block vectors (MultiVector) -------------------------------------------- */
+int gbfe_mv_create(gbfe_mesh *mesh, uint32_t m, int dtype, gbfe_mv **out);
+int gbfe_mv_destroy(gbfe_mv *mv);
+int gbfe_mv_copy_in(gbfe_mv *mv, const void *host_rowmajor);
+int gbfe_mv_copy_out(const gbfe_mv *mv, void *host_rowmajor);
+int gbfe_mv_copy(const gbfe_mv *src, gbfe_mv *dst); /* same shape; converts dtype */
+int gbfe_mv_set_value(gbfe_mv *mv, double value);
+int gbfe_mv_device_ptr(const gbfe_mv *mv, void **ptr);
+/* MultiVector::l2Norms (MultiVector.t.cpp:553-578); deterministic reduction */
+int gbfe_mv_l2_norms(const gbfe_mv *mv, double *norms_host);
+/* blasLapack::dotMultiVector: per-column sum_i x_i y_i */
+int gbfe_mv_dots(const gbfe_mv *x, const gbfe_mv *y, double *dots_host);
+
+/* ---- the apply -------------------------------------------------------------
+ * OperatorContext::apply(X, Y, updateGhostX, updateGhostY)
+ * (linearAlgebra/OperatorContext.h:104-108).  Y is overwritten.  X is modified
+ * by distributeParentToChild exactly as the reference documents
+ * (OperatorContext.h:79-83).  On one GPU the ghost flags are no-ops.
+ * X and Y may be F64 (FP64 path) or both F32 (mixed path: split-BF16 tensor
+ * products accumulated in FP32; needs an operator built with GBFE_PREC_MIXED). */
+int gbfe_apply(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
+
+/* ---- Chebyshev filters -----------------------------------------------------
+ * ResidualChebyshevFilterGEP (linearAlgebra/ChebyshevFilter.t.cpp:242-444).
+ * eigenvalues: host array of length m.  X is the input subspace, Y the output.
+ * precision: GBFE_F64 runs the recurrence in FP64; GBFE_F32 runs it in FP32
+ * with split-BF16 tensor-core cell products (the initial residual and the
+ * final reconstruction stay FP64). */
+int gbfe_residual_chebyshev_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
+                                   const double *eigenvalues, gbfe_mv *X, uint32_t degree,
+                                   double wanted_lower, double wanted_upper,
+                                   double unwanted_upper, int precision, gbfe_mv *Y);
+/* ChebyshevFilter (ChebyshevFilter.t.cpp:39-135); result in Y (and X). */
+int gbfe_chebyshev_filter(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *X, uint32_t degree,
+                          double wanted_lower, double wanted_upper, double unwanted_upper,
+                          gbfe_mv *Y);
+
+/* ---- FP64 dense stages -------------------------------------------------------
+ * OrthonormalizationFunctions::CholeskyGramSchmidt, serial LAPACK branch
+ * (OrthonormalizationFunctions.t.cpp:356-415): S = X^T B X, potrf('L'),
+ * trtri('L'), X_o = X S^T (row-major view). */
+int gbfe_cholesky_gram_schmidt(const gbfe_op *B, gbfe_mv *X, gbfe_mv *X_ortho);
+/* RayleighRitzEigenSolver::solve, LAPACK branch
+ * (RayleighRitzEigenSolver.t.cpp:233-301): X^T A X, syevd('V','L'), X Q. */
+int gbfe_rayleigh_ritz(const gbfe_op *A, gbfe_mv *X, double *eigenvalues_host, gbfe_mv *X_out);
+/* KohnShamEigenSolver::getLinearEigenSolveResidual
+ * (KohnShamEigenSolver.t.cpp:574-684): ||A x_i - eps_i B x_i||_2. */
+int gbfe_eigen_residual_norms(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X,
+                              const double *eigenvalues, double *norms_host);
+
+/* ---- ChFSI ---------------------------------------------------------------- */
+typedef struct {
+  uint32_t degree;              /* Chebyshev polynomial degree                */
+  uint32_t max_passes;          /* maxChebyshevFilterPass                     */
+  uint32_t n_wanted;            /* eigenpairs checked for convergence         */
+  int      filter_precision;    /* GBFE_F64 or GBFE_F32 (mixed)               */
+  double   residual_tol;        /* eigenSolveResidualTolerance               */
+  double   wanted_lower;        /* bounds; set use_lanczos=1 to estimate them */
+  double   wanted_upper;
+  double   unwanted_upper;
+  int      use_lanczos;         /* 1: LanczosExtremeEigenSolver-style bounds  */
+  uint32_t lanczos_steps;       /* Krylov dimension (reference default 20)    */
+  uint64_t lanczos_seed;
+  int      fixed_passes;        /* 1: run exactly max_passes passes           */
+} gbfe_ks_params;
+
+/* ChebyshevFilteredEigenSolver::solve (ChebyshevFilteredEigenSolver.t.cpp:
+ * 194-437): filter -> Cholesky-GS -> Rayleigh-Ritz, one pass.
+ * eigenvalues (host, length m) in: previous Ritz values; out: new ones. */
+int gbfe_chfsi_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv *X,
+                    double *eigenvalues, uint32_t degree, double wanted_lower,
+                    double wanted_upper, double unwanted_upper, int filter_precision);
+/* KohnShamEigenSolver::solve pass loop (KohnShamEigenSolver.t.cpp:214-536)
+ * without the Fermi-level / occupancy step: bounds, up to max_passes ChFSI
+ * passes, residual check on the first n_wanted pairs.  X in: initial block,
+ * out: eigenvectors.  eigenvalues/residuals: host arrays of length m. */
+int gbfe_ks_eigen_solve(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv *X,
+                        const gbfe_ks_params *params, double *eigenvalues, double *residuals,
+                        uint32_t *passes_out);
+/* LanczosExtremeEigenSolver-style spectrum bounds of B^-1 A
+ * (LanczosExtremeEigenSolver.t.cpp:296-440): out[0] = smallest, out[1] =
+ * largest Ritz value, out[2] = last beta (residual). */
+int gbfe_lanczos_bounds(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
+                        uint32_t steps, uint64_t seed, double *out3);
+
+/* ---- CG -------------------------------------------------------------------
+ * CGLinearSolver::solve (linearAlgebra/CGLinearSolver.t.cpp:68-313) with
+ * per-component convergence.  x: in initial guess, out solution.
+ * Returns GBFE_OK, GBFE_ERR_NOT_CONVERGED or GBFE_ERR_DIVERGED. */
+int gbfe_cg_solve(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b, gbfe_mv *x,
+                  uint32_t max_iter, double abs_tol, double rel_tol, double div_tol,
+                  uint32_t *iters_out, double *rnorm_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBFE_H */

@@ -1,0 +1,66 @@
+#!/usr/bin/env bash
+# Builds oracle/_ref/ref_driver: the reference's own CPU implementation of the
+# hot path, compiled directly from its sources (no CMake, no deal.II), linked
+# against scipy's bundled LP64 OpenBLAS.  Test infrastructure only: it makes
+# the golden vectors in tests/golden/.  Outputs go to oracle/_ref/ only.
+#
+#   REF  : reference source tree (default /root/reference)
+#   The one reference-side defect that stops the serial build -- a stray ';'
+#   at utils/MPIWrapper.cpp:334 in the non-MPI branch -- is patched into a
+#   copy under oracle/_ref/patched/ at build time.
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${REF:-/root/reference}"
+OUT="$HERE/_ref"
+SRC="$REF/src"
+if [ ! -d "$SRC" ]; then echo "reference sources not found at $SRC" >&2; exit 1; fi
+mkdir -p "$OUT/patched" "$OUT/obj"
+
+BLASDIR="$(python3 -c 'import scipy, os; print(os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs"))')"
+BLASLIB="$(ls "$BLASDIR"/libscipy_openblas*.so | head -1)"
+
+sed '334s/;$//' "$SRC/utils/MPIWrapper.cpp" > "$OUT/patched/MPIWrapper.cpp"
+
+CXXFLAGS="-std=c++17 -O2 -DNDEBUG -w -I$HERE/ref_harness/shadow -I$SRC"
+SOURCES=(
+  utils/Exceptions.cpp utils/MemoryTransfer.cpp utils/MPITypes.cpp utils/MPIRequestersNBX.cpp
+  utils/MPIPatternP2P.cpp utils/MPIErrorCodeHandler.cpp utils/Defaults.cpp utils/NumberUtils.cpp
+  utils/MPICommunicatorP2PKernels.cpp utils/MemoryManager.cpp utils/RandNumGen.cpp
+  linearAlgebra/BlasAPIWrapperHost.cpp linearAlgebra/LapackAPIWrapperHost.cpp linearAlgebra/BlasLapackKernels.cpp
+  linearAlgebra/LinearAlgebraTypes.cpp linearAlgebra/Defaults.cpp linearAlgebra/MultiVector.cpp
+  linearAlgebra/Vector.cpp linearAlgebra/VectorAttributes.cpp linearAlgebra/LinAlgOpContext.cpp
+  linearAlgebra/IdentityOperatorContext.cpp linearAlgebra/LinearAlgebraProfiler.cpp basis/ConstraintsInternal.cpp
+)
+OBJS=()
+pids=()
+for s in "${SOURCES[@]}"; do
+  o="$OUT/obj/$(echo "$s" | tr '/' '_').o"
+  OBJS+=("$o")
+  if [ ! -f "$o" ] || [ "$SRC/$s" -nt "$o" ]; then
+    g++ $CXXFLAGS -c "$SRC/$s" -o "$o" & pids+=($!)
+  fi
+done
+o="$OUT/obj/MPIWrapper.o"; OBJS+=("$o")
+[ -f "$o" ] || { g++ $CXXFLAGS -I"$SRC/utils" -c "$OUT/patched/MPIWrapper.cpp" -o "$o" & pids+=($!); }
+o="$OUT/obj/ref_driver.o"; OBJS+=("$o")
+if [ ! -f "$o" ] || [ "$HERE/ref_harness/ref_driver.cpp" -nt "$o" ]; then
+  g++ $CXXFLAGS -c "$HERE/ref_harness/ref_driver.cpp" -o "$o" & pids+=($!)
+fi
+for p in "${pids[@]}"; do wait "$p"; done
+
+# Point the Fortran BLAS/LAPACK names the reference calls at scipy's prefixed
+# exports by renaming the undefined symbols in the compiled objects.
+EXPORTS="$(nm -D "$BLASLIB")"
+RENAMES=()
+for sym in $(nm -u "${OBJS[@]}" 2>/dev/null | awk '{print $NF}' | grep -E '^[a-z]+_$' | sort -u); do
+  if grep -q " T scipy_${sym}$" <<< "$EXPORTS"; then RENAMES+=(--redefine-sym "${sym}=scipy_${sym}"); fi
+done
+mkdir -p "$OUT/link"
+LINKOBJS=()
+for o in "${OBJS[@]}"; do
+  l="$OUT/link/$(basename "$o")"
+  objcopy "${RENAMES[@]}" "$o" "$l"
+  LINKOBJS+=("$l")
+done
+g++ -o "$OUT/ref_driver" "${LINKOBJS[@]}" "$BLASLIB" -Wl,-rpath,"$(dirname "$BLASLIB")"
+echo "built $OUT/ref_driver"
