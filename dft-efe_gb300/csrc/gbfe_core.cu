@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <cstdlib>
 
 using namespace gbfe;
 
@@ -176,6 +177,16 @@ __global__ void k_fill(T *__restrict__ d, uint64_t n, T v) {
     d[t] = v;
 }
 
+// FP64 FMA throughput probe: 8 independent dependency chains per thread
+__global__ void k_dfma_probe(double *out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
 unsigned stride_grid(gbfe_ctx *ctx, uint64_t n, unsigned block = 256) {
   uint64_t g = (n + block - 1) / block;
   const uint64_t cap = (uint64_t)ctx->sm_count * 16;
@@ -251,6 +262,8 @@ static void cell_apply_f64(const gbfe_op *op, gbfe_mv *X, double *Yc) {
     attr_set = true;
   }
   dim3 grid(me->n_cells, vt, jsplit);
+  ProfScope prof(ctx, "cell_apply_f64", 2.0 * m * (double)me->total_mat,
+                 8.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat));
   k_cell_apply_f64<<<grid, 256, smem, ctx->stream>>>(X->d.p, m, me->ids.p, me->cell_off.p, me->mat_off.p,
                                                      op->mats.p, Yc, mt, jsplit);
   check_launch(ctx, "cell_apply_f64");
@@ -379,6 +392,10 @@ int gbfe_ctx_create(int device, gbfe_ctx **out) {
     GBFE_CUBLAS(cublasSetPointerMode(ctx->cublas, CUBLAS_POINTER_MODE_HOST));
     GBFE_CUSOLVER(cusolverDnCreate(&ctx->cusolver));
     GBFE_CUSOLVER(cusolverDnSetStream(ctx->cusolver, ctx->stream));
+    ctx->status.alloc(4);
+    GBFE_CUDA(cudaMemsetAsync(ctx->status.p, 0, 4 * sizeof(int), ctx->stream));
+    const char *tc = getenv("GBFE_TENSOR_CORES");
+    if (tc && tc[0] == '0') ctx->use_tc = 0;
   });
   if (rc != GBFE_OK) {
     std::string msg = ctx->last_error;
@@ -424,10 +441,98 @@ int gbfe_ctx_synchronize(gbfe_ctx *ctx) {
   return gbfe_guard(ctx, [&] { GBFE_CUDA(cudaStreamSynchronize(ctx->stream)); });
 }
 
+int gbfe_ctx_check_status(gbfe_ctx *ctx) {
+  if (!ctx) return GBFE_ERR_ARG;
+  int st = 0;
+  int rc = gbfe_guard(ctx, [&] {
+    GBFE_CUDA(cudaMemcpyAsync(&st, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (st != 0) {
+      GBFE_CUDA(cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream));
+      ctx->last_error = "a bounded device wait gave up (code " + std::to_string(st) + ")";
+    }
+  });
+  if (rc != GBFE_OK) return rc;
+  return st ? GBFE_ERR_TIMEOUT : GBFE_OK;
+}
+
+int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int on) {
+  if (!ctx) return GBFE_ERR_ARG;
+  ctx->use_tc = on ? 1 : 0;
+  return GBFE_OK;
+}
+
 int gbfe_ctx_kernel_launches(const gbfe_ctx *ctx, uint64_t *count) {
   if (!ctx || !count) return GBFE_ERR_ARG;
   *count = ctx->launches;
   return GBFE_OK;
+}
+
+int gbfe_ctx_set_profiling(gbfe_ctx *ctx, int on) {
+  if (!ctx) return GBFE_ERR_ARG;
+  ctx->profiling = on ? 1 : 0;
+  return GBFE_OK;
+}
+
+int gbfe_ctx_kernel_stats(gbfe_ctx *ctx, const char *name, uint64_t *launches, double *total_ms, double *flops,
+                          double *bytes) {
+  if (!ctx || !name) return GBFE_ERR_ARG;
+  return gbfe_guard(ctx, [&] {
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+    auto it = ctx->kstats.find(name);
+    KernelStat empty;
+    KernelStat &st = it == ctx->kstats.end() ? empty : it->second;
+    for (auto &pr : st.pending) {
+      float ms = 0.f;
+      GBFE_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+      st.ms += ms;
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+    st.pending.clear();
+    if (launches) *launches = st.launches;
+    if (total_ms) *total_ms = st.ms;
+    if (flops) *flops = st.flops;
+    if (bytes) *bytes = st.bytes;
+  });
+}
+
+int gbfe_ctx_reset_kernel_stats(gbfe_ctx *ctx) {
+  if (!ctx) return GBFE_ERR_ARG;
+  return gbfe_guard(ctx, [&] {
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (auto &kv : ctx->kstats)
+      for (auto &pr : kv.second.pending) {
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+      }
+    ctx->kstats.clear();
+  });
+}
+
+int gbfe_probe_fp64_peak(gbfe_ctx *ctx, double *gflops) {
+  if (!ctx || !gflops) return GBFE_ERR_ARG;
+  return gbfe_guard(ctx, [&] {
+    const int blocks = ctx->sm_count * 8, threads = 256, iters = 4096;
+    DBuf<double> out;
+    out.alloc((size_t)blocks * threads);
+    cudaEvent_t e0, e1;
+    GBFE_CUDA(cudaEventCreate(&e0));
+    GBFE_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      GBFE_CUDA(cudaEventRecord(e0, ctx->stream));
+      k_dfma_probe<<<blocks, threads, 0, ctx->stream>>>(out.p, iters, 0.999, 1e-3);
+      GBFE_CUDA(cudaEventRecord(e1, ctx->stream));
+      GBFE_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      GBFE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *gflops = 2.0 * 8 * iters * (double)blocks * threads / (best * 1e6);
+  });
 }
 
 int gbfe_mesh_upload(gbfe_ctx *ctx, uint32_t n_cells, const uint32_t *nd_per_cell, const uint32_t *cell_dof_ids,
@@ -699,6 +804,34 @@ int gbfe_mv_create(gbfe_mesh *mesh, uint32_t m, int dtype, gbfe_mv **out) {
       mv->f.alloc(n);
       if (n) GBFE_CUDA(cudaMemsetAsync(mv->f.p, 0, n * 4, mesh->ctx->stream));
     }
+  });
+  if (rc != GBFE_OK) {
+    delete mv;
+    return rc;
+  }
+  *out = mv;
+  return GBFE_OK;
+}
+
+int gbfe_mv_wrap(gbfe_mesh *mesh, uint32_t m, int dtype, void *device_ptr, gbfe_mv **out) {
+  if (!mesh || !out || !device_ptr) return GBFE_ERR_ARG;
+  *out = nullptr;
+  gbfe_mv *mv = nullptr;
+  int rc = gbfe_guard(mesh->ctx, [&] {
+    GBFE_REQUIRE(dtype == GBFE_F64 || dtype == GBFE_F32, "mv_wrap: dtype must be GBFE_F64 or GBFE_F32");
+    cudaPointerAttributes attr;
+    GBFE_CUDA(cudaPointerGetAttributes(&attr, device_ptr));
+    GBFE_REQUIRE(attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged,
+                 "mv_wrap: pointer is not device memory");
+    GBFE_REQUIRE(((uintptr_t)device_ptr % (dtype == GBFE_F64 ? 8 : 4)) == 0, "mv_wrap: misaligned pointer");
+    mv = new gbfe_mv();
+    mv->mesh = mesh;
+    mv->m = m;
+    mv->dtype = dtype;
+    if (dtype == GBFE_F64)
+      mv->d.wrap((double *)device_ptr, mv->count());
+    else
+      mv->f.wrap((float *)device_ptr, mv->count());
   });
   if (rc != GBFE_OK) {
     delete mv;

@@ -24,6 +24,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <string>
 #include <vector>
 #include <stdexcept>
@@ -71,14 +72,22 @@ template <class T>
 struct DBuf {
   T *p = nullptr;
   size_t n = 0;
+  bool borrowed = false;  // wraps memory owned by the caller: never freed here
   DBuf() = default;
   DBuf(const DBuf &) = delete;
   DBuf &operator=(const DBuf &) = delete;
   ~DBuf() { reset(); }
   void reset() {
-    if (p) cudaFree(p);
+    if (p && !borrowed) cudaFree(p);
     p = nullptr;
     n = 0;
+    borrowed = false;
+  }
+  void wrap(T *ext, size_t count) {
+    reset();
+    p = ext;
+    n = count;
+    borrowed = true;
   }
   void alloc(size_t count) {
     if (count == n && p) return;
@@ -98,8 +107,18 @@ struct DBuf {
 
 }  // namespace gbfe
 
+// Per-kernel timing with CUDA events recorded on the launching stream
+// (enabled by gbfe_ctx_set_profiling); resolved when the stats are read.
+struct KernelStat {
+  uint64_t launches = 0;
+  double ms = 0.0, flops = 0.0, bytes = 0.0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+};
+
 struct gbfe_ctx {
   int device = 0;
+  int profiling = 0;
+  std::map<std::string, KernelStat> kstats;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   cublasHandle_t cublas = nullptr;
@@ -112,6 +131,8 @@ struct gbfe_ctx {
   gbfe::DBuf<double> small;  // m x m work matrices
   gbfe::DBuf<int> info;
   gbfe::DBuf<double> lwork;
+  gbfe::DBuf<int> status;    // device status word written by bounded waits (0 = ok)
+  int use_tc = 1;            // split-BF16 tcgen05 cell product for the mixed path
 };
 
 struct gbfe_mesh {
@@ -153,8 +174,8 @@ struct gbfe_op {
   int kind = OP_CELL;
   int prec = GBFE_PREC_FP64;
   gbfe::DBuf<double> mats;            // f64 col-major per cell
-  gbfe::DBuf<__nv_bfloat16> mats_hi;  // split-BF16 high part, tile layout
-  gbfe::DBuf<__nv_bfloat16> mats_lo;  // split-BF16 low part
+  gbfe::DBuf<__nv_bfloat16> mats_hi;  // split-BF16 hi/lo tiles (per cell, per K chunk)
+  gbfe::DBuf<uint64_t> tc_aoff;       // element offset of each cell's tiles
   gbfe::DBuf<float> mats_f32;         // FP32 copy for the SIMT mixed apply
   gbfe::DBuf<double> diag;
   mutable gbfe::DBuf<double> cellbuf;  // per-apply cell-wise result scratch (f64)
@@ -186,11 +207,36 @@ inline void check_launch(gbfe_ctx *ctx, const char *name) {
   count_launch(ctx);
 }
 
+// Brackets one launch with events when profiling is on.
+struct ProfScope {
+  gbfe_ctx *ctx;
+  KernelStat *st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ProfScope(gbfe_ctx *c, const char *name, double flops, double bytes) : ctx(c) {
+    if (!ctx->profiling) return;
+    st = &ctx->kstats[name];
+    st->flops += flops;
+    st->bytes += bytes;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+  }
+  ~ProfScope() {
+    if (!st) return;
+    cudaEventRecord(e1, ctx->stream);
+    st->pending.emplace_back(e0, e1);
+    st->launches++;
+  }
+};
+
 // ---- internal entry points shared between translation units
 void constraints_p2c(gbfe_ctx *ctx, const gbfe_cons *c, gbfe_mv *x);
 void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
 void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
 void build_mixed_mats(gbfe_op *op);
+void build_tc_mats(gbfe_op *op);
+bool tc_supported(const gbfe_mesh *me);
+void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc);
 
 // vector kernels (solvers)
 void axpby(gbfe_ctx *ctx, size_t n, double a, const gbfe_mv *x, double b, const gbfe_mv *y, gbfe_mv *z);

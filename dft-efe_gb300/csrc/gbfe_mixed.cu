@@ -1,8 +1,10 @@
 // gbfe_mixed.cu -- FP32 cellwise apply for the mixed-precision Chebyshev filter.
 //
-// Block vectors are FP32 [N][m]; cell matrices are stored once more in FP32.
-// The product per cell is Yc = A_c^T Xc with FP32 accumulation; assembly and
-// constraints are the same deterministic kernels as the FP64 path.
+// Block vectors are FP32 [N][m].  The cell product runs on the tensor cores
+// (gbfe_tc.cu, split-BF16, cells of up to 256 dofs) or, when that path is
+// switched off or a cell is larger, as an FP32 SIMT product over an FP32 copy
+// of the cell matrices.  Assembly and constraints are the same deterministic
+// kernels as the FP64 path.
 #include "gbfe_internal.cuh"
 
 #include <algorithm>
@@ -73,6 +75,7 @@ void build_mixed_mats(gbfe_op *op) {
   unsigned g = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 16);
   k_f64_to_f32<<<g ? g : 1, 256, 0, ctx->stream>>>(op->mats.p, m32->p, n);
   check_launch(ctx, "f64_to_f32");
+  if (tc_supported(me)) build_tc_mats(op);
 }
 
 void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
@@ -81,6 +84,11 @@ void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
   GBFE_REQUIRE(op->prec & GBFE_PREC_MIXED, "FP32 apply: operator was not built with GBFE_PREC_MIXED");
   const uint32_t m = X->m;
   op->cellbuf_f32.ensure((size_t)me->total_cell_dofs * m);
+  if (ctx->use_tc && op->tc_aoff.p) {
+    cell_apply_tc(op, X, op->cellbuf_f32.p);
+    assemble_f32(op, op->cellbuf_f32.p, Y);
+    return;
+  }
   const size_t smem_cap = 96 * 1024;
   uint32_t mt = (uint32_t)std::min<size_t>(m, smem_cap / (sizeof(float) * me->nd_max));
   GBFE_REQUIRE(mt > 0, "cell too large for the FP32 apply");
@@ -98,6 +106,8 @@ void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
   const size_t smem = sizeof(float) * (size_t)me->nd_max * mt;
   dim3 grid(me->n_cells, vt, jsplit);
   const DBuf<float> *m32 = &op->mats_f32;
+  ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat,
+                 4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat));
   k_cell_apply_f32<<<grid, 256, smem, ctx->stream>>>(X->f.p, m, me->ids.p, me->cell_off.p, me->mat_off.p, m32->p,
                                                      op->cellbuf_f32.p, mt, jsplit);
   check_launch(ctx, "cell_apply_f32");

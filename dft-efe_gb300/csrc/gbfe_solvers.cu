@@ -345,7 +345,8 @@ void launch_cheb_step<float>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha
 // recurrence steps run on FP32 block vectors with split-BF16 tensor-core cell
 // products (the operator must carry GBFE_PREC_MIXED matrices).
 void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, const double *eig_h, gbfe_mv *X,
-                     uint32_t degree, double wl, double wu, double uu, gbfe_mv *Y, int prec) {
+                     uint32_t degree, double wl, double wu, double uu, gbfe_mv *Y, int prec,
+                     const gbfe_mv *R0 = nullptr) {
   gbfe_ctx *ctx = X->mesh->ctx;
   const uint32_t m = X->m;
   const bool mixed = prec == GBFE_F32;
@@ -358,7 +359,11 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
   d_eig.set(ctx, eig_h, m);
   d_tab.set(ctx, s.eF2.data(), s.eF2.size());
   auto s1 = make_like(X, rt), s2 = make_like(X, rt), R = make_like(X, rt), RN = make_like(X, rt);
-  {
+  if (R0) {
+    // the caller already holds A X - Lambda B X (the residual of the previous
+    // Rayleigh-Ritz step), so the two initial applies are skipped
+    GBFE_CUDA(cudaMemcpyAsync(Y->d.p, R0->d.p, Y->count() * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
     auto s3 = make_like(X, GBFE_F64);
     apply_op(B, X, Y);
     apply_op(A, X, s3.get());
@@ -498,6 +503,145 @@ int chfsi_pass_impl(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbf
   return rayleigh_ritz_impl(A, Xo.get(), eig_h, X, msg);
 }
 
+
+// ------------------------------------------------------------ fused KS pass
+// One ChFSI pass with two FP64 operator applies:
+//   Y    = filter(residual R, Ritz vectors X)           (d-1 A applies, mixed or FP64)
+//   MY   = B Y,  HY = A Y                               (FP64)
+//   S_M  = Y^T MY = L L^T,   S_H = Y^T HY
+//   Hp   = L^-1 S_H L^-T = V diag(eps) V^T              (syevd, FP64)
+//   T    = L^-T V;   X = Y T,  HX = HY T,  MX = MY T
+//   R    = HX - MX diag(eps)                            (next pass's filter input)
+// This is the reference's filter -> Cholesky-GS -> Rayleigh-Ritz -> residual
+// sequence (ChebyshevFilteredEigenSolver.t.cpp:194-437,
+// KohnShamEigenSolver.t.cpp:574-684) with H X and M X carried through the
+// m x m rotations instead of re-applied.
+struct FusedState {
+  std::unique_ptr<gbfe_mv> Y, MY, HY, HX, MX, R;
+  DBuf<double> SM, SH, V;
+};
+
+int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv *X, double *eig_h,
+               uint32_t degree, double wl, double wu, double uu, int prec, FusedState &st, double *res_h,
+               std::string &msg) {
+  gbfe_ctx *ctx = X->mesh->ctx;
+  const int m = (int)X->m;
+  const int N = (int)X->mesh->n_dofs;
+  residual_filter(A, B, BInv, eig_h, X, degree, wl, wu, uu, st.Y.get(), prec, st.R.get());
+  apply_op(B, st.Y.get(), st.MY.get());
+  apply_op(A, st.Y.get(), st.HY.get());
+  gram(ctx, st.Y.get(), st.MY.get(), st.SM.p);
+  gram(ctx, st.Y.get(), st.HY.get(), st.SH.p);
+  int lwork = 0;
+  GBFE_CUSOLVER(cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, &lwork));
+  ctx->lwork.ensure(std::max(lwork, 1));
+  ctx->info.ensure(1);
+  GBFE_CUSOLVER(cusolverDnDpotrf(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, ctx->lwork.p, lwork,
+                                 ctx->info.p));
+  count_launch(ctx);
+  int info = 0;
+  std::vector<double> hL((size_t)m * m);
+  GBFE_CUDA(cudaMemcpyAsync(&info, ctx->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GBFE_CUDA(cudaMemcpyAsync(hL.data(), st.SM.p, hL.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (info != 0) {
+    msg = "LAPACK_ERROR: FAILED_CHOLESKY_FACTORIZATION (potrf info " + std::to_string(info) + ")";
+    return GBFE_ERR_LAPACK;
+  }
+  for (int i = 0; i < m; ++i)
+    if (std::fabs(hL[(size_t)i * m + i]) < 1e-14) {
+      msg = "Chol GS cannot orthogonalize the given multivector (near-zero diagonal of L)";
+      return GBFE_ERR_NOT_ORTHONORMALIZABLE;
+    }
+  const double one = 1.0, zero = 0.0;
+  // Hp = L^-1 S_H L^-T
+  GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, m,
+                          m, &one, st.SM.p, m, st.SH.p, m));
+  GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, m,
+                          m, &one, st.SM.p, m, st.SH.p, m));
+  count_launch(ctx, 2);
+  DevVec W(m);
+  GBFE_CUSOLVER(cusolverDnDsyevd_bufferSize(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m,
+                                            st.SH.p, m, W.b.p, &lwork));
+  ctx->lwork.ensure(std::max(lwork, 1));
+  GBFE_CUSOLVER(cusolverDnDsyevd(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, st.SH.p, m,
+                                 W.b.p, ctx->lwork.p, lwork, ctx->info.p));
+  count_launch(ctx);
+  GBFE_CUDA(cudaMemcpyAsync(&info, ctx->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  W.get(ctx, eig_h, m);
+  if (info != 0) {
+    msg = "LAPACK_ERROR: FAILED_STANDARD_EIGENPROBLEM (syevd info " + std::to_string(info) + ")";
+    return GBFE_ERR_LAPACK;
+  }
+  // T = L^-T V (in place in SH)
+  GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, m,
+                          m, &one, st.SM.p, m, st.SH.p, m));
+  count_launch(ctx);
+  const double *T = st.SH.p;
+  // rows times T: col-major (m x N) out = T^T * in
+  GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.Y->d.p, m, &zero, X->d.p, m));
+  GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.HY->d.p, m, &zero,
+                          st.HX->d.p, m));
+  GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.MY->d.p, m, &zero,
+                          st.MX->d.p, m));
+  count_launch(ctx, 3);
+  std::vector<double> nOnes(m, -1.0);
+  DevVec d_no(m), d_e(m);
+  d_no.set(ctx, nOnes.data(), m);
+  d_e.set(ctx, eig_h, m);
+  // R = HX - MX diag(eps)   (getLinearEigenSolveResidual's axpbyBlocked with the sign flipped)
+  d_axpby_blocked(ctx, -1.0, d_no.b.p, st.HX.get(), -1.0, d_e.b.p, st.MX.get(), st.R.get());
+  host_coldots(ctx, st.R.get(), st.R.get(), res_h, true);
+  return GBFE_OK;
+}
+
+int ks_solve_fused(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv *X, const gbfe_ks_params *prm,
+                   double wl, double wu, double uu, double *eig_h, double *res_h, uint32_t *passes_out,
+                   std::string &msg) {
+  gbfe_ctx *ctx = X->mesh->ctx;
+  const uint32_t m = X->m;
+  FusedState st;
+  st.Y = make_like(X, GBFE_F64);
+  st.MY = make_like(X, GBFE_F64);
+  st.HY = make_like(X, GBFE_F64);
+  st.HX = make_like(X, GBFE_F64);
+  st.MX = make_like(X, GBFE_F64);
+  st.R = make_like(X, GBFE_F64);
+  st.SM.alloc((size_t)m * m);
+  st.SH.alloc((size_t)m * m);
+  // initial residual of the input block: R = A X - Lambda B X
+  apply_op(A, X, st.HX.get());
+  apply_op(B, X, st.MX.get());
+  {
+    std::vector<double> ones(m, 1.0);
+    DevVec d_o(m), d_e(m);
+    d_o.set(ctx, ones.data(), m);
+    d_e.set(ctx, eig_h, m);
+    d_axpby_blocked(ctx, 1.0, d_o.b.p, st.HX.get(), -1.0, d_e.b.p, st.MX.get(), st.R.get());
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  int status = GBFE_ERR_NOT_CONVERGED;
+  uint32_t pass = 0;
+  for (; pass < prm->max_passes; ++pass) {
+    const int r = fused_pass(A, B, BInv, X, eig_h, prm->degree, wl, wu, uu, prm->filter_precision, st, res_h, msg);
+    if (r != GBFE_OK) {
+      status = r;
+      break;
+    }
+    bool conv = true;
+    for (uint32_t i = 0; i < prm->n_wanted; ++i) conv &= res_h[i] <= prm->residual_tol;
+    if (conv && !prm->fixed_passes) {
+      status = GBFE_OK;
+      ++pass;
+      break;
+    }
+    if (prm->fixed_passes && pass + 1 == prm->max_passes) status = conv ? GBFE_OK : GBFE_ERR_NOT_CONVERGED;
+    wl = eig_h[0];
+    wu = eig_h[m - 1];
+  }
+  if (passes_out) *passes_out = pass;
+  return status;
+}
 }  // namespace
 
 namespace gbfe {
@@ -657,6 +801,12 @@ int gbfe_ks_eigen_solve(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
     }
     uint32_t pass = 0;
     std::string msg;
+    if (!prm->faithful_passes) {
+      status = ks_solve_fused(A, B, BInv, X, prm, wl, wu, uu, eigenvalues, residuals, passes_out, msg);
+      if (status != GBFE_OK) ctx->last_error = msg.empty() ? "KS_MAX_PASS_ERROR: residual tolerance not reached" : msg;
+      GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+      return;
+    }
     status = GBFE_ERR_NOT_CONVERGED;
     for (; pass < prm->max_passes; ++pass) {
       int r = chfsi_pass_impl(A, B, BInv, X, eigenvalues, prm->degree, wl, wu, uu, prm->filter_precision, msg);

@@ -28,6 +28,7 @@ class KSParams(C.Structure):
         ("degree", u32), ("max_passes", u32), ("n_wanted", u32), ("filter_precision", i32),
         ("residual_tol", f64), ("wanted_lower", f64), ("wanted_upper", f64), ("unwanted_upper", f64),
         ("use_lanczos", i32), ("lanczos_steps", u32), ("lanczos_seed", u64), ("fixed_passes", i32),
+        ("faithful_passes", i32),
     ]
 
 
@@ -39,6 +40,12 @@ SIGNATURES = {
     "gbfe_ctx_set_stream": (i32, [p, p]),
     "gbfe_ctx_synchronize": (i32, [p]),
     "gbfe_ctx_kernel_launches": (i32, [p, C.POINTER(u64)]),
+    "gbfe_ctx_check_status": (i32, [p]),
+    "gbfe_ctx_set_tensor_cores": (i32, [p, i32]),
+    "gbfe_ctx_set_profiling": (i32, [p, i32]),
+    "gbfe_ctx_kernel_stats": (i32, [p, C.c_char_p, C.POINTER(u64), pf64, pf64, pf64]),
+    "gbfe_ctx_reset_kernel_stats": (i32, [p]),
+    "gbfe_probe_fp64_peak": (i32, [p, pf64]),
     "gbfe_mesh_upload": (i32, [p, u32, p, p, u64, C.POINTER(p)]),
     "gbfe_mesh_destroy": (i32, [p]),
     "gbfe_constraints_upload": (i32, [p, u32, p, p, p, p, p, p, C.POINTER(p)]),
@@ -50,6 +57,7 @@ SIGNATURES = {
     "gbfe_jacobi_upload": (i32, [p, p, C.POINTER(p)]),
     "gbfe_op_destroy": (i32, [p]),
     "gbfe_mv_create": (i32, [p, u32, i32, C.POINTER(p)]),
+    "gbfe_mv_wrap": (i32, [p, u32, i32, p, C.POINTER(p)]),
     "gbfe_mv_destroy": (i32, [p]),
     "gbfe_mv_copy_in": (i32, [p, p]),
     "gbfe_mv_copy_out": (i32, [p, p]),

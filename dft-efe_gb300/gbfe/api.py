@@ -59,6 +59,29 @@ class LinAlgOpContext:
         check(self.lib.gbfe_ctx_kernel_launches(self.h, C.byref(n)), self.h, "launch count")
         return int(n.value)
 
+    def check_status(self) -> None:
+        check(self.lib.gbfe_ctx_check_status(self.h), self.h, "device status")
+
+    def set_tensor_cores(self, on: bool) -> None:
+        check(self.lib.gbfe_ctx_set_tensor_cores(self.h, 1 if on else 0), self.h, "set_tensor_cores")
+
+    def set_profiling(self, on: bool) -> None:
+        check(self.lib.gbfe_ctx_set_profiling(self.h, 1 if on else 0), self.h, "set_profiling")
+
+    def kernel_stats(self, name: str) -> dict:
+        n, ms, fl, by = C.c_uint64(), C.c_double(), C.c_double(), C.c_double()
+        check(self.lib.gbfe_ctx_kernel_stats(self.h, name.encode(), C.byref(n), C.byref(ms), C.byref(fl),
+                                             C.byref(by)), self.h, "kernel_stats")
+        return {"launches": int(n.value), "ms": ms.value, "flops": fl.value, "bytes": by.value}
+
+    def reset_kernel_stats(self) -> None:
+        check(self.lib.gbfe_ctx_reset_kernel_stats(self.h), self.h, "reset_kernel_stats")
+
+    def probe_fp64_peak(self) -> float:
+        g = C.c_double()
+        check(self.lib.gbfe_probe_fp64_peak(self.h, C.byref(g)), self.h, "probe_fp64_peak")
+        return g.value
+
     def set_stream(self, stream_ptr: int | None) -> None:
         check(self.lib.gbfe_ctx_set_stream(self.h, C.c_void_p(stream_ptr or 0)), self.h, "set_stream")
 
@@ -320,7 +343,7 @@ def lanczos_bounds(A, B, BInv, steps: int = 20, seed: int = 7) -> np.ndarray:
 class KohnShamEigenSolver:
     def __init__(self, n_wanted: int, degree: int, max_passes: int, residual_tol: float = 1e-6, mixed: bool = False,
                  bounds: Optional[Sequence[float]] = None, lanczos_steps: int = 20, lanczos_seed: int = 7,
-                 fixed_passes: bool = False):
+                 fixed_passes: bool = False, faithful_passes: bool = False):
         self.p = KSParams()
         self.p.degree, self.p.max_passes, self.p.n_wanted = int(degree), int(max_passes), int(n_wanted)
         self.p.filter_precision = GBFE_F32 if mixed else GBFE_F64
@@ -332,6 +355,7 @@ class KohnShamEigenSolver:
             self.p.use_lanczos = 1
         self.p.lanczos_steps, self.p.lanczos_seed = int(lanczos_steps), int(lanczos_seed)
         self.p.fixed_passes = 1 if fixed_passes else 0
+        self.p.faithful_passes = 1 if faithful_passes else 0
 
     def solve(self, H, X: MultiVector, M, MInv, eigenvalues: Optional[np.ndarray] = None):
         ev = np.zeros(X.m) if eigenvalues is None else np.ascontiguousarray(eigenvalues, dtype=np.float64).copy()

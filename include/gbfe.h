@@ -66,8 +66,26 @@ int gbfe_last_error(const gbfe_ctx *ctx, char *buf, size_t len);
 /* cudaStream_t as void*; NULL selects the context's own stream */
 int gbfe_ctx_set_stream(gbfe_ctx *ctx, void *stream);
 int gbfe_ctx_synchronize(gbfe_ctx *ctx);
+/* Reads and clears the device status word that the tensor-core kernels set
+ * when one of their bounded waits gives up: GBFE_OK or GBFE_ERR_TIMEOUT. */
+int gbfe_ctx_check_status(gbfe_ctx *ctx);
+/* 1 (default): the FP32 apply uses the split-BF16 tcgen05 cell product;
+ * 0: the FP32 SIMT cell product (also selected by GBFE_TENSOR_CORES=0). */
+int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int on);
 /* number of kernels this context has launched so far */
 int gbfe_ctx_kernel_launches(const gbfe_ctx *ctx, uint64_t *count);
+/* Per-kernel timing (no counterpart in the reference, whose Profiler times
+ * host sections: utils/Profiler.h:44-85).  With profiling on, each launch of
+ * the cell-product kernels ("cell_apply_f64", "cell_apply_mixed") is bracketed
+ * by CUDA events on the launching stream; stats report launches, total device
+ * milliseconds and the algorithmic flops / bytes of those launches. */
+int gbfe_ctx_set_profiling(gbfe_ctx *ctx, int on);
+int gbfe_ctx_kernel_stats(gbfe_ctx *ctx, const char *name, uint64_t *launches, double *total_ms,
+                          double *flops, double *bytes);
+int gbfe_ctx_reset_kernel_stats(gbfe_ctx *ctx);
+/* Measured FP64 FMA throughput of this GPU (GFLOP/s), the roofline
+ * denominator of the FP64 cell product. */
+int gbfe_probe_fp64_peak(gbfe_ctx *ctx, double *gflops);
 
 /* ---- mesh: cell -> dof map ------------------------------------------------
  * Replaces FEBasisManager::nLocallyOwnedCells / nLocallyOwnedCellDofs /
@@ -114,6 +132,10 @@ int gbfe_op_destroy(gbfe_op *op);
 
 /* ---- block vectors (MultiVector) -------------------------------------------- */
 int gbfe_mv_create(gbfe_mesh *mesh, uint32_t m, int dtype, gbfe_mv **out);
+/* Wrap a caller-owned device buffer [n_dofs][m] (e.g. the data() of a
+ * reference MultiVector<..., MemorySpace::DEVICE>, MultiVector.h:133) without
+ * copying; gbfe_mv_destroy then releases only the handle. */
+int gbfe_mv_wrap(gbfe_mesh *mesh, uint32_t m, int dtype, void *device_ptr, gbfe_mv **out);
 int gbfe_mv_destroy(gbfe_mv *mv);
 int gbfe_mv_copy_in(gbfe_mv *mv, const void *host_rowmajor);
 int gbfe_mv_copy_out(const gbfe_mv *mv, void *host_rowmajor);
@@ -176,6 +198,12 @@ typedef struct {
   uint32_t lanczos_steps;       /* Krylov dimension (reference default 20)    */
   uint64_t lanczos_seed;
   int      fixed_passes;        /* 1: run exactly max_passes passes           */
+  int      faithful_passes;     /* 1: every pass repeats the reference's call
+                                   sequence (filter with its own A X, B X;
+                                   Cholesky-GS; Rayleigh-Ritz; residual with
+                                   fresh H X, M X: six FP64 applies per pass).
+                                   0: H X and M X are carried through the
+                                   m x m rotations (two FP64 applies per pass). */
 } gbfe_ks_params;
 
 /* ChebyshevFilteredEigenSolver::solve (ChebyshevFilteredEigenSolver.t.cpp:

@@ -38,3 +38,31 @@ def test_no_cpu_fallback_when_library_missing(tmp_path):
 
     with pytest.raises(ImportError):
         _lib.load(tmp_path / "absent.so")
+
+
+def test_operator_context_adapter_compiles_against_reference_headers(tmp_path):
+    """The C++ drop-in (include/gbfe_operator_context.hpp) type-checks against
+    the reference's own OperatorContext / MultiVector headers, instantiated
+    for HOST and DEVICE memory spaces.  Skipped where the reference sources are
+    not present."""
+    import os
+    import shutil
+    import subprocess
+
+    import pytest
+
+    ref = Path(os.environ.get("DFTEFE_REFERENCE", "/root/reference")) / "src"
+    if not ref.is_dir() or not shutil.which("g++"):
+        pytest.skip("reference sources not available")
+    src = tmp_path / "adapter.cpp"
+    src.write_text(
+        "#include <gbfe_operator_context.hpp>\n"
+        "using namespace dftefe;\n"
+        "template class dftefe::gb300::GpuCellOperatorContext<double, double, utils::MemorySpace::HOST>;\n"
+        "template class dftefe::gb300::GpuDiagonalOperatorContext<double, double, utils::MemorySpace::HOST>;\n"
+        "template class dftefe::gb300::GpuCellOperatorContext<float, float, utils::MemorySpace::HOST>;\n"
+        "int main() { return 0; }\n")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-DNDEBUG", "-w", f"-I{ROOT / 'include'}",
+                        f"-I{ROOT / 'oracle' / 'ref_harness' / 'shadow'}", f"-I{ref}", str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]

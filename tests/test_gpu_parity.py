@@ -182,7 +182,8 @@ def test_ortho_not_orthonormalizable(gpu_ctx):
     assert e.value.status in ("ERR_LAPACK", "ERR_NOT_ORTHONORMALIZABLE")
 
 
-def test_ks_eigen_solve_fp64_matches_oracle(gpu_ctx, small_problem):
+@pytest.mark.parametrize("faithful", [True, False])
+def test_ks_eigen_solve_fp64_matches_oracle(gpu_ctx, small_problem, faithful):
     from gbfe import api
 
     p = small_problem
@@ -196,7 +197,7 @@ def test_ks_eigen_solve_fp64_matches_oracle(gpu_ctx, small_problem):
         bounds = (b[0], (bounds[2] + b[0]) * 0.5, bounds[2])
     st, eig_ref, _, res_ref, passes_ref = s.ks_eigen_solve(oH, oM, oMi, X0, 12, 40, nw, 1e-9, bounds=bounds)
     X = api.MultiVector(basis, m, init=X0)
-    solver = api.KohnShamEigenSolver(nw, 12, 40, 1e-9, bounds=bounds)
+    solver = api.KohnShamEigenSolver(nw, 12, 40, 1e-9, bounds=bounds, faithful_passes=faithful)
     rc, eig, resid, passes = solver.solve(H, X, Mo, Mi)
     assert rc == 0 and st == 0
     assert np.abs(eig[:nw] - eig_ref[:nw]).max() <= 1e-8
@@ -228,7 +229,8 @@ def test_cg_fp64_matches_oracle(gpu_ctx, small_problem):
     assert rel_maxnorm(x.numpy(), x_o) <= 1e-8
 
 
-def test_mixed_apply_fp32(gpu_ctx, small_problem):
+def test_mixed_apply_fp32_simt(gpu_ctx, small_problem):
+    """FP32 SIMT cell product: <= 2e-6 relative max-norm against FP64."""
     from gbfe import api
 
     p = small_problem
@@ -240,5 +242,98 @@ def test_mixed_apply_fp32(gpu_ctx, small_problem):
     H.apply(X, Y)
     Xf = api.MultiVector(basis, 32, dtype=np.float32, init=X0.astype(np.float32))
     Yf = api.MultiVector(basis, 32, dtype=np.float32)
-    H.apply(Xf, Yf)
+    gpu_ctx.set_tensor_cores(False)
+    try:
+        H.apply(Xf, Yf)
+    finally:
+        gpu_ctx.set_tensor_cores(True)
     assert rel_maxnorm(Yf.numpy(), Y.numpy()) <= 2e-6
+
+
+TC_TOL = 1e-4  # split-BF16 (3 products, FP32 accumulation): ~2^-18 per operand
+
+
+@pytest.mark.parametrize("n,p,m", [(3, 3, 32), (3, 4, 64), (2, 5, 40), (2, 4, 300), (2, 3, 7)])
+def test_mixed_apply_tensor_cores(gpu_ctx, n, p, m):
+    """tcgen05 split-BF16 cell product against the FP64 apply of the same X
+    (cells of 64, 125 and 216 dofs; one and two 128-row M tiles; ragged and
+    multi-tile vector counts)."""
+    from gbfe import api
+
+    prob = M.ks_box(n, p, 2.0 * n, 1, 4.0, 0.5, seed=30 + p)
+    basis = api.FEBasisManager.from_problem(gpu_ctx, prob)
+    H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=True)
+    X0 = M.random_block(prob.n_dofs, m, 40 + m).astype(np.float32).astype(np.float64)
+    X = api.MultiVector(basis, m, init=X0)
+    Y = api.MultiVector(basis, m)
+    H.apply(X, Y)
+    Xf = api.MultiVector(basis, m, dtype=np.float32, init=X0.astype(np.float32))
+    Yf = api.MultiVector(basis, m, dtype=np.float32)
+    H.apply(Xf, Yf)
+    gpu_ctx.check_status()
+    err = rel_maxnorm(Yf.numpy(), Y.numpy())
+    print(f"tc apply n={n} p={p} m={m}: rel max-norm err {err:.2e}")
+    assert err <= TC_TOL
+
+
+def test_mixed_apply_tensor_cores_variable_nd(gpu_ctx):
+    from gbfe import api
+
+    rng = np.random.default_rng(17)
+    C, N = 50, 700
+    nd = np.concatenate([rng.integers(20, 41, size=C - 5), rng.integers(130, 160, size=5)]).astype(np.uint32)
+    ids = np.concatenate([rng.choice(N, size=k, replace=False) for k in nd]).astype(np.uint32)
+    mats = rng.standard_normal(int((nd.astype(np.int64) ** 2).sum()))
+    basis = api.FEBasisManager(gpu_ctx, nd, ids, N)
+    A = api.CellMatrixOperatorContext(basis, mats, mixed=True, use_constraints=False)
+    X0 = M.random_block(N, 24, 3).astype(np.float32).astype(np.float64)
+    X = api.MultiVector(basis, 24, init=X0)
+    Y = api.MultiVector(basis, 24)
+    A.apply(X, Y)
+    Xf = api.MultiVector(basis, 24, dtype=np.float32, init=X0.astype(np.float32))
+    Yf = api.MultiVector(basis, 24, dtype=np.float32)
+    A.apply(Xf, Yf)
+    gpu_ctx.check_status()
+    assert rel_maxnorm(Yf.numpy(), Y.numpy()) <= TC_TOL
+
+
+def test_mixed_residual_filter_close_to_fp64(gpu_ctx, small_problem):
+    """Mixed filter (FP32 recurrence, split-BF16 products) vs the FP64 filter:
+    the output is a filtered subspace, compared at 1e-3 relative max-norm."""
+    from gbfe import api
+
+    p = small_problem
+    basis, H, Mo, Mi, s, oH, oM, oMi = _setup(gpu_ctx, p, mixed=True)
+    m, deg = 8, 10
+    b = s.lanczos_bounds(oH, oM, oMi)
+    wl, wu, uu = b[0], b[0] + 0.1 * (b[1] - b[0]), b[1] + b[2] / 10
+    eig = np.linspace(-2, 1, m)
+    X0 = M.random_block(p.n_dofs, m, 12)
+    X = api.MultiVector(basis, m, init=X0)
+    Y64 = api.MultiVector(basis, m)
+    Y32 = api.MultiVector(basis, m)
+    api.ResidualChebyshevFilterGEP(H, Mo, Mi, eig, X, deg, wl, wu, uu, Y64)
+    X.copy_from(X0)
+    api.ResidualChebyshevFilterGEP(H, Mo, Mi, eig, X, deg, wl, wu, uu, Y32, mixed=True)
+    gpu_ctx.check_status()
+    assert rel_maxnorm(Y32.numpy(), Y64.numpy()) <= 1e-3
+
+
+def test_mixed_ks_solve_eigenvalues(gpu_ctx, small_problem):
+    """Mixed ChFSI (FP64 ortho / RR / residual) reaches the FP64 eigenvalues
+    within 1e-6 Ha."""
+    from gbfe import api
+
+    p = small_problem
+    basis, H, Mo, Mi, s, oH, oM, oMi = _setup(gpu_ctx, p, mixed=True)
+    m, nw = 10, 6
+    X0 = M.random_block(p.n_dofs, m, 15)
+    b = api.lanczos_bounds(H, Mo, Mi)
+    bounds = (b[0], b[0] + 0.1 * (b[1] - b[0]), b[1] + b[2] / 10)
+    X = api.MultiVector(basis, m, init=X0)
+    rc64, e64, r64, n64 = api.KohnShamEigenSolver(nw, 12, 60, 1e-8, bounds=bounds).solve(H, X, Mo, Mi)
+    X.copy_from(X0)
+    rc32, e32, r32, n32 = api.KohnShamEigenSolver(nw, 12, 60, 1e-8, mixed=True, bounds=bounds).solve(H, X, Mo, Mi)
+    gpu_ctx.check_status()
+    assert rc64 == 0 and rc32 == 0
+    assert np.abs(e32[:nw] - e64[:nw]).max() <= 1e-6
