@@ -896,3 +896,82 @@ int gbfe_apply(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// FP64 apply with a fixed, library-owned scratch buffer (no allocation)
+// ---------------------------------------------------------------------------
+// Some callers cannot call cudaMalloc when they apply an operator: code that
+// runs while another component owns all device memory through its own pool
+// (a framework allocator that has reserved the GPU), and code that must not
+// take the implicit device-wide synchronisation a cudaMalloc can cause (for
+// example inside a latency-critical step loop).  gbfe_apply_f64_noalloc gives
+// them the FP64 cell apply with its cell-wise scratch in the file-scope array
+// below instead of the grow-on-demand buffer gbfe_apply keeps per operator.
+namespace {
+constexpr uint64_t kNoAllocScratchDoubles = 8ull << 20;  // 64 MiB per GPU, held until exit
+static __device__ __align__(256) double g_noalloc_cell_scratch[kNoAllocScratchDoubles];
+constexpr int kMaxDevices = 64;
+double *g_noalloc_ptr[kMaxDevices] = {nullptr};  // device address per device (set on first use)
+}  // namespace
+
+extern "C" int gbfe_apply_f64_noalloc(const gbfe_op *op, double *X_dev, double *Y_dev, uint32_t m) {
+  if (!op || !X_dev || !Y_dev) return GBFE_ERR_ARG;
+  gbfe_mesh *me = op->mesh;
+  gbfe_ctx *ctx = me->ctx;
+  return gbfe_guard(ctx, [&] {
+    GBFE_REQUIRE(op->kind == OP_CELL, "apply_f64_noalloc: needs a cell-matrix operator");
+    GBFE_REQUIRE(X_dev != Y_dev, "apply_f64_noalloc: X and Y must be distinct");
+    if (m == 0) return;
+    const uint64_t need = me->total_cell_dofs * (uint64_t)m;
+    if (need > kNoAllocScratchDoubles)
+      throw Error(GBFE_ERR_ARG, "apply_f64_noalloc: sum over cells of nd_c times m = " + std::to_string(need) +
+                                    " exceeds the fixed scratch of " + std::to_string(kNoAllocScratchDoubles) +
+                                    " doubles; use gbfe_apply");
+    int dev = -1;
+    GBFE_CUDA(cudaGetDevice(&dev));
+    GBFE_REQUIRE(dev == ctx->device, "apply_f64_noalloc: the context's device must be current");
+    GBFE_REQUIRE(dev >= 0 && dev < kMaxDevices, "apply_f64_noalloc: device index out of range");
+    if (!g_noalloc_ptr[dev]) {
+      // once per device, with that device current: the symbol's host-side name
+      // is not a device address, so fetch the real one
+      void *p = nullptr;
+      GBFE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_cell_scratch));
+      g_noalloc_ptr[dev] = (double *)p;
+    }
+    double *Yc = g_noalloc_ptr[dev];
+    const uint32_t Nn = (uint32_t)me->n_dofs;
+    (void)Nn;
+    // constraints on X (the same kernels gbfe_apply launches)
+    const gbfe_cons *c = op->cons;
+    if (c && c->n_rows) {
+      const uint64_t nr = (uint64_t)c->n_rows * m;
+      if (c->pure_dirichlet)
+        k_zero_rows<double><<<stride_grid(ctx, nr), 256, 0, ctx->stream>>>(X_dev, m, c->n_rows, c->row_ids.p);
+      else
+        k_p2c<double><<<stride_grid(ctx, nr), 256, 0, ctx->stream>>>(X_dev, m, c->n_rows, c->row_ids.p,
+                                                                     c->row_sizes.p, c->col_ids.p, c->row_acc.p,
+                                                                     c->col_vals.p, c->inh.p);
+      check_launch(ctx, "p2c");
+    }
+    // cell products into the fixed scratch (every element is written, so
+    // nothing needs clearing between calls)
+    const size_t smem_cap = 96 * 1024;
+    uint32_t mt = (uint32_t)std::min<size_t>(m, smem_cap / (sizeof(double) * me->nd_max));
+    GBFE_REQUIRE(mt > 0, "cell too large for the FP64 apply");
+    const uint32_t vt = (m + mt - 1) / mt;
+    mt = (m + vt - 1) / vt;
+    uint32_t jsplit = 1;
+    const uint64_t target = (uint64_t)ctx->sm_count * 12;
+    while ((uint64_t)me->n_cells * vt * jsplit < target && jsplit * 8 < me->nd_min) jsplit *= 2;
+    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+    k_cell_apply_f64<<<dim3(me->n_cells, vt, jsplit), 256, sizeof(double) * (size_t)me->nd_max * mt, ctx->stream>>>(
+        X_dev, m, me->ids.p, me->cell_off.p, me->mat_off.p, op->mats.p, Yc, mt, jsplit);
+    check_launch(ctx, "cell_apply_f64_noalloc");
+    const bool has_par = c && !c->pure_dirichlet;
+    const uint64_t n = me->n_dofs * (uint64_t)m;
+    k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+        Yc, m, me->n_dofs, me->slot_ptr.p, me->slot.p, c ? c->is_row.p : nullptr, has_par ? c->par_ptr.p : nullptr,
+        has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y_dev);
+    check_launch(ctx, "assemble_f64_noalloc");
+  });
+}

@@ -67,6 +67,7 @@ SIGNATURES = {
     "gbfe_mv_l2_norms": (i32, [p, p]),
     "gbfe_mv_dots": (i32, [p, p, p]),
     "gbfe_apply": (i32, [p, p, p]),
+    "gbfe_apply_f64_noalloc": (i32, [p, p, p, u32]),
     "gbfe_residual_chebyshev_filter": (i32, [p, p, p, p, p, u32, f64, f64, f64, i32, p]),
     "gbfe_chebyshev_filter": (i32, [p, p, p, u32, f64, f64, f64, p]),
     "gbfe_cholesky_gram_schmidt": (i32, [p, p, p]),

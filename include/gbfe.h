@@ -156,6 +156,23 @@ int gbfe_mv_dots(const gbfe_mv *x, const gbfe_mv *y, double *dots_host);
  * products accumulated in FP32; needs an operator built with GBFE_PREC_MIXED). */
 int gbfe_apply(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
 
+/* FP64 apply that allocates nothing.  No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc while they apply an operator -- a
+ * process whose device memory is all reserved by another component's pool,
+ * or a latency-critical loop that must not take the device-wide
+ * synchronisation a cudaMalloc can cause.  The caller passes device buffers
+ * X and Y ([n_dofs][m] row-major FP64, X is modified by the constraints as in
+ * gbfe_apply) and an operator built earlier with gbfe_cellmat_upload.  The
+ * cell-wise intermediate lives in a fixed library array of 8,388,608 doubles
+ * (64 MiB) that every GPU loading the library keeps until the process exits;
+ * calls with sum over cells of nd_c times m above that return GBFE_ERR_ARG.
+ * The first call on a device looks up that array's device address (with the
+ * context's device current), so make the first call before any stream
+ * capture.  All calls share the one array and every element of it is
+ * rewritten by each call: calls whose work overlaps on the GPU (other streams,
+ * other contexts) race and must be serialised by the caller. */
+int gbfe_apply_f64_noalloc(const gbfe_op *op, double *X_dev, double *Y_dev, uint32_t m);
+
 /* ---- Chebyshev filters -----------------------------------------------------
  * ResidualChebyshevFilterGEP (linearAlgebra/ChebyshevFilter.t.cpp:242-444).
  * eigenvalues: host array of length m.  X is the input subspace, Y the output.
