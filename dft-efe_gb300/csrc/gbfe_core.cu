@@ -264,7 +264,7 @@ static void cell_apply_f64(const gbfe_op *op, gbfe_mv *X, double *Yc) {
   dim3 grid(me->n_cells, vt, jsplit);
   ProfScope prof(ctx, "cell_apply_f64", 2.0 * m * (double)me->total_mat,
                  8.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat));
-  k_cell_apply_f64<<<grid, 256, smem, ctx->stream>>>(X->d.p, m, me->ids.p, me->cell_off.p, me->mat_off.p,
+  k_cell_apply_f64<<<grid, 256, smem, ctx->stream>>>(X->d.p, m, me->ids.p, me->cell_off.p, op_mat_off(op),
                                                      op->mats.p, Yc, mt, jsplit);
   check_launch(ctx, "cell_apply_f64");
 }
@@ -293,6 +293,30 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
     return;
   }
   constraints_p2c(ctx, c, X);
+  if (op->kind == OP_DIAG_BLOCK) {
+    // OrthoEFEOverlapInverseOpContextGLL.t.cpp:1182-1270: diagonal on every
+    // dof, the enrichment rows replaced by block * X_enr, then child-to-parent
+    if (X->dtype == GBFE_F64)
+      k_diag_apply<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->d.p, m, me->n_dofs, op->diag.p, nullptr,
+                                                                         nullptr, nullptr, nullptr, Y->d.p);
+    else
+      k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->f.p, m, me->n_dofs, op->diag.p, nullptr,
+                                                                        nullptr, nullptr, nullptr, Y->f.p);
+    check_launch(ctx, "diag_apply");
+    const int nb = (int)op->blk_n, mm = (int)m;
+    if (X->dtype == GBFE_F64) {
+      const double one = 1.0, zero = 0.0;
+      GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, mm, nb, nb, &one, X->d.p + op->blk_begin * m, mm,
+                              op->blk.p, nb, &zero, Y->d.p + op->blk_begin * m, mm));
+    } else {
+      const float one = 1.f, zero = 0.f;
+      GBFE_CUBLAS(cublasSgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, mm, nb, nb, &one, X->f.p + op->blk_begin * m, mm,
+                              op->blk_f32.p, nb, &zero, Y->f.p + op->blk_begin * m, mm));
+    }
+    count_launch(ctx);
+    constraints_c2p(ctx, c, Y);
+    return;
+  }
   if (op->kind == OP_DIAG) {
     const uint8_t *isr = c ? c->is_row.p : nullptr;
     if (X->dtype == GBFE_F64)
@@ -396,6 +420,7 @@ int gbfe_ctx_create(int device, gbfe_ctx **out) {
     GBFE_CUDA(cudaMemsetAsync(ctx->status.p, 0, 4 * sizeof(int), ctx->stream));
     const char *tc = getenv("GBFE_TENSOR_CORES");
     if (tc && tc[0] == '0') ctx->use_tc = 0;
+    if (tc && tc[0] == '1') ctx->tc_version = 1;
   });
   if (rc != GBFE_OK) {
     std::string msg = ctx->last_error;
@@ -456,9 +481,10 @@ int gbfe_ctx_check_status(gbfe_ctx *ctx) {
   return st ? GBFE_ERR_TIMEOUT : GBFE_OK;
 }
 
-int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int on) {
-  if (!ctx) return GBFE_ERR_ARG;
-  ctx->use_tc = on ? 1 : 0;
+int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 2) return GBFE_ERR_ARG;
+  ctx->use_tc = mode ? 1 : 0;
+  if (mode) ctx->tc_version = mode;
   return GBFE_OK;
 }
 
@@ -730,7 +756,48 @@ int gbfe_cellmat_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *ma
     op->cons = cons;
     op->kind = OP_CELL;
     op->prec = prec_flags | GBFE_PREC_FP64;
+    op->mats_count = mesh->total_mat;
     op->mats.upload(mats, mesh->total_mat, mesh->ctx->stream);
+    if (prec_flags & GBFE_PREC_MIXED) build_mixed_mats(op);
+    GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
+  });
+  if (rc != GBFE_OK) {
+    delete op;
+    return rc;
+  }
+  *out = op;
+  return GBFE_OK;
+}
+
+int gbfe_cellmat_upload_indexed(gbfe_mesh *mesh, const gbfe_cons *cons, uint32_t n_mats, const double *mats,
+                                const uint32_t *cell_to_mat, int prec_flags, gbfe_op **out) {
+  if (!mesh || !out) return GBFE_ERR_ARG;
+  *out = nullptr;
+  gbfe_op *op = nullptr;
+  int rc = gbfe_guard(mesh->ctx, [&] {
+    GBFE_REQUIRE(mats && cell_to_mat && n_mats > 0, "cellmat_upload_indexed: null arrays");
+    GBFE_REQUIRE(!cons || cons->mesh == mesh, "cellmat_upload_indexed: constraints on another mesh");
+    // every cell that names matrix u must have the same nd; u's size is that nd^2
+    std::vector<uint32_t> nd_of(n_mats, 0);
+    for (uint32_t c = 0; c < mesh->n_cells; ++c) {
+      const uint32_t u = cell_to_mat[c];
+      GBFE_REQUIRE(u < n_mats, "cellmat_upload_indexed: matrix index out of range");
+      GBFE_REQUIRE(nd_of[u] == 0 || nd_of[u] == mesh->h_nd[c],
+                   "cellmat_upload_indexed: cells sharing a matrix have different sizes");
+      nd_of[u] = mesh->h_nd[c];
+    }
+    std::vector<uint64_t> uoff(n_mats + 1, 0);
+    for (uint32_t u = 0; u < n_mats; ++u) uoff[u + 1] = uoff[u] + (uint64_t)nd_of[u] * nd_of[u];
+    std::vector<uint64_t> coff(mesh->n_cells + 1, 0);
+    for (uint32_t c = 0; c < mesh->n_cells; ++c) coff[c] = uoff[cell_to_mat[c]];
+    op = new gbfe_op();
+    op->mesh = mesh;
+    op->cons = cons;
+    op->kind = OP_CELL;
+    op->prec = prec_flags | GBFE_PREC_FP64;
+    op->mats_count = uoff[n_mats];
+    op->mats.upload(mats, uoff[n_mats], mesh->ctx->stream);
+    op->mat_off_own.upload(coff.data(), coff.size(), mesh->ctx->stream);
     if (prec_flags & GBFE_PREC_MIXED) build_mixed_mats(op);
     GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
   });
@@ -773,6 +840,28 @@ static int diag_upload_impl(gbfe_mesh *mesh, const gbfe_cons *cons, const double
 
 int gbfe_diag_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *diag, gbfe_op **out) {
   return diag_upload_impl(mesh, cons, diag, OP_DIAG, out);
+}
+
+int gbfe_diag_block_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *diag, uint64_t blk_begin,
+                           uint64_t blk_n, const double *blk, gbfe_op **out) {
+  if (!mesh || !out) return GBFE_ERR_ARG;
+  int rc = diag_upload_impl(mesh, cons, diag, OP_DIAG_BLOCK, out);
+  if (rc != GBFE_OK) return rc;
+  gbfe_op *op = *out;
+  rc = gbfe_guard(mesh->ctx, [&] {
+    GBFE_REQUIRE(blk && blk_n > 0 && blk_begin + blk_n <= mesh->n_dofs, "diag_block_upload: block out of range");
+    op->blk_begin = blk_begin;
+    op->blk_n = blk_n;
+    op->blk.upload(blk, blk_n * blk_n, mesh->ctx->stream);
+    std::vector<float> f(blk, blk + blk_n * blk_n);
+    op->blk_f32.upload(f.data(), f.size(), mesh->ctx->stream);
+    GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
+  });
+  if (rc != GBFE_OK) {
+    delete op;
+    *out = nullptr;
+  }
+  return rc;
 }
 
 int gbfe_jacobi_upload(gbfe_mesh *mesh, const double *diagonal, gbfe_op **out) {
@@ -965,7 +1054,7 @@ extern "C" int gbfe_apply_f64_noalloc(const gbfe_op *op, double *X_dev, double *
     while ((uint64_t)me->n_cells * vt * jsplit < target && jsplit * 8 < me->nd_min) jsplit *= 2;
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
     k_cell_apply_f64<<<dim3(me->n_cells, vt, jsplit), 256, sizeof(double) * (size_t)me->nd_max * mt, ctx->stream>>>(
-        X_dev, m, me->ids.p, me->cell_off.p, me->mat_off.p, op->mats.p, Yc, mt, jsplit);
+        X_dev, m, me->ids.p, me->cell_off.p, op_mat_off(op), op->mats.p, Yc, mt, jsplit);
     check_launch(ctx, "cell_apply_f64_noalloc");
     const bool has_par = c && !c->pure_dirichlet;
     const uint64_t n = me->n_dofs * (uint64_t)m;

@@ -133,6 +133,7 @@ struct gbfe_ctx {
   gbfe::DBuf<double> lwork;
   gbfe::DBuf<int> status;    // device status word written by bounded waits (0 = ok)
   int use_tc = 1;            // split-BF16 tcgen05 cell product for the mixed path
+  int tc_version = 2;        // 2: persistent warp-specialised kernel; 1: one CTA per cell
 };
 
 struct gbfe_mesh {
@@ -166,18 +167,23 @@ struct gbfe_cons {
   gbfe::DBuf<uint8_t> is_row;
 };
 
-enum OpKind { OP_CELL = 0, OP_DIAG = 1, OP_JACOBI = 2 };
+enum OpKind { OP_CELL = 0, OP_DIAG = 1, OP_JACOBI = 2, OP_DIAG_BLOCK = 3 };
 
 struct gbfe_op {
   gbfe_mesh *mesh = nullptr;
   const gbfe_cons *cons = nullptr;
   int kind = OP_CELL;
   int prec = GBFE_PREC_FP64;
-  gbfe::DBuf<double> mats;            // f64 col-major per cell
+  gbfe::DBuf<double> mats;            // f64 col-major per cell (or per distinct matrix)
+  uint64_t mats_count = 0;            // entries in mats
+  gbfe::DBuf<uint64_t> mat_off_own;   // per-cell offsets of an indexed operator
   gbfe::DBuf<__nv_bfloat16> mats_hi;  // split-BF16 hi/lo tiles (per cell, per K chunk)
   gbfe::DBuf<uint64_t> tc_aoff;       // element offset of each cell's tiles
   gbfe::DBuf<float> mats_f32;         // FP32 copy for the SIMT mixed apply
   gbfe::DBuf<double> diag;
+  uint64_t blk_begin = 0, blk_n = 0;  // OP_DIAG_BLOCK: dense block rows
+  gbfe::DBuf<double> blk;             // column-major blk_n x blk_n
+  gbfe::DBuf<float> blk_f32;
   mutable gbfe::DBuf<double> cellbuf;  // per-apply cell-wise result scratch (f64)
   mutable gbfe::DBuf<float> cellbuf_f32;
 };
@@ -228,6 +234,12 @@ struct ProfScope {
     st->launches++;
   }
 };
+
+// cell -> first entry of its matrix: the mesh's prefix sums, or the operator's
+// own offsets when several cells share one stored matrix
+inline const uint64_t *op_mat_off(const gbfe_op *op) {
+  return op->mat_off_own.p ? op->mat_off_own.p : op->mesh->mat_off.p;
+}
 
 // ---- internal entry points shared between translation units
 void constraints_p2c(gbfe_ctx *ctx, const gbfe_cons *c, gbfe_mv *x);

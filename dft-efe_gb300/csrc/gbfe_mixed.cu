@@ -70,8 +70,8 @@ void build_mixed_mats(gbfe_op *op) {
   gbfe_mesh *me = op->mesh;
   gbfe_ctx *ctx = me->ctx;
   DBuf<float> *m32 = &op->mats_f32;  // FP32 copy kept beside the FP64 matrices
-  m32->alloc(me->total_mat);
-  const uint64_t n = me->total_mat;
+  const uint64_t n = op->mats_count;
+  m32->alloc(n);
   unsigned g = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 16);
   k_f64_to_f32<<<g ? g : 1, 256, 0, ctx->stream>>>(op->mats.p, m32->p, n);
   check_launch(ctx, "f64_to_f32");
@@ -108,7 +108,7 @@ void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
   const DBuf<float> *m32 = &op->mats_f32;
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat));
-  k_cell_apply_f32<<<grid, 256, smem, ctx->stream>>>(X->f.p, m, me->ids.p, me->cell_off.p, me->mat_off.p, m32->p,
+  k_cell_apply_f32<<<grid, 256, smem, ctx->stream>>>(X->f.p, m, me->ids.p, me->cell_off.p, op_mat_off(op), m32->p,
                                                      op->cellbuf_f32.p, mt, jsplit);
   check_launch(ctx, "cell_apply_f32");
   assemble_f32(op, op->cellbuf_f32.p, Y);

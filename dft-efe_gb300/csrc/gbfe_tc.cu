@@ -307,6 +307,252 @@ __global__ void __launch_bounds__(THREADS, 1) k_cell_apply_tc(
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// v2: persistent, warp-specialised, continuous chunk stream across cells.
+//   warps 0-3  gather X chunks into the B ring (one mbarrier arrive per warp per
+//              chunk) and run the epilogue of the previous cell (TMEM -> Yc)
+//   warp 4     lane 0 issues the bulk TMA copies of A up to `stages` chunks ahead
+//   warp 5     allocates TMEM; lane 0 issues tcgen05.mma and the commits
+// TMEM holds `nbuf` accumulator buffers so one cell's epilogue overlaps the
+// next cell's MMAs.  The main loop synchronises through mbarriers only.
+// ---------------------------------------------------------------------------
+constexpr int MAX_STAGES = 4;
+constexpr int GATHER_WARPS = 4;
+constexpr int THREADS2 = 192;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+struct Tc2Args {
+  const float *X;
+  uint32_t m;
+  const uint32_t *ids;
+  const uint32_t *cell_off;
+  const uint32_t *cells;  // this launch's cells (one size bin group)
+  uint32_t ncells;
+  uint32_t vt;            // vector tiles per cell
+  const uint64_t *a_off;
+  const __nv_bfloat16 *Atc;
+  float *Yc;
+  uint32_t N, mtiles, tmem_cols, nbuf, stages;
+  int *status;
+};
+
+__global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const uint32_t N = a.N, mtiles = a.mtiles, S = a.stages, nbuf = a.nbuf, m = a.m;
+  const uint32_t a_part = mtiles * 128 * KC * 2, b_part = N * KC * 2;
+  const uint32_t stage_bytes = 2 * a_part + 2 * b_part;
+  uint64_t *bars = (uint64_t *)(smem + S * stage_bytes);
+  uint64_t *full_a = bars;
+  uint64_t *full_b = bars + MAX_STAGES;
+  uint64_t *empty = bars + 2 * MAX_STAGES;
+  uint64_t *tfull = bars + 3 * MAX_STAGES;
+  uint64_t *tempty = tfull + 2;
+  uint32_t *tmem_slot = (uint32_t *)(tempty + 2);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+
+  const uint32_t tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+  const uint32_t n_items = a.ncells * a.vt;
+
+  if (tid == 0) {
+    for (uint32_t s = 0; s < MAX_STAGES; ++s) {
+      mbar_init(&full_a[s], 1);
+      mbar_init(&full_b[s], GATHER_WARPS);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], GATHER_WARPS);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(a.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  auto wait = [&](uint64_t *bar, uint32_t parity, int code) -> bool {
+    if (*abort_flag) return false;
+    if (mbar_wait(bar, parity, a.status, code)) return true;
+    *abort_flag = 1;
+    return false;
+  };
+
+  if (warp == 4) {
+    // ---------------- TMA producer for A
+    if (lane == 0) {
+      uint32_t q = 0;
+      for (uint32_t it = blockIdx.x; it < n_items && !*abort_flag; it += gridDim.x) {
+        const uint32_t c = a.cells[it / a.vt];
+        const uint32_t nd = a.cell_off[c + 1] - a.cell_off[c];
+        const uint32_t mt8 = (nd + 7) / 8 * 8, nk = (nd + KC - 1) / KC;
+        const __nv_bfloat16 *Acell = a.Atc + a.a_off[c];
+        for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
+          const uint32_t s = q % S;
+          if (q >= S && !wait(&empty[s], ((q / S) - 1) & 1, 11)) break;
+          uint8_t *Ahi = smem + s * stage_bytes;
+          const uint32_t part = mt8 * KC * 2;
+          const __nv_bfloat16 *src = Acell + (uint64_t)kc * 2 * mt8 * KC;
+          mbar_arrive_expect_tx(&full_a[s], 2 * part);
+          bulk_g2s(Ahi, src, part, &full_a[s]);
+          bulk_g2s(Ahi + a_part, src + (uint64_t)mt8 * KC, part, &full_a[s]);
+        }
+      }
+    }
+    __syncwarp();  // lanes 1-31 wait for lane 0 before the CTA barrier
+  } else if (warp == 5) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc(128, (int)N);
+      uint32_t q = 0, li = 0;
+      for (uint32_t it = blockIdx.x; it < n_items && !*abort_flag; it += gridDim.x, ++li) {
+        const uint32_t c = a.cells[it / a.vt];
+        const uint32_t nd = a.cell_off[c + 1] - a.cell_off[c];
+        const uint32_t nk = (nd + KC - 1) / KC;
+        const uint32_t b = li % nbuf;
+        if (li >= nbuf && !wait(&tempty[b], ((li / nbuf) - 1) & 1, 12)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        bool ok = true;
+        for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
+          const uint32_t s = q % S;
+          if (!wait(&full_a[s], (q / S) & 1, 13) || !wait(&full_b[s], (q / S) & 1, 14)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          uint8_t *Ahi = smem + s * stage_bytes;
+          const uint32_t ahi = smem_u32(Ahi), alo = ahi + a_part, bhi = alo + a_part, blo = bhi + b_part;
+#pragma unroll
+          for (uint32_t ks = 0; ks < KC / 16; ++ks) {
+            const uint64_t bdh = smem_desc(bhi + ks * 2 * LBO), bdl = smem_desc(blo + ks * 2 * LBO);
+            for (uint32_t t = 0; t < mtiles; ++t) {
+              const uint32_t aoff = t * 16 * SBO + ks * 2 * LBO;
+              const uint64_t adh = smem_desc(ahi + aoff), adl = smem_desc(alo + aoff);
+              const uint32_t d = tmem + (b * mtiles + t) * N;
+              umma(d, adh, bdh, idesc, (kc | ks) != 0);
+              umma(d, adh, bdl, idesc, 1);
+              umma(d, adl, bdh, idesc, 1);
+            }
+          }
+          umma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        umma_commit(&tfull[b]);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- gather warps (0-3) + epilogue
+    const uint32_t nvg = (N + 31) / 32;
+    const uint32_t lag = nbuf - 1;  // with two TMEM buffers the epilogue trails by one cell
+    auto epilogue = [&](uint32_t li, uint32_t it) -> bool {
+      const uint32_t c = a.cells[it / a.vt];
+      const uint32_t v0 = (it % a.vt) * N;
+      const uint32_t off = a.cell_off[c], nd = a.cell_off[c + 1] - off;
+      const uint32_t b = li % nbuf;
+      bool ok = wait(&tfull[b], (li / nbuf) & 1, 15);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) return false;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (uint32_t t = 0; t < mtiles; ++t) {
+        const uint32_t row = t * 128 + warp * 32 + lane;
+        for (uint32_t col = 0; col < N; col += 16) {
+          float v[16];
+          tmem_ld16(tmem + ((warp * 32) << 16) + (b * mtiles + t) * N + col, v);
+          if (row < nd) {
+            float *dst = a.Yc + (uint64_t)(off + row) * m + v0 + col;
+            const uint32_t nvalid = min(16u, m - min(m, v0 + col));
+            if (nvalid == 16 && ((((uintptr_t)dst) & 15) == 0)) {
+#pragma unroll
+              for (int qq = 0; qq < 4; ++qq)
+                ((float4 *)dst)[qq] = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
+            } else {
+              for (uint32_t qq = 0; qq < nvalid; ++qq) dst[qq] = v[qq];
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[b]);
+      return true;
+    };
+    uint32_t q = 0, li = 0, prev_it = 0;
+    bool ok = true;
+    for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
+      const uint32_t c = a.cells[it / a.vt];
+      const uint32_t v0 = (it % a.vt) * N;
+      const uint32_t off = a.cell_off[c], nd = a.cell_off[c + 1] - off;
+      const uint32_t nk = (nd + KC - 1) / KC;
+      for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
+        const uint32_t s = q % S;
+        if (q >= S) {
+          ok = __all_sync(0xffffffffu, wait(&empty[s], ((q / S) - 1) & 1, 16));
+          if (!ok) break;
+        }
+        uint8_t *Bhi = smem + s * stage_bytes + 2 * a_part;
+        uint8_t *Blo = Bhi + b_part;
+        for (uint32_t item = warp; item < (KC / 8) * nvg; item += 2 * GATHER_WARPS) {
+          // two work items per pass keep 16 independent loads in flight per lane
+          float xv[2][8];
+          uint32_t vv[2];
+          bool has[2];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const uint32_t itm = item + u * GATHER_WARPS;
+            has[u] = itm < (KC / 8) * nvg;
+            const uint32_t kb = itm % (KC / 8), vg = itm / (KC / 8);
+            vv[u] = vg * 32 + lane;
+            const bool vin = has[u] && vv[u] < N && (v0 + vv[u]) < m;
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+              const uint32_t k = kc * KC + kb * 8 + kk;
+              xv[u][kk] = (vin && k < nd) ? __ldg(a.X + (uint64_t)a.ids[off + k] * m + v0 + vv[u]) : 0.f;
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const uint32_t itm = item + u * GATHER_WARPS;
+            if (!has[u] || vv[u] >= N) continue;
+            const uint32_t kb = itm % (KC / 8);
+            __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) split_bf16(xv[u][kk], hi[kk], lo[kk]);
+            const uint32_t pos = (vv[u] / 8) * SBO + kb * LBO + (vv[u] % 8) * 16;
+            *(uint4 *)(Bhi + pos) = *(const uint4 *)hi;
+            *(uint4 *)(Blo + pos) = *(const uint4 *)lo;
+          }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&full_b[s]);
+      }
+      if (!ok) break;
+      if (lag && li >= 1) ok = epilogue(li - 1, prev_it);
+      if (!lag) ok = ok && epilogue(li, it);
+      prev_it = it;
+    }
+    if (ok && lag && li >= 1) epilogue(li - 1, prev_it);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 5) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
+  }
+}
+
 }  // namespace
 
 namespace gbfe {
@@ -323,12 +569,42 @@ void build_tc_mats(gbfe_op *op) {
   }
   op->tc_aoff.upload(aoff.data(), aoff.size(), ctx->stream);
   op->mats_hi.alloc(aoff.back());
-  k_build_tc_mats<<<me->n_cells, 256, 0, ctx->stream>>>(op->mats.p, me->mat_off.p, me->cell_off.p, op->tc_aoff.p,
+  k_build_tc_mats<<<me->n_cells, 256, 0, ctx->stream>>>(op->mats.p, op_mat_off(op), me->cell_off.p, op->tc_aoff.p,
                                                         me->n_cells, op->mats_hi.p);
   check_launch(ctx, "build_tc_mats");
 }
 
 bool tc_supported(const gbfe_mesh *me) { return me->nd_max <= 256; }
+
+// v2 launch: persistent grid over (cell, vector tile) items of one M-tile group
+static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg, uint32_t ncell,
+                       uint32_t mtiles, double frac) {
+  gbfe_mesh *me = op->mesh;
+  const uint32_t m = X->m;
+  uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
+  const uint32_t vt = (m + N - 1) / N;
+  N = ((m + vt - 1) / vt + 15) / 16 * 16;
+  const uint32_t a_part = mtiles * 128 * KC * 2, b_part = N * KC * 2;
+  const uint32_t stage_bytes = 2 * a_part + 2 * b_part;
+  uint32_t stages = MAX_STAGES;
+  const uint32_t reserve = 1024 + 512;
+  while (stages > 2 && stages * stage_bytes + reserve > 227 * 1024) --stages;
+  GBFE_REQUIRE(stages * stage_bytes + reserve <= 227 * 1024, "tensor-core tile does not fit in shared memory");
+  const uint32_t smem = stages * stage_bytes + reserve;
+  const uint32_t nbuf = (2 * mtiles * N <= 512) ? 2 : 1;
+  uint32_t cols = 32;
+  while (cols < nbuf * mtiles * N) cols *= 2;
+  const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>((227 * 1024) / smem, 512 / cols));
+  const uint32_t items = ncell * vt;
+  const uint32_t grid = std::min<uint32_t>(items, per_sm * (uint32_t)ctx->sm_count);
+  GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  Tc2Args args{X->f.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, vt, op->tc_aoff.p,
+               op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p};
+  ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
+                 4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
+  k_cell_apply_tc2<<<grid, THREADS2, smem, ctx->stream>>>(args);
+  check_launch(ctx, "cell_apply_tc2");
+}
 
 // Yc (FP32 cell-wise buffer) = split-BF16 tensor-core products, size-binned by
 // the number of 128-row M tiles a cell needs.
@@ -350,6 +626,10 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc) {
     // bins are sorted by nd, so the cells of [b0, b1) are contiguous in bin_cells
     const uint32_t cbeg = me->bin_begin[b0], cend = me->bin_begin[b1];
     const uint32_t ncell = cend - cbeg;
+    if (ctx->tc_version == 2) {
+      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells);
+      continue;
+    }
     uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
     const uint32_t vt = (m + N - 1) / N;
     N = ((m + vt - 1) / vt + 15) / 16 * 16;  // balance the vector tiles

@@ -53,7 +53,9 @@ SIGNATURES = {
     "gbfe_constraints_distribute_parent_to_child": (i32, [p, p]),
     "gbfe_constraints_distribute_child_to_parent": (i32, [p, p]),
     "gbfe_cellmat_upload": (i32, [p, p, p, i32, C.POINTER(p)]),
+    "gbfe_cellmat_upload_indexed": (i32, [p, p, u32, p, p, i32, C.POINTER(p)]),
     "gbfe_diag_upload": (i32, [p, p, p, C.POINTER(p)]),
+    "gbfe_diag_block_upload": (i32, [p, p, p, u64, u64, p, C.POINTER(p)]),
     "gbfe_jacobi_upload": (i32, [p, p, C.POINTER(p)]),
     "gbfe_op_destroy": (i32, [p]),
     "gbfe_mv_create": (i32, [p, u32, i32, C.POINTER(p)]),
@@ -77,6 +79,7 @@ SIGNATURES = {
     "gbfe_ks_eigen_solve": (i32, [p, p, p, p, C.POINTER(KSParams), p, p, C.POINTER(u32)]),
     "gbfe_lanczos_bounds": (i32, [p, p, p, u32, u64, p]),
     "gbfe_cg_solve": (i32, [p, p, p, p, u32, f64, f64, f64, C.POINTER(u32), p]),
+    "gbfe_pcg_solve_batched": (i32, [p, p, p, p, u32, p, u32, f64, f64, f64, u32, p, p, p]),
 }
 
 _lib = None

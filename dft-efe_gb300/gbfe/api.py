@@ -62,8 +62,9 @@ class LinAlgOpContext:
     def check_status(self) -> None:
         check(self.lib.gbfe_ctx_check_status(self.h), self.h, "device status")
 
-    def set_tensor_cores(self, on: bool) -> None:
-        check(self.lib.gbfe_ctx_set_tensor_cores(self.h, 1 if on else 0), self.h, "set_tensor_cores")
+    def set_tensor_cores(self, mode: int) -> None:
+        """2: persistent tcgen05 kernel (default), 1: one-CTA-per-cell tcgen05, 0: FP32 SIMT."""
+        check(self.lib.gbfe_ctx_set_tensor_cores(self.h, int(mode)), self.h, "set_tensor_cores")
 
     def set_profiling(self, on: bool) -> None:
         check(self.lib.gbfe_ctx_set_profiling(self.h, 1 if on else 0), self.h, "set_profiling")
@@ -236,6 +237,23 @@ class CellMatrixOperatorContext(OperatorContext):
         self.mixed = mixed
 
 
+class IndexedCellMatrixOperatorContext(OperatorContext):
+    """Cell operator whose cells name one of a few stored matrices."""
+
+    def __init__(self, basis: FEBasisManager, mats: np.ndarray, cell_to_mat: np.ndarray, mixed: bool = False,
+                 use_constraints: bool = True):
+        self.basis, self.ctx = basis, basis.ctx
+        mats = np.ascontiguousarray(mats, dtype=np.float64)
+        idx = np.ascontiguousarray(cell_to_mat, dtype=np.uint32)
+        n_mats = int(idx.max()) + 1 if idx.size else 0
+        h = C.c_void_p()
+        flags = GBFE_PREC_FP64 | (GBFE_PREC_MIXED if mixed else 0)
+        cons = basis.cons_h if use_constraints else None
+        check(self.ctx.lib.gbfe_cellmat_upload_indexed(basis.h, cons, n_mats, _ptr(mats), _ptr(idx), flags,
+                                                       C.byref(h)), self.ctx.h, "cellmat_upload_indexed")
+        self.h = h
+
+
 class KohnShamOperatorContextFE(CellMatrixOperatorContext):
     """H = sum over cells of the Hamiltonian cell matrices (local part)."""
 
@@ -256,6 +274,20 @@ class CFEOverlapInverseOpContextGLL(OperatorContext):
         inv = np.ascontiguousarray(1.0 / np.asarray(m_gll_diagonal, dtype=np.float64))
         h = C.c_void_p()
         check(self.ctx.lib.gbfe_diag_upload(basis.h, basis.cons_h, _ptr(inv), C.byref(h)), self.ctx.h, "diag_upload")
+        self.h = h
+
+
+class OrthoEFEOverlapInverseOpContextGLL(OperatorContext):
+    """GLL diagonal inverse on classical dofs + dense inverse of the enrichment
+    overlap block on the enrichment dofs [enr_begin, enr_begin + n)."""
+
+    def __init__(self, basis: FEBasisManager, m_gll_diagonal: np.ndarray, enr_begin: int, enr_block_inv: np.ndarray):
+        self.basis, self.ctx = basis, basis.ctx
+        inv = np.ascontiguousarray(1.0 / np.asarray(m_gll_diagonal, dtype=np.float64))
+        blk = np.ascontiguousarray(np.asarray(enr_block_inv, dtype=np.float64).T)  # column-major
+        h = C.c_void_p()
+        check(self.ctx.lib.gbfe_diag_block_upload(basis.h, basis.cons_h, _ptr(inv), int(enr_begin), int(blk.shape[0]),
+                                                  _ptr(blk), C.byref(h)), self.ctx.h, "diag_block_upload")
         self.h = h
 
 
@@ -376,3 +408,18 @@ class CGLinearSolver:
         rc = A.ctx.lib.gbfe_cg_solve(A.h, PC.h, b.h, x.h, self.maxIter, float(self.absTol), float(self.relTol),
                                      float(self.divTol), C.byref(iters), _ptr(rn))
         return rc, int(iters.value), rn
+
+
+def pcg_solve_batched(A, PC, b: MultiVector, x: MultiVector, inst_dof_off: np.ndarray, maxIter: int,
+                      absoluteTol: float, relativeTol: float, divergenceTol: float, iters_chunk: int = 16):
+    """Batched CGLinearSolver over block-diagonal independent instances.
+    Returns (iterations, status, residual norms) per instance."""
+    off = np.ascontiguousarray(inst_dof_off, dtype=np.uint64)
+    n = off.size - 1
+    iters = np.zeros(n, np.uint32)
+    status = np.zeros(n, np.int32)
+    rn = np.zeros(n)
+    check(A.ctx.lib.gbfe_pcg_solve_batched(A.h, PC.h, b.h, x.h, n, _ptr(off), int(maxIter), float(absoluteTol),
+                                           float(relativeTol), float(divergenceTol), int(iters_chunk), _ptr(iters),
+                                           _ptr(status), _ptr(rn)), A.ctx.h, "pcg_solve_batched")
+    return iters, status, rn

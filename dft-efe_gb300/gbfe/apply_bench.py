@@ -1,0 +1,76 @@
+"""Time one FE operator apply (the Hamiltonian on a block of vectors).
+
+    python -m gbfe.apply_bench --config cfg2c --precision mixed --reps 20
+
+Prints one JSON line: device time per apply (CUDA events on the library's
+stream via the per-kernel statistics), algorithmic GFLOP/s (2 m sum nd_c^2)
+and GB/s (2 N m s_x + sum nd_c^2 s_A) of the cell-product kernel, and the
+whole apply.  The workloads are the seeded synthetic meshes of gbfe.mesh.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import api
+from . import mesh as M
+
+WORKLOADS = {
+    "cfg1": dict(n=8, p=3, L=20.0, atoms=4, Z=4.0, rc=0.5, layout="uniform_inner_half", nq=4, m=24, seed=12346),
+    "cfg2c": dict(n=12, p=4, L=24.0, atoms=8, Z=6.0, rc=0.4, layout="uniform_inner_half", nq=None, m=64,
+                  seed=12347),
+    "cfg3": dict(n=24, p=5, L=40.0, atoms=64, Z=4.0, rc=0.5, layout="jittered_cubic", nq=None, m=512, seed=12348),
+}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", default="cfg2c", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["f64", "mixed", "mixed_v1", "simt"])
+    ap.add_argument("--m", type=int, default=0, help="vectors (0: the workload's)")
+    ap.add_argument("--reps", type=int, default=10)
+    args = ap.parse_args()
+    w = WORKLOADS[args.config]
+    m = args.m or w["m"]
+    prob = M.ks_box(w["n"], w["p"], w["L"], w["atoms"], w["Z"], w["rc"], w["seed"], atom_layout=w["layout"],
+                    nq=w["nq"], matrices=("H",))
+    ctx = api.LinAlgOpContext(0)
+    basis = api.FEBasisManager.from_problem(ctx, prob)
+    mixed = args.precision != "f64"
+    H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=mixed)
+    dt = np.float32 if mixed else np.float64
+    X = api.MultiVector(basis, m, dtype=dt, init=M.random_block(prob.n_dofs, m, 1).astype(dt))
+    Y = api.MultiVector(basis, m, dtype=dt)
+    if args.precision == "simt":
+        ctx.set_tensor_cores(0)
+    elif args.precision == "mixed_v1":
+        ctx.set_tensor_cores(1)
+    for _ in range(3):
+        H.apply(X, Y)
+    ctx.synchronize()
+    ctx.set_profiling(True)
+    ctx.reset_kernel_stats()
+    t0 = time.perf_counter()
+    for _ in range(args.reps):
+        H.apply(X, Y)
+    ctx.synchronize()
+    wall = (time.perf_counter() - t0) / args.reps
+    st = ctx.kernel_stats("cell_apply_f64" if not mixed else "cell_apply_mixed")
+    ctx.check_status()
+    sx = 4 if mixed else 8
+    flops = 2.0 * m * float((prob.nd_per_cell.astype(np.float64) ** 2).sum())
+    bytes_ = 2.0 * prob.n_dofs * m * sx + float((prob.nd_per_cell.astype(np.float64) ** 2).sum()) * (4 if mixed else 8)
+    k_ms = st["ms"] / max(1, st["launches"]) * max(1, st["launches"] // args.reps)
+    print(json.dumps({
+        "config": args.config, "precision": args.precision, "m": m, "n_dofs": prob.n_dofs, "cells": prob.n_cells,
+        "nd": prob.nd, "cell_kernel_ms": k_ms, "apply_wall_ms": wall * 1e3,
+        "cell_kernel_tflops": flops / (k_ms * 1e-3) / 1e12, "cell_kernel_gbs": bytes_ / (k_ms * 1e-3) / 1e9,
+        "algorithmic_gflop": flops / 1e9, "algorithmic_mb": bytes_ / 1e6,
+    }))
+
+
+if __name__ == "__main__":
+    main()

@@ -69,9 +69,11 @@ int gbfe_ctx_synchronize(gbfe_ctx *ctx);
 /* Reads and clears the device status word that the tensor-core kernels set
  * when one of their bounded waits gives up: GBFE_OK or GBFE_ERR_TIMEOUT. */
 int gbfe_ctx_check_status(gbfe_ctx *ctx);
-/* 1 (default): the FP32 apply uses the split-BF16 tcgen05 cell product;
- * 0: the FP32 SIMT cell product (also selected by GBFE_TENSOR_CORES=0). */
-int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int on);
+/* Cell product of the FP32 apply: 2 (default) the persistent warp-specialised
+ * split-BF16 tcgen05 kernel; 1 the one-CTA-per-cell tcgen05 kernel; 0 the FP32
+ * SIMT kernel.  The environment variable GBFE_TENSOR_CORES=0|1 sets the
+ * initial mode of a new context. */
+int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode);
 /* number of kernels this context has launched so far */
 int gbfe_ctx_kernel_launches(const gbfe_ctx *ctx, uint64_t *count);
 /* Per-kernel timing (no counterpart in the reference, whose Profiler times
@@ -119,11 +121,27 @@ int gbfe_constraints_distribute_child_to_parent(const gbfe_cons *cons, gbfe_mv *
  * `prec_flags` is a mask of GBFE_PREC_*. */
 int gbfe_cellmat_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *mats,
                         int prec_flags, gbfe_op **out);
+/* Cell-matrix operator whose cells share stored matrices: `mats` holds n_mats
+ * matrices (column-major, concatenated in index order; matrix u has nd x nd
+ * entries where nd is the size of the cells that name it) and cell_to_mat[c]
+ * names cell c's matrix.  On a uniform mesh (every cell's Laplace or mass
+ * matrix identical) this stores one matrix instead of one per cell; the
+ * apply is the same as gbfe_cellmat_upload with the matrices expanded. */
+int gbfe_cellmat_upload_indexed(gbfe_mesh *mesh, const gbfe_cons *cons, uint32_t n_mats,
+                                const double *mats, const uint32_t *cell_to_mat, int prec_flags,
+                                gbfe_op **out);
 /* Diagonal operator with constraints: CFEOverlapInverseOpContextGLL
  * (CFEOverlapInverseOpContextGLL.t.cpp:528-559) or the lumped
  * CFEOverlapOperatorContext (:546-582).  `diag` holds the diagonal entries
  * (already inverted for an inverse operator). */
 int gbfe_diag_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *diag, gbfe_op **out);
+/* OrthoEFE inverse overlap (basis/OrthoEFEOverlapInverseOpContextGLL.t.cpp:
+ * 1182-1270): Y = diag o X on every dof, then the rows [blk_begin, blk_begin +
+ * blk_n) (the enrichment dofs) are replaced by blk * X[those rows] (blk is the
+ * column-major blk_n x blk_n inverse of the enrichment overlap block), then
+ * child-to-parent constraints. */
+int gbfe_diag_block_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *diag,
+                           uint64_t blk_begin, uint64_t blk_n, const double *blk, gbfe_op **out);
 /* Jacobi preconditioner: Y = diagInv o X, no constraints
  * (linearAlgebra/PreconditionerJacobi.t.cpp:23-80; the reciprocal is taken
  * here from `diagonal` exactly as the reference constructor does). */
@@ -249,6 +267,20 @@ int gbfe_lanczos_bounds(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
 int gbfe_cg_solve(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b, gbfe_mv *x,
                   uint32_t max_iter, double abs_tol, double rel_tol, double div_tol,
                   uint32_t *iters_out, double *rnorm_host);
+
+/* Batched CG over independent instances stored as one block-diagonal system
+ * (instance i owns dofs [inst_dof_off[i], inst_dof_off[i+1]) of b and x, and
+ * A / PC act block-diagonally).  Per instance this is CGLinearSolver::solve
+ * (CGLinearSolver.t.cpp:68-313) with one component; all instances advance in
+ * the same kernels, their scalars stay on the device, and `iters_chunk`
+ * iterations are replayed as one captured CUDA graph between host checks.
+ * Outputs per instance (host arrays of n_inst): iterations, status
+ * (GBFE_OK / GBFE_ERR_NOT_CONVERGED / GBFE_ERR_DIVERGED) and final residual
+ * norm.  Returns GBFE_OK when the call itself succeeded. */
+int gbfe_pcg_solve_batched(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b, gbfe_mv *x,
+                           uint32_t n_inst, const uint64_t *inst_dof_off, uint32_t max_iter,
+                           double abs_tol, double rel_tol, double div_tol, uint32_t iters_chunk,
+                           uint32_t *iters_out, int *status_out, double *rnorm_out);
 
 #ifdef __cplusplus
 }

@@ -62,11 +62,15 @@ typedef struct {
 } orc_cons;
 
 typedef struct {
-  int kind; /* 0: cell matrices, 1: diagonal with constraints, 2: diagonal without */
+  int kind; /* 0: cell matrices, 1: diagonal with constraints, 2: diagonal without,
+               3: diagonal + dense block on [blk_begin, blk_begin + blk_n) with constraints */
   const orc_mesh *mesh;
   const orc_cons *cons;
   const double *mats; /* kind 0: column-major per cell, concatenated */
-  const double *diag; /* kind 1/2: [n_dofs] */
+  const double *diag; /* kind 1/2/3: [n_dofs] */
+  uint64_t blk_begin;
+  uint64_t blk_n;
+  const double *blk; /* kind 3: column-major blk_n x blk_n */
 } orc_op;
 
 static orc_dgemm_fn g_dgemm = 0;
@@ -156,10 +160,23 @@ int orc_apply(const orc_op *op, double *X, double *Y, uint32_t m) {
     if (op->cons) orc_c2p(op->cons, Y, m);
     return 0;
   }
-  if (op->kind == 1 && op->cons) orc_p2c(op->cons, X, m);
+  const int with_cons = (op->kind == 1 || op->kind == 3) && op->cons;
+  if (with_cons) orc_p2c(op->cons, X, m);
   for (uint64_t i = 0; i < N; ++i)
     for (uint32_t v = 0; v < m; ++v) Y[i * m + v] = op->diag[i] * X[i * m + v];
-  if (op->kind == 1 && op->cons) orc_c2p(op->cons, Y, m);
+  if (op->kind == 3) {
+    /* OrthoEFEOverlapInverseOpContextGLL.t.cpp:1182-1270: the enrichment rows
+       of Y are replaced by the dense block times the enrichment rows of X
+       (gemm('N','T') on the column-major [m x nEnr] view) */
+    const uint64_t b0 = op->blk_begin, nb = op->blk_n;
+    for (uint64_t e = 0; e < nb; ++e)
+      for (uint32_t v = 0; v < m; ++v) {
+        double acc = 0.0;
+        for (uint64_t f = 0; f < nb; ++f) acc += op->blk[e + nb * f] * X[(b0 + f) * m + v];
+        Y[(b0 + e) * m + v] = acc;
+      }
+  }
+  if (with_cons) orc_c2p(op->cons, Y, m);
   return 0;
 }
 

@@ -54,7 +54,7 @@ class _Cons(C.Structure):
 
 class _Op(C.Structure):
     _fields_ = [("kind", C.c_int), ("mesh", C.c_void_p), ("cons", C.c_void_p), ("mats", C.c_void_p),
-                ("diag", C.c_void_p)]
+                ("diag", C.c_void_p), ("blk_begin", C.c_uint64), ("blk_n", C.c_uint64), ("blk", C.c_void_p)]
 
 
 _lib = None
@@ -142,6 +142,14 @@ class OracleSystem:
 
     def jacobi_op(self, diagonal):
         return self._op(2, diag=1.0 / np.asarray(diagonal, dtype=np.float64), use_cons=False)
+
+    def diag_block_op(self, diag, blk_begin, blk, use_cons=True):
+        """OrthoEFE inverse overlap: diagonal + dense block on [blk_begin, blk_begin + n)."""
+        op = self._op(3, diag=diag, use_cons=use_cons)
+        b = np.ascontiguousarray(np.asarray(blk, dtype=np.float64).T)  # store column-major
+        self.keep.append(b)
+        op.blk_begin, op.blk_n, op.blk = int(blk_begin), int(b.shape[0]), b.ctypes.data
+        return op
 
     # ---- operations (row-major [N][m] float64 arrays, modified like the reference)
     def apply(self, op, X: np.ndarray) -> np.ndarray:

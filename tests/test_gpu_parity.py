@@ -242,19 +242,20 @@ def test_mixed_apply_fp32_simt(gpu_ctx, small_problem):
     H.apply(X, Y)
     Xf = api.MultiVector(basis, 32, dtype=np.float32, init=X0.astype(np.float32))
     Yf = api.MultiVector(basis, 32, dtype=np.float32)
-    gpu_ctx.set_tensor_cores(False)
+    gpu_ctx.set_tensor_cores(0)
     try:
         H.apply(Xf, Yf)
     finally:
-        gpu_ctx.set_tensor_cores(True)
+        gpu_ctx.set_tensor_cores(2)
     assert rel_maxnorm(Yf.numpy(), Y.numpy()) <= 2e-6
 
 
 TC_TOL = 1e-4  # split-BF16 (3 products, FP32 accumulation): ~2^-18 per operand
 
 
-@pytest.mark.parametrize("n,p,m", [(3, 3, 32), (3, 4, 64), (2, 5, 40), (2, 4, 300), (2, 3, 7)])
-def test_mixed_apply_tensor_cores(gpu_ctx, n, p, m):
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("n,p,m", [(3, 3, 32), (3, 4, 64), (2, 5, 40), (2, 4, 300), (2, 3, 7), (5, 4, 24)])
+def test_mixed_apply_tensor_cores(gpu_ctx, n, p, m, mode):
     """tcgen05 split-BF16 cell product against the FP64 apply of the same X
     (cells of 64, 125 and 216 dofs; one and two 128-row M tiles; ragged and
     multi-tile vector counts)."""
@@ -269,11 +270,36 @@ def test_mixed_apply_tensor_cores(gpu_ctx, n, p, m):
     H.apply(X, Y)
     Xf = api.MultiVector(basis, m, dtype=np.float32, init=X0.astype(np.float32))
     Yf = api.MultiVector(basis, m, dtype=np.float32)
-    H.apply(Xf, Yf)
-    gpu_ctx.check_status()
+    gpu_ctx.set_tensor_cores(mode)
+    try:
+        H.apply(Xf, Yf)
+        gpu_ctx.check_status()
+    finally:
+        gpu_ctx.set_tensor_cores(2)
     err = rel_maxnorm(Yf.numpy(), Y.numpy())
-    print(f"tc apply n={n} p={p} m={m}: rel max-norm err {err:.2e}")
+    print(f"tc{mode} apply n={n} p={p} m={m}: rel max-norm err {err:.2e}")
     assert err <= TC_TOL
+
+
+def test_tensor_core_kernels_agree_bitwise(gpu_ctx):
+    """The persistent kernel and the one-CTA-per-cell kernel issue the same
+    MMAs in the same order per cell, so their results are identical."""
+    from gbfe import api
+
+    prob = M.ks_box(4, 4, 8.0, 1, 4.0, 0.5, seed=44)
+    basis = api.FEBasisManager.from_problem(gpu_ctx, prob)
+    H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=True)
+    X0 = M.random_block(prob.n_dofs, 48, 5).astype(np.float32)
+    outs = []
+    for mode in (1, 2, 2):
+        Xf = api.MultiVector(basis, 48, dtype=np.float32, init=X0)
+        Yf = api.MultiVector(basis, 48, dtype=np.float32)
+        gpu_ctx.set_tensor_cores(mode)
+        H.apply(Xf, Yf)
+        gpu_ctx.check_status()
+        outs.append(Yf.numpy())
+    gpu_ctx.set_tensor_cores(2)
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
 
 
 def test_mixed_apply_tensor_cores_variable_nd(gpu_ctx):
