@@ -24,7 +24,9 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <atomic>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 #include <stdexcept>
@@ -134,6 +136,7 @@ struct gbfe_ctx {
   gbfe::DBuf<int> status;    // device status word written by bounded waits (0 = ok)
   int use_tc = 1;            // split-BF16 tcgen05 cell product for the mixed path
   int tc_version = 2;        // 2: persistent warp-specialised kernel; 1: one CTA per cell
+  std::atomic<int> *cancel = nullptr;  // polled between passes / iterations when set
 };
 
 struct gbfe_mesh {

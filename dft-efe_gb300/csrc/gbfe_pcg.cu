@@ -263,6 +263,12 @@ extern "C" int gbfe_pcg_solve_batched(const gbfe_op *A, const gbfe_op *PC, const
       GBFE_CUDA(cudaMemcpyAsync(&active, d_active_count, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
       GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
       if (active == 0 || done_iters > max_iter) break;
+      if (ctx->cancel && ctx->cancel->load()) {
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        ctx->profiling = was_profiling;
+        throw Error(GBFE_ERR_CANCELLED, "cancelled");
+      }
       GBFE_CUDA(cudaGraphLaunch(exec, ctx->stream));
       ctx->launches += per_replay;
       done_iters += chunk;

@@ -623,6 +623,11 @@ int ks_solve_fused(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe
   int status = GBFE_ERR_NOT_CONVERGED;
   uint32_t pass = 0;
   for (; pass < prm->max_passes; ++pass) {
+    if (ctx->cancel && ctx->cancel->load()) {
+      status = GBFE_ERR_CANCELLED;
+      msg = "cancelled";
+      break;
+    }
     const int r = fused_pass(A, B, BInv, X, eig_h, prm->degree, wl, wu, uu, prm->filter_precision, st, res_h, msg);
     if (r != GBFE_OK) {
       status = r;
@@ -858,6 +863,10 @@ int gbfe_cg_solve(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b, gbfe_mv
     status = 99;
     uint32_t iter = 0;
     for (; iter <= max_iter; ++iter) {
+      if (ctx->cancel && ctx->cancel->load()) {
+        status = GBFE_ERR_CANCELLED;
+        break;
+      }
       if (iter == 0) {
         apply_op(A, xw.get(), w.get());
         d_axpby_blocked(ctx, 1.0, d_ones.b.p, b, 1.0, d_nones.b.p, w.get(), r.get());
@@ -898,7 +907,7 @@ int gbfe_cg_solve(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b, gbfe_mv
       all = std::all_of(conv.begin(), conv.end(), [](char c) { return c != 0; });
       if (diverge || all) break;
     }
-    if (iter > max_iter) status = GBFE_ERR_NOT_CONVERGED;
+    if (iter > max_iter && status != GBFE_ERR_CANCELLED) status = GBFE_ERR_NOT_CONVERGED;
     if (status == 99) status = GBFE_ERR_NOT_CONVERGED;
     GBFE_CUDA(cudaMemcpyAsync(x->d.p, xc->d.p, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -906,6 +915,7 @@ int gbfe_cg_solve(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b, gbfe_mv
     if (rnorm_host) std::copy(rn.begin(), rn.end(), rnorm_host);
     if (status == GBFE_ERR_NOT_CONVERGED) ctx->last_error = "FAILED_TO_CONVERGE";
     if (status == GBFE_ERR_DIVERGED) ctx->last_error = "RESIDUAL_DIVERGENCE";
+    if (status == GBFE_ERR_CANCELLED) ctx->last_error = "cancelled";
   });
   return rc != GBFE_OK ? rc : status;
 }

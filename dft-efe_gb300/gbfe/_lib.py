@@ -32,6 +32,17 @@ class KSParams(C.Structure):
     ]
 
 
+class MeshDesc(C.Structure):
+    _fields_ = [("n_cells", u32), ("nd_per_cell", p), ("cell_dof_ids", p), ("n_dofs", u64), ("n_cons_rows", u32),
+                ("row_ids", p), ("row_sizes", p), ("col_ids", p), ("row_acc", p), ("col_values", p),
+                ("inhomogeneities", p)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", i32), ("t_submit", f64), ("t_admit", f64), ("t_done", f64), ("passes_or_iters", u32),
+                ("footprint_bytes", u64), ("message", C.c_char * 256)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "gbfe_ctx_create": (i32, [i32, C.POINTER(p)]),
@@ -80,6 +91,18 @@ SIGNATURES = {
     "gbfe_lanczos_bounds": (i32, [p, p, p, u32, u64, p]),
     "gbfe_cg_solve": (i32, [p, p, p, p, u32, f64, f64, f64, C.POINTER(u32), p]),
     "gbfe_pcg_solve_batched": (i32, [p, p, p, p, u32, p, u32, f64, f64, f64, u32, p, p, p]),
+    "gbfe_server_create": (i32, [i32, u32, u64, C.POINTER(p)]),
+    "gbfe_server_destroy": (i32, [p]),
+    "gbfe_server_submit_ks": (i32, [p, C.POINTER(MeshDesc), p, p, p, u64, u64, p, p, u32, C.POINTER(KSParams),
+                                    C.POINTER(u64)]),
+    "gbfe_server_submit_poisson": (i32, [p, C.POINTER(MeshDesc), u32, p, p, p, p, u32, f64, f64, f64,
+                                         C.POINTER(u64)]),
+    "gbfe_server_cancel": (i32, [p, u64]),
+    "gbfe_server_wait": (i32, [p, u64, f64, C.POINTER(RequestInfo)]),
+    "gbfe_server_result": (i32, [p, u64, p, p]),
+    "gbfe_server_release": (i32, [p, u64]),
+    "gbfe_server_stats": (i32, [p, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u32)]),
+    "gbfe_server_inject_alloc_failures": (i32, [p, i32]),
 }
 
 _lib = None

@@ -282,6 +282,65 @@ int gbfe_pcg_solve_batched(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b
                            double abs_tol, double rel_tol, double div_tol, uint32_t iters_chunk,
                            uint32_t *iters_out, int *status_out, double *rnorm_out);
 
+/* ---- serving ---------------------------------------------------------------
+ * A continuous-batching request loop (no counterpart in the reference, which
+ * solves one problem per process).  The server owns `slots` contexts, each with
+ * its own CUDA stream and worker thread.  Requests (KS eigen solves or Poisson
+ * solves, each on its own mesh) are admitted in arrival order as soon as a slot
+ * is free and their estimated HBM footprint fits `hbm_budget_bytes` beside the
+ * resident requests; a request that can never fit finishes with
+ * GBFE_ERR_ALLOC.  An admitted request keeps its mesh, matrices and vectors
+ * resident until it finishes; the kernels of concurrently admitted requests
+ * overlap on the device.  A request's result does not depend on the mix. */
+typedef struct gbfe_server gbfe_server;
+
+typedef struct {
+  uint32_t n_cells;
+  const uint32_t *nd_per_cell;
+  const uint32_t *cell_dof_ids;
+  uint64_t n_dofs;
+  uint32_t n_cons_rows;
+  const uint32_t *row_ids, *row_sizes, *col_ids, *row_acc;
+  const double *col_values, *inhomogeneities;
+} gbfe_mesh_desc;
+
+typedef struct {
+  int status;              /* the solve's status (GBFE_OK, ..._NOT_CONVERGED, ..._ALLOC, ..._CANCELLED) */
+  double t_submit, t_admit, t_done;  /* seconds, steady clock */
+  uint32_t passes_or_iters;
+  uint64_t footprint_bytes;
+  char message[256];
+} gbfe_request_info;
+
+int gbfe_server_create(int device, uint32_t slots, uint64_t hbm_budget_bytes, gbfe_server **out);
+int gbfe_server_destroy(gbfe_server *server);
+/* KS request: H, M cell matrices (gbfe_cellmat_upload layout), the inverse
+ * GLL diagonal (and, for enriched meshes, the dense enrichment block of
+ * gbfe_diag_block_upload; blk_n = 0 otherwise), the initial block X0 and the
+ * solve parameters.  All arrays are copied; the caller may free them. */
+int gbfe_server_submit_ks(gbfe_server *server, const gbfe_mesh_desc *mesh, const double *H, const double *M,
+                          const double *minv_diag, uint64_t blk_begin, uint64_t blk_n, const double *blk,
+                          const double *X0, uint32_t m, const gbfe_ks_params *params, uint64_t *id_out);
+/* Poisson request: indexed Laplace matrices (gbfe_cellmat_upload_indexed),
+ * the Jacobi diagonal, the right-hand side and the CG tolerances. */
+int gbfe_server_submit_poisson(gbfe_server *server, const gbfe_mesh_desc *mesh, uint32_t n_mats,
+                               const double *mats, const uint32_t *cell_to_mat, const double *jacobi_diag,
+                               const double *b, uint32_t max_iter, double abs_tol, double rel_tol,
+                               double div_tol, uint64_t *id_out);
+/* Queued requests are dropped; running ones stop at their next pass/iteration
+ * boundary with GBFE_ERR_CANCELLED. */
+int gbfe_server_cancel(gbfe_server *server, uint64_t id);
+/* Blocks until request `id` finishes or `timeout_s` passes (GBFE_ERR_TIMEOUT). */
+int gbfe_server_wait(gbfe_server *server, uint64_t id, double timeout_s, gbfe_request_info *info);
+/* KS: eigenvalues and residual norms (m each); Poisson: the solution (n_dofs). */
+int gbfe_server_result(gbfe_server *server, uint64_t id, double *values, double *residuals);
+int gbfe_server_release(gbfe_server *server, uint64_t id);
+int gbfe_server_stats(gbfe_server *server, uint64_t *admitted, uint64_t *completed, uint64_t *rejected,
+                      uint64_t *used_bytes, uint32_t *queued);
+/* Fault injection for tests (host side): the next `count` admitted requests
+ * fail their device upload with GBFE_ERR_ALLOC. */
+int gbfe_server_inject_alloc_failures(gbfe_server *server, int count);
+
 #ifdef __cplusplus
 }
 #endif
