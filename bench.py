@@ -277,6 +277,224 @@ def run_gpu(args, cfg_name, rank, world):
                 h2d=prob.n_dofs * m * 8, d2h=prob.n_dofs * m * 8 + 2 * m * 8)
 
 
+# ----------------------------------------------------------------------------- batched Poisson (configs[3])
+def _cpu_poisson_worker(args):
+    """Oracle CGLinearSolver restatement on one Poisson instance (FP64, one thread)."""
+    i, seed = args
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    sys.path.insert(0, str(ROOT / "dft-efe_gb300"))
+    sys.path.insert(0, str(ROOT))
+    import gbfe.poisson as P
+    from oracle import oracle as O
+
+    pb = P.batch(64, seed=seed)
+    v = P.instance_view(pb, i)
+    s = O.OracleSystem(v["nd"], v["ids"], v["N"], v["cons"])
+    t0 = time.perf_counter()
+    rc, x, it, rn = s.cg(s.cell_op(v["K"]), s.jacobi_op(v["diag"]), v["b"][:, None], np.zeros((v["N"], 1)), 20000,
+                         1e-14, 1e-10, 1e10)
+    return time.perf_counter() - t0, v["N"], it
+
+
+def run_poisson(args):
+    import torch
+
+    import gbfe.poisson as P
+    from gbfe import api
+
+    seed = 12349
+    pb = P.batch(64, seed=seed)
+    ctx = api.LinAlgOpContext(0)
+    basis = api.FEBasisManager(ctx, pb.nd_per_cell, pb.cell_dof_ids, pb.n_dofs, pb.constraints)
+    K = api.IndexedCellMatrixOperatorContext(basis, pb.mats, pb.cell_to_mat)
+    J = api.PreconditionerJacobi(basis, pb.jacobi_diag)
+    b = api.MultiVector(basis, 1, init=pb.b[:, None])
+    x = api.MultiVector(basis, 1)
+
+    def solve():
+        x.setValue(0.0)
+        return api.pcg_solve_batched(K, J, b, x, pb.inst_dof_off, 20000, 1e-14, 1e-10, 1e10, iters_chunk=16)
+
+    for _ in range(args.warmup):
+        iters, status, rn = solve()
+    ctx.synchronize()
+    l0 = ctx.kernel_launches()
+    lat = []
+    clocks = ClockSampler(ROOT / "gpurun_out" / "bench_clocks_poisson.csv" if (ROOT / "gpurun_out").is_dir() else None)
+    with clocks:
+        time.sleep(0.3)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ts = time.perf_counter()
+            iters, status, rn = solve()
+            lat.append(time.perf_counter() - ts)
+        ctx.synchronize()
+        t_total = time.perf_counter() - t0
+    launches = ctx.kernel_launches() - l0
+    # roofline of the FP64 cell product: the same operator on the same vector, event-timed
+    ctx.set_profiling(True)
+    ctx.reset_kernel_stats()
+    w = api.MultiVector(basis, 1)
+    for _ in range(10):
+        K.apply(x, w)
+    st = ctx.kernel_stats("cell_apply_f64")
+    ctx.set_profiling(False)
+    peak = ctx.probe_fp64_peak() / 1e3
+    avg_ms = st["ms"] / max(1, st["launches"])
+    achieved = st["flops"] / max(1, st["launches"]) / (avg_ms * 1e-3) / 1e12
+    # e2e through the C ABI with host buffers: b in, x out
+    pinned_b = torch.empty((pb.n_dofs, 1), dtype=torch.float64, pin_memory=True)
+    pinned_b.numpy()[:] = pb.b[:, None]
+    pinned_x = torch.empty((pb.n_dofs, 1), dtype=torch.float64, pin_memory=True)
+    e2e = []
+    for _ in range(args.steps):
+        ctx.synchronize()
+        ts = time.perf_counter()
+        ctx.lib.gbfe_mv_copy_in(b.h, api.C.c_void_p(pinned_b.data_ptr()))
+        solve()
+        ctx.lib.gbfe_mv_copy_out(x.h, api.C.c_void_p(pinned_x.data_ptr()))
+        e2e.append(time.perf_counter() - ts)
+    value = 64 * args.steps / t_total
+    line = {
+        "metric": "batched Poisson CG solves/s (64 independent instances, Jacobi-PCG to relative residual 1e-10, FP64)",
+        "value": value, "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded generator)",
+        "config": {"workload": "cfg4", "instances": 64, "n_dofs_total": pb.n_dofs, "cells_total": int(pb.nd_per_cell.size),
+                   "iterations_min_max": [int(iters.min()), int(iters.max())], "all_converged": bool((status == 0).all()),
+                   "graph_chunk": 16, "l2": "working set larger than L2"},
+        "latency_ms": {"p50": pct(lat, 50) * 1e3, "p99": pct(lat, 99) * 1e3},
+        "roofline": {"kernel": "cell_apply_f64 (m=1)", "bound": "fp64", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "DFMA throughput probe run in this process",
+                     "measured": "10 event-timed applies of the same operator after the timed region"},
+        "clocks": clocks.summary(),
+        "e2e": {"value": 64 / float(np.mean(e2e)), "unit": "solves/s", "h2d_bytes_per_step": pb.n_dofs * 8,
+                "d2h_bytes_per_step": pb.n_dofs * 8},
+        "gpu_launches": launches,
+    }
+    if not args.no_cpu_baseline:
+        import multiprocessing as mp
+
+        procs = args.cpu_procs or os.cpu_count() or 1
+        sample = list(range(min(procs, 64)))
+        with mp.get_context("spawn").Pool(procs) as pool:
+            res = pool.map(_cpu_poisson_worker, [(i, seed) for i in sample])
+        cpu_work = sum(t for t, _, _ in res)
+        work_sample = sum(n * it for _, n, it in res)
+        sizes = np.diff(pb.inst_dof_off.astype(np.int64))
+        work_all = float((sizes * iters.astype(np.int64)).sum())
+        t_all = cpu_work * work_all / work_sample
+        line["cpu_baseline"] = {"value": 64 / (t_all / procs), "unit": "solves/s", "cores": procs, "kind": "port",
+                                "sample": f"oracle CG on instances 0..{len(sample) - 1}, one per single-threaded "
+                                          f"process ({cpu_work:.1f} s of CPU), extrapolated to all 64 by dofs x "
+                                          f"iterations"}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------- serving stream (configs[4])
+def run_serving(args):
+    import gbfe.enrichment as E
+    import gbfe.mesh as M
+    import gbfe.poisson as P
+    from gbfe import api
+    from gbfe.serve import Server, poisson_request_from_batch
+
+    rng = np.random.default_rng(12350)
+    n_req = args.requests
+    # a pool of distinct problems; requests draw from it (each request is its own solve)
+    ks_pool = []
+    for k in range(6):
+        n = int(rng.integers(6, 11))
+        p = int(rng.choice([3, 4]))
+        atoms = int(rng.integers(2, 17))
+        Z = float(rng.choice([1.0, 4.0, 6.0]))
+        enr = bool(rng.random() < 0.3)
+        L = 2.0 * n
+        if enr:
+            prob = E.enriched_problem(n, p, L, atoms, Z, 0.5, seed=100 + k)
+        else:
+            prob = M.ks_box(n, p, L, atoms, Z, 0.5, seed=100 + k)
+        m = int(rng.choice([16, 24, 32]))
+        deg = int(rng.integers(15, 31))
+        ks_pool.append((prob, m, max(4, m // 2), deg))
+    pb = P.batch(24, seed=12351, n_range=(6, 14))
+    # FP64 reference eigenvalues of each pool problem (one FP64 solve alone)
+    srv = Server(slots=1, hbm_budget_bytes=200 << 30)
+    ref = []
+    iso = {"ks": [], "poisson": []}
+    for prob, m, nw, deg in ks_pool:
+        X0 = M.random_block(prob.n_dofs, m, 7)
+        rid = srv.submit_ks(prob, X0, nw, deg, 60, 1e-6, mixed=False)
+        srv.wait(rid)
+        ref.append(srv.ks_result(rid, m)[0])
+        rid = srv.submit_ks(prob, X0, nw, deg, 60, 1e-6, mixed=True)
+        iso["ks"].append(srv.wait(rid).latency)
+    for i in range(4):
+        rid = srv.submit_poisson(poisson_request_from_batch(pb, i))
+        iso["poisson"].append(srv.wait(rid).latency)
+    srv.close()
+    kinds = rng.random(n_req) < 0.25  # KS : Poisson = 1 : 3
+    gaps = rng.exponential(1.0 / args.rate, size=n_req)
+    srv = Server(slots=args.slots, hbm_budget_bytes=int(args.hbm_budget_gb * (1 << 30)))
+    reqs = []
+    t0 = time.perf_counter()
+    next_t = t0
+    for j in range(n_req):
+        next_t += gaps[j]
+        while time.perf_counter() < next_t:
+            time.sleep(min(0.002, max(0.0, next_t - time.perf_counter())))
+        if kinds[j]:
+            k = int(rng.integers(len(ks_pool)))
+            prob, m, nw, deg = ks_pool[k]
+            rid = srv.submit_ks(prob, M.random_block(prob.n_dofs, m, 7), nw, deg, 60, 1e-6, mixed=True)
+            reqs.append(("ks", rid, k))
+        else:
+            i = int(rng.integers(pb.n_inst))
+            rid = srv.submit_poisson(poisson_request_from_batch(pb, i))
+            reqs.append(("poisson", rid, i))
+    lat = {"ks": [], "poisson": []}
+    errs, ok = [], 0
+    for kind, rid, k in reqs:
+        info = srv.wait(rid, 3600.0)
+        lat[kind].append(info.latency)
+        if kind == "ks":
+            prob, m, nw, deg = ks_pool[k]
+            eig = srv.ks_result(rid, m)[0]
+            err = float(np.abs(eig[:nw] - ref[k][:nw]).max())
+            errs.append(err)
+            ok += int(info.status == 0 and err <= EIG_TOL)
+        else:
+            ok += int(info.status == 0)
+        srv.release(rid)
+    makespan = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    all_lat = lat["ks"] + lat["poisson"]
+    line = {
+        "metric": "serving: solves/s of a Poisson-arrival stream of KS (mixed, |d_eps|<=1e-6 Ha) and Poisson "
+                  "requests; p50/p99 latency",
+        "value": ok / makespan, "unit": "solves/s", "n_gpus": 1, "steps": n_req, "warmup": 0,
+        "ms_per_step": makespan / n_req * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+bf16x3 filter / f64 (KS); f64 (Poisson)", "data": "synthetic (seeded generator)",
+        "config": {"workload": "cfg5", "requests": n_req, "arrival_rate_per_s": args.rate, "slots": args.slots,
+                   "hbm_budget_gb": args.hbm_budget_gb, "ks_pool": len(ks_pool), "poisson_pool": pb.n_inst,
+                   "ks_fraction": 0.25},
+        "latency_ms": {"p50": pct(all_lat, 50) * 1e3, "p99": pct(all_lat, 99) * 1e3,
+                       "ks_p50": pct(lat["ks"], 50) * 1e3 if lat["ks"] else None,
+                       "ks_p99": pct(lat["ks"], 99) * 1e3 if lat["ks"] else None,
+                       "poisson_p50": pct(lat["poisson"], 50) * 1e3, "poisson_p99": pct(lat["poisson"], 99) * 1e3},
+        "isolated_ms": {"ks_median": float(np.median(iso["ks"])) * 1e3,
+                        "poisson_median": float(np.median(iso["poisson"])) * 1e3},
+        "accuracy": {"max_abs_eig_err_Ha": max(errs) if errs else None, "valid": ok, "of": n_req},
+        "server": st,
+        "e2e": {"value": ok / makespan, "unit": "solves/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                "note": "every request uploads its mesh, matrices and vectors and downloads its result"},
+    }
+    print(json.dumps(line))
+
+
 def pct(v, q):
     return float(np.percentile(np.asarray(v), q))
 
@@ -287,7 +505,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbfe", choices=["gbfe", "reference"])
-    ap.add_argument("--config", default="cfg2c", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="cfg2c", choices=sorted(CONFIGS) + ["cfg4", "cfg5"])
+    ap.add_argument("--requests", type=int, default=96, help="cfg5: requests in the stream")
+    ap.add_argument("--rate", type=float, default=20.0, help="cfg5: mean arrivals per second")
+    ap.add_argument("--slots", type=int, default=4, help="cfg5: concurrent requests")
+    ap.add_argument("--hbm-budget-gb", type=float, default=64.0, help="cfg5: HBM admission budget")
     ap.add_argument("--fp64-repeats", type=int, default=2)
     ap.add_argument("--cpu-procs", type=int, default=0, help="oracle processes for the CPU baseline (0: all cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -296,7 +518,11 @@ def main():
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    cfg = CONFIGS[args.config]
+    if args.config in ("cfg4", "cfg5") and args.impl == "gbfe":
+        if rank == 0:
+            (run_poisson if args.config == "cfg4" else run_serving)(args)
+        return
+    cfg = CONFIGS.get(args.config, CONFIGS["cfg2c"])
     procs = args.cpu_procs or os.cpu_count() or 1
     metric = "ChFSI solves/s at |d_eps|<=1e-6 Ha (mixed precision), FP64 beside it"
 

@@ -59,9 +59,9 @@ def test_admission_respects_budget_and_rejects_oversize(gpu_ctx, workload):
     from gbfe.serve import Server
 
     ks, pb = workload
-    srv = Server(slots=4, hbm_budget_bytes=1 << 30)
+    srv = Server(slots=4, hbm_budget_bytes=256 << 20)
     big = M.ks_box(3, 3, 6.0, 1, 4.0, 0.5, seed=1)
-    # footprint of a 4096-vector block exceeds a 1 GiB budget: rejected, never admitted
+    # the estimated footprint of a 4096-vector block (~410 MB) exceeds a 256 MiB budget: rejected, never admitted
     rid_big = srv.submit_ks(big, M.random_block(big.n_dofs, 4096, 1), 4, 6, 2)
     info = srv.wait(rid_big)
     assert info.status == 3  # GBFE_ERR_ALLOC
