@@ -7,13 +7,17 @@ reach the tolerance) of a fixed workload from the same seeded random block.
 A mixed solve counts only if its wanted eigenvalues agree with the FP64 solve
 of the same inputs within 1e-6 Ha.
 
-Workloads (synthetic, seeded; see gbfe/mesh.py):
-  cfg2c  12^3 hex cells of degree 4 on a 24 bohr cube, 8 atoms (Z=6, rc=0.4),
-         64 vectors -- the classical part of the enriched configuration
-         (enrichment functions are not generated yet); default
+Workloads (synthetic, seeded; see gbfe/mesh.py, gbfe/enrichment.py):
+  cfg2   12^3 hex cells of degree 4 on a 24 bohr cube, 8 atoms (Z=6, rc=0.4),
+         five orthogonalised enrichment functions per atom (cells of 125-145
+         dofs), 64 vectors; default
+  cfg2c  the same without enrichment (all cells of 125 dofs)
   cfg1   8^3 cells of degree 3, 20 bohr, 4 atoms (Z=4, rc=0.5), 24 vectors,
          degree 20
   cfg3   24^3 cells of degree 5, 40 bohr, 64 atoms, 512 vectors, degree 30
+  cfg4   64 independent Poisson solves batched in one Jacobi-PCG (FP64)
+  cfg5   a Poisson-arrival stream of KS and Poisson requests through the
+         serving loop (p50 / p99 latency)
 
 --impl reference times the reference's CPU implementation of the same solve
 (the oracle port in oracle/, per-cell dgemm through OpenBLAS as the reference
@@ -44,6 +48,8 @@ CHEBY_ORDER_LOOKUP = [(10, 6), (50, 9), (100, 12), (200, 16), (300, 19), (500, 2
                       (500000, 1000)]
 
 CONFIGS = {
+    "cfg2": dict(n=12, p=4, L=24.0, atoms=8, Z=6.0, rc=0.4, layout="uniform_inner_half", nq=None, m=64,
+                 n_wanted=48, degree=None, max_passes=40, tol=1e-6, seed=12347, enriched=True),
     "cfg1": dict(n=8, p=3, L=20.0, atoms=4, Z=4.0, rc=0.5, layout="uniform_inner_half", nq=4, m=24, n_wanted=16,
                  degree=20, max_passes=30, tol=1e-6, seed=12346),
     "cfg2c": dict(n=12, p=4, L=24.0, atoms=8, Z=6.0, rc=0.4, layout="uniform_inner_half", nq=None, m=64,
@@ -65,6 +71,10 @@ def cheby_degree(unwanted_upper: float) -> int:
 def make_problem(cfg):
     import gbfe.mesh as M
 
+    if cfg.get("enriched"):
+        import gbfe.enrichment as E
+
+        return E.enriched_problem(cfg["n"], cfg["p"], cfg["L"], cfg["atoms"], cfg["Z"], cfg["rc"], cfg["seed"])
     return M.ks_box(cfg["n"], cfg["p"], cfg["L"], cfg["atoms"], cfg["Z"], cfg["rc"], cfg["seed"],
                     atom_layout=cfg["layout"], nq=cfg["nq"])
 
@@ -150,7 +160,11 @@ def _cpu_worker(args):
         cfg["m"] = m_override
     prob = make_problem(cfg)
     s = O.OracleSystem.from_problem(prob)
-    H, Mo, Mi = s.cell_op(prob.H), s.cell_op(prob.M), s.diag_op(1.0 / prob.m_gll_diag)
+    H, Mo = s.cell_op(prob.H), s.cell_op(prob.M)
+    if "enr_block_inv" in prob.extra:
+        Mi = s.diag_block_op(1.0 / prob.m_gll_diag, prob.extra["enr_begin"], prob.extra["enr_block_inv"])
+    else:
+        Mi = s.diag_op(1.0 / prob.m_gll_diag)
     (wl, wu, uu), deg = lanczos_setup(prob, cfg, lambda: s.lanczos_bounds(H, Mo, Mi, 20, 7))
     X = M.random_block(prob.n_dofs, cfg["m"], cfg["seed"] + 1)
     eig = np.zeros(cfg["m"])
@@ -188,9 +202,13 @@ def run_gpu(args, cfg_name, rank, world):
     prob = make_problem(cfg)
     ctx = api.LinAlgOpContext(0)
     basis = api.FEBasisManager.from_problem(ctx, prob)
-    H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=True)
-    Mo = api.CFEOverlapOperatorContext(basis, prob.M, mixed=True)
-    Mi = api.CFEOverlapInverseOpContextGLL(basis, prob.m_gll_diag)
+    H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=True, fp64_tensor=True)
+    Mo = api.CFEOverlapOperatorContext(basis, prob.M, mixed=True, fp64_tensor=True)
+    if "enr_block_inv" in prob.extra:
+        Mi = api.OrthoEFEOverlapInverseOpContextGLL(basis, prob.m_gll_diag, prob.extra["enr_begin"],
+                                                    prob.extra["enr_block_inv"])
+    else:
+        Mi = api.CFEOverlapInverseOpContextGLL(basis, prob.m_gll_diag)
     m, nw = cfg["m"], cfg["n_wanted"]
     (wl, wu, uu), deg = lanczos_setup(prob, cfg, lambda: api.lanczos_bounds(H, Mo, Mi, 20, 7))
     X0 = M.random_block(prob.n_dofs, m, cfg["seed"] + 1)
@@ -198,7 +216,10 @@ def run_gpu(args, cfg_name, rank, world):
     X = api.MultiVector(basis, m)
 
     def solver(mixed):
-        return api.KohnShamEigenSolver(nw, deg, cfg["max_passes"], cfg["tol"], mixed=mixed, bounds=(wl, wu, uu))
+        # the mixed solve runs its FP64 stages on the sliced tensor-core FP64
+        # product; the FP64 arm is the plain FP64 FMA path
+        return api.KohnShamEigenSolver(nw, deg, cfg["max_passes"], cfg["tol"], mixed=mixed, bounds=(wl, wu, uu),
+                                       fp64_tensor=mixed)
 
     def solve(mixed):
         X0dev.copy_to(X)
@@ -254,6 +275,7 @@ def run_gpu(args, cfg_name, rank, world):
     launches = ctx.kernel_launches() - launches0
     st_mixed = ctx.kernel_stats("cell_apply_mixed")
     st_f64 = ctx.kernel_stats("cell_apply_f64")
+    st_oz = ctx.kernel_stats("cell_apply_f64_oz")
     ctx.set_profiling(False)
 
     # e2e: the same solve through the C ABI with host buffers each step
@@ -273,7 +295,7 @@ def run_gpu(args, cfg_name, rank, world):
     fp64_peak = ctx.probe_fp64_peak()
     return dict(cfg=cfg, prob=prob, deg=deg, bounds=(wl, wu, uu), fp64_times=fp64_times, passes64=passes64,
                 rc64=rc64, lat=lat, errs=errs, passes=passes, ok=ok, t_total=t_total, launches=launches,
-                st_mixed=st_mixed, st_f64=st_f64, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
+                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
                 h2d=prob.n_dofs * m * 8, d2h=prob.n_dofs * m * 8 + 2 * m * 8)
 
 
@@ -505,7 +527,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbfe", choices=["gbfe", "reference"])
-    ap.add_argument("--config", default="cfg2c", choices=sorted(CONFIGS) + ["cfg4", "cfg5"])
+    ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS) + ["cfg4", "cfg5"])
     ap.add_argument("--requests", type=int, default=96, help="cfg5: requests in the stream")
     ap.add_argument("--rate", type=float, default=20.0, help="cfg5: mean arrivals per second")
     ap.add_argument("--slots", type=int, default=4, help="cfg5: concurrent requests")
@@ -532,7 +554,7 @@ def main():
         # passes per solve: the pass count the FP64 solve of the same inputs
         # needs (measured on the GPU path, which matches the oracle pass for
         # pass), so that the CPU arm is timed on a bounded sample of passes.
-        passes = {"cfg1": 20, "cfg2c": 24, "cfg3": 24}[args.config]
+        passes = {"cfg1": 20, "cfg2": 24, "cfg2c": 24, "cfg3": 24}[args.config]
         vals = []
         for _ in range(args.warmup):
             pass
@@ -565,8 +587,9 @@ def main():
         t_step = float(t.item()) / args.steps
     value = world / t_step  # replicas: every rank solves its own copy
     fp64_sps = 1.0 / float(np.median(r["fp64_times"]))
-    st = r["st_f64"] if r["st_f64"]["ms"] >= r["st_mixed"]["ms"] else r["st_mixed"]
-    dom = "cell_apply_f64" if st is r["st_f64"] else "cell_apply_mixed"
+    cand = {"cell_apply_f64": r["st_f64"], "cell_apply_mixed": r["st_mixed"], "cell_apply_f64_oz": r["st_oz"]}
+    dom = max(cand, key=lambda k: cand[k]["ms"])
+    st = cand[dom]
     avg_ms = st["ms"] / max(1, st["launches"])
     flops_per_launch = st["flops"] / max(1, st["launches"])
     achieved = flops_per_launch / (avg_ms * 1e-3) / 1e12
@@ -577,11 +600,14 @@ def main():
                 "launches": st["launches"], "avg_launch_ms": avg_ms, "flops_per_launch": flops_per_launch}
     else:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() \
-            else {"bf16_tflops": 1900.0}
-        roof = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
-                "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
-                "launches": st["launches"], "avg_launch_ms": avg_ms, "flops_per_launch": flops_per_launch}
-    other = r["st_mixed"] if dom == "cell_apply_f64" else r["st_f64"]
+            else {"hbm_gbs": 6800.0}
+        gbs = st["bytes"] / max(1, st["launches"]) / (avg_ms * 1e-3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": gbs / peaks["hbm_gbs"], "traffic": None, "launches": st["launches"],
+                "avg_launch_ms": avg_ms, "algorithmic_tflops": achieved,
+                "bytes_per_launch": st["bytes"] / max(1, st["launches"]),
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"}
+    others = {k: v for k, v in cand.items() if k != dom}
     e2e_sps = world / float(np.mean(r["e2e_lat"]))
     line = {
         "metric": "ChFSI solves/s at |d_eps|<=1e-6 Ha (mixed precision), FP64 beside it",
@@ -598,7 +624,7 @@ def main():
         "accuracy": {"max_abs_eig_err_Ha": max(r["errs"]), "valid_solves": r["ok"], "of": args.steps,
                      "passes": r["passes"]},
         "roofline": roof,
-        "other_kernel": {"name": "cell_apply_mixed" if dom == "cell_apply_f64" else "cell_apply_f64", **other},
+        "other_kernels": others,
         "clocks": r["clocks"],
         "e2e": {"value": e2e_sps, "unit": "solves/s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
         "gpu_launches": r["launches"],

@@ -336,7 +336,10 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
     return;
   }
   op->cellbuf.ensure((size_t)me->total_cell_dofs * m);
-  cell_apply_f64(op, X, op->cellbuf.p);
+  if (ctx->fp64_tc && op->oz_aoff.p)
+    cell_apply_oz(op, X, op->cellbuf.p);
+  else
+    cell_apply_f64(op, X, op->cellbuf.p);
   const uint8_t *isr = c ? c->is_row.p : nullptr;
   k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
       op->cellbuf.p, m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr, has_par ? c->par_ptr.p : nullptr,
@@ -485,6 +488,12 @@ int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode) {
   if (!ctx || mode < 0 || mode > 2) return GBFE_ERR_ARG;
   ctx->use_tc = mode ? 1 : 0;
   if (mode) ctx->tc_version = mode;
+  return GBFE_OK;
+}
+
+int gbfe_ctx_set_fp64_apply(gbfe_ctx *ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 1) return GBFE_ERR_ARG;
+  ctx->fp64_tc = mode;
   return GBFE_OK;
 }
 
@@ -759,6 +768,7 @@ int gbfe_cellmat_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double *ma
     op->mats_count = mesh->total_mat;
     op->mats.upload(mats, mesh->total_mat, mesh->ctx->stream);
     if (prec_flags & GBFE_PREC_MIXED) build_mixed_mats(op);
+    if ((prec_flags & GBFE_PREC_FP64_TENSOR) && oz_supported(mesh)) build_oz_mats(op);
     GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
   });
   if (rc != GBFE_OK) {
@@ -799,6 +809,7 @@ int gbfe_cellmat_upload_indexed(gbfe_mesh *mesh, const gbfe_cons *cons, uint32_t
     op->mats.upload(mats, uoff[n_mats], mesh->ctx->stream);
     op->mat_off_own.upload(coff.data(), coff.size(), mesh->ctx->stream);
     if (prec_flags & GBFE_PREC_MIXED) build_mixed_mats(op);
+    if ((prec_flags & GBFE_PREC_FP64_TENSOR) && oz_supported(mesh)) build_oz_mats(op);
     GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
   });
   if (rc != GBFE_OK) {

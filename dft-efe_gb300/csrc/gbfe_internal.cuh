@@ -137,6 +137,7 @@ struct gbfe_ctx {
   int use_tc = 1;            // split-BF16 tcgen05 cell product for the mixed path
   int tc_version = 2;        // 2: persistent warp-specialised kernel; 1: one CTA per cell
   std::atomic<int> *cancel = nullptr;  // polled between passes / iterations when set
+  int fp64_tc = 0;           // 1: FP64 applies use the sliced tensor-core product when built
 };
 
 struct gbfe_mesh {
@@ -182,6 +183,10 @@ struct gbfe_op {
   gbfe::DBuf<uint64_t> mat_off_own;   // per-cell offsets of an indexed operator
   gbfe::DBuf<__nv_bfloat16> mats_hi;  // split-BF16 hi/lo tiles (per cell, per K chunk)
   gbfe::DBuf<uint64_t> tc_aoff;       // element offset of each cell's tiles
+  gbfe::DBuf<__nv_bfloat16> oz_mats;  // 8 integer slices per entry (FP64-accurate tensor product)
+  gbfe::DBuf<uint64_t> oz_aoff;
+  gbfe::DBuf<int> oz_row_exp;         // per cell row exponent of the slices
+  mutable gbfe::DBuf<int> oz_xexp;    // per-vector exponent of the current X
   gbfe::DBuf<float> mats_f32;         // FP32 copy for the SIMT mixed apply
   gbfe::DBuf<double> diag;
   uint64_t blk_begin = 0, blk_n = 0;  // OP_DIAG_BLOCK: dense block rows
@@ -252,6 +257,9 @@ void build_mixed_mats(gbfe_op *op);
 void build_tc_mats(gbfe_op *op);
 bool tc_supported(const gbfe_mesh *me);
 void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc);
+bool oz_supported(const gbfe_mesh *me);
+void build_oz_mats(gbfe_op *op);
+void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc);
 
 // vector kernels (solvers)
 void axpby(gbfe_ctx *ctx, size_t n, double a, const gbfe_mv *x, double b, const gbfe_mv *y, gbfe_mv *z);

@@ -806,6 +806,13 @@ int gbfe_ks_eigen_solve(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
     }
     uint32_t pass = 0;
     std::string msg;
+    const int saved_fp64 = ctx->fp64_tc;
+    ctx->fp64_tc = prm->fp64_apply ? 1 : 0;
+    struct Restore {
+      gbfe_ctx *c;
+      int v;
+      ~Restore() { c->fp64_tc = v; }
+    } restore{ctx, saved_fp64};
     if (!prm->faithful_passes) {
       status = ks_solve_fused(A, B, BInv, X, prm, wl, wu, uu, eigenvalues, residuals, passes_out, msg);
       if (status != GBFE_OK) ctx->last_error = msg.empty() ? "KS_MAX_PASS_ERROR: residual tolerance not reached" : msg;

@@ -25,6 +25,7 @@
 // in a device status word, skips the rest of its work, frees its TMEM and
 // returns.
 #include "gbfe_internal.cuh"
+#include "gbfe_tc_ptx.cuh"
 
 #include <algorithm>
 
@@ -36,89 +37,7 @@ void assemble_f32(const gbfe_op *op, const float *Yc, gbfe_mv *Y);
 
 namespace {
 
-constexpr int KC = 32;       // K extent of one pipeline stage (2 MMA K-steps)
-constexpr int STAGES = 3;
-constexpr int THREADS = 128;  // 4 warps: gather, epilogue; thread 0 issues TMA + MMA
-constexpr uint32_t CORE_BYTES = 128;             // one 8 x 16-byte core matrix
-constexpr uint32_t SBO = (KC / 8) * CORE_BYTES;  // stride between 8-row groups
-constexpr uint32_t LBO = CORE_BYTES;             // stride between K-adjacent core matrices
-constexpr uint32_t WAIT_LIMIT = 1u << 24;        // bounded mbarrier polls
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
-  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((LBO >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((SBO >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05; no swizzle, base offset 0
-  return d;
-}
-
-// kind::f16 instruction descriptor: D f32, A bf16, B bf16, both K-major
-__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-// bounded wait on the given phase parity; false (and an error code) on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code) {
-  const uint32_t a = smem_u32(bar);
-  for (uint32_t it = 0; it < WAIT_LIMIT; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  atomicCAS(status, 0, code);
-  return false;
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-          tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
-      : "memory");
-}
-
-__device__ __forceinline__ void umma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
-  hi = __float2bfloat16_rn(x);
-  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-}
+using namespace gbfe::tc;
 
 // Pre-split A_op = A_c^T into the per-(cell, K chunk) tile layout:
 // [hi: MT8 rows x KC][lo: MT8 rows x KC], element (r, kk) at
@@ -320,10 +239,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_cell_apply_tc(
 constexpr int MAX_STAGES = 4;
 constexpr int GATHER_WARPS = 4;
 constexpr int THREADS2 = 192;
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 
 struct Tc2Args {
   const float *X;

@@ -16,7 +16,7 @@ STATUS_NAMES = {
     5: "ERR_LAPACK", 6: "ERR_NOT_CONVERGED", 7: "ERR_DIVERGED", 8: "ERR_TIMEOUT", 9: "ERR_CANCELLED",
 }
 GBFE_F64, GBFE_F32 = 0, 1
-GBFE_PREC_FP64, GBFE_PREC_MIXED = 1, 2
+GBFE_PREC_FP64, GBFE_PREC_MIXED, GBFE_PREC_FP64_TENSOR = 1, 2, 4
 
 p = C.c_void_p
 u32, u64, i32, f64 = C.c_uint32, C.c_uint64, C.c_int, C.c_double
@@ -28,7 +28,7 @@ class KSParams(C.Structure):
         ("degree", u32), ("max_passes", u32), ("n_wanted", u32), ("filter_precision", i32),
         ("residual_tol", f64), ("wanted_lower", f64), ("wanted_upper", f64), ("unwanted_upper", f64),
         ("use_lanczos", i32), ("lanczos_steps", u32), ("lanczos_seed", u64), ("fixed_passes", i32),
-        ("faithful_passes", i32),
+        ("fp64_apply", i32), ("faithful_passes", i32),
     ]
 
 
@@ -54,6 +54,7 @@ SIGNATURES = {
     "gbfe_ctx_check_status": (i32, [p]),
     "gbfe_ctx_set_tensor_cores": (i32, [p, i32]),
     "gbfe_ctx_set_profiling": (i32, [p, i32]),
+    "gbfe_ctx_set_fp64_apply": (i32, [p, i32]),
     "gbfe_ctx_kernel_stats": (i32, [p, C.c_char_p, C.POINTER(u64), pf64, pf64, pf64]),
     "gbfe_ctx_reset_kernel_stats": (i32, [p]),
     "gbfe_probe_fp64_peak": (i32, [p, pf64]),

@@ -33,7 +33,8 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import GBFE_F32, GBFE_F64, GBFE_PREC_FP64, GBFE_PREC_MIXED, GBFEError, KSParams, check
+from ._lib import (GBFE_F32, GBFE_F64, GBFE_PREC_FP64, GBFE_PREC_FP64_TENSOR, GBFE_PREC_MIXED, GBFEError, KSParams,
+                   check)
 
 
 def _ptr(a: np.ndarray) -> C.c_void_p:
@@ -65,6 +66,10 @@ class LinAlgOpContext:
     def set_tensor_cores(self, mode: int) -> None:
         """2: persistent tcgen05 kernel (default), 1: one-CTA-per-cell tcgen05, 0: FP32 SIMT."""
         check(self.lib.gbfe_ctx_set_tensor_cores(self.h, int(mode)), self.h, "set_tensor_cores")
+
+    def set_fp64_apply(self, mode: int) -> None:
+        """0: FP64 FMA cell product; 1: FP64-accurate sliced tensor-core product."""
+        check(self.lib.gbfe_ctx_set_fp64_apply(self.h, int(mode)), self.h, "set_fp64_apply")
 
     def set_profiling(self, on: bool) -> None:
         check(self.lib.gbfe_ctx_set_profiling(self.h, 1 if on else 0), self.h, "set_profiling")
@@ -225,11 +230,11 @@ class OperatorContext:
 
 class CellMatrixOperatorContext(OperatorContext):
     def __init__(self, basis: FEBasisManager, cell_matrices: np.ndarray, mixed: bool = False,
-                 use_constraints: bool = True):
+                 use_constraints: bool = True, fp64_tensor: bool = False):
         self.basis, self.ctx = basis, basis.ctx
         mats = np.ascontiguousarray(cell_matrices, dtype=np.float64)
         h = C.c_void_p()
-        flags = GBFE_PREC_FP64 | (GBFE_PREC_MIXED if mixed else 0)
+        flags = GBFE_PREC_FP64 | (GBFE_PREC_MIXED if mixed else 0) | (GBFE_PREC_FP64_TENSOR if fp64_tensor else 0)
         cons = basis.cons_h if use_constraints else None
         check(self.ctx.lib.gbfe_cellmat_upload(basis.h, cons, _ptr(mats), flags, C.byref(h)), self.ctx.h,
               "cellmat_upload")
@@ -375,7 +380,7 @@ def lanczos_bounds(A, B, BInv, steps: int = 20, seed: int = 7) -> np.ndarray:
 class KohnShamEigenSolver:
     def __init__(self, n_wanted: int, degree: int, max_passes: int, residual_tol: float = 1e-6, mixed: bool = False,
                  bounds: Optional[Sequence[float]] = None, lanczos_steps: int = 20, lanczos_seed: int = 7,
-                 fixed_passes: bool = False, faithful_passes: bool = False):
+                 fixed_passes: bool = False, faithful_passes: bool = False, fp64_tensor: bool = False):
         self.p = KSParams()
         self.p.degree, self.p.max_passes, self.p.n_wanted = int(degree), int(max_passes), int(n_wanted)
         self.p.filter_precision = GBFE_F32 if mixed else GBFE_F64
@@ -388,6 +393,7 @@ class KohnShamEigenSolver:
         self.p.lanczos_steps, self.p.lanczos_seed = int(lanczos_steps), int(lanczos_seed)
         self.p.fixed_passes = 1 if fixed_passes else 0
         self.p.faithful_passes = 1 if faithful_passes else 0
+        self.p.fp64_apply = 1 if fp64_tensor else 0
 
     def solve(self, H, X: MultiVector, M, MInv, eigenvalues: Optional[np.ndarray] = None):
         ev = np.zeros(X.m) if eigenvalues is None else np.ascontiguousarray(eigenvalues, dtype=np.float64).copy()

@@ -29,7 +29,7 @@ WORKLOADS = {
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="cfg2c", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="mixed", choices=["f64", "mixed", "mixed_v1", "simt"])
+    ap.add_argument("--precision", default="mixed", choices=["f64", "f64_tensor", "mixed", "mixed_v1", "simt"])
     ap.add_argument("--m", type=int, default=0, help="vectors (0: the workload's)")
     ap.add_argument("--reps", type=int, default=10)
     args = ap.parse_args()
@@ -39,8 +39,10 @@ def main() -> None:
                     nq=w["nq"], matrices=("H",))
     ctx = api.LinAlgOpContext(0)
     basis = api.FEBasisManager.from_problem(ctx, prob)
-    mixed = args.precision != "f64"
-    H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=mixed)
+    mixed = args.precision not in ("f64", "f64_tensor")
+    H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=mixed, fp64_tensor=args.precision == "f64_tensor")
+    if args.precision == "f64_tensor":
+        ctx.set_fp64_apply(1)
     dt = np.float32 if mixed else np.float64
     X = api.MultiVector(basis, m, dtype=dt, init=M.random_block(prob.n_dofs, m, 1).astype(dt))
     Y = api.MultiVector(basis, m, dtype=dt)
@@ -58,7 +60,8 @@ def main() -> None:
         H.apply(X, Y)
     ctx.synchronize()
     wall = (time.perf_counter() - t0) / args.reps
-    st = ctx.kernel_stats("cell_apply_f64" if not mixed else "cell_apply_mixed")
+    st = ctx.kernel_stats({"f64": "cell_apply_f64", "f64_tensor": "cell_apply_f64_oz"}.get(args.precision,
+                                                                                         "cell_apply_mixed"))
     ctx.check_status()
     sx = 4 if mixed else 8
     flops = 2.0 * m * float((prob.nd_per_cell.astype(np.float64) ** 2).sum())

@@ -48,7 +48,9 @@ enum { GBFE_F64 = 0, GBFE_F32 = 1 };
 /* cell-matrix precision variants an operator carries */
 enum {
   GBFE_PREC_FP64 = 1,          /* FP64 matrices (always present)               */
-  GBFE_PREC_MIXED = 2          /* + split-BF16 hi/lo copies for the FP32 path   */
+  GBFE_PREC_MIXED = 2,         /* + split-BF16 hi/lo copies for the FP32 path   */
+  GBFE_PREC_FP64_TENSOR = 4    /* + 8-slice integer copies for the FP64-accurate
+                                  tensor-core product (cells up to 256 dofs)    */
 };
 
 typedef struct gbfe_ctx gbfe_ctx;
@@ -74,6 +76,11 @@ int gbfe_ctx_check_status(gbfe_ctx *ctx);
  * SIMT kernel.  The environment variable GBFE_TENSOR_CORES=0|1 sets the
  * initial mode of a new context. */
 int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode);
+/* FP64 applies: 0 (default) FP64 FMA cell product; 1 the FP64-accurate
+ * sliced tensor-core product (Ozaki-style splitting into eight 7-bit slices,
+ * exact FP32 accumulation per level), for operators built with
+ * GBFE_PREC_FP64_TENSOR. */
+int gbfe_ctx_set_fp64_apply(gbfe_ctx *ctx, int mode);
 /* number of kernels this context has launched so far */
 int gbfe_ctx_kernel_launches(const gbfe_ctx *ctx, uint64_t *count);
 /* Per-kernel timing (no counterpart in the reference, whose Profiler times
@@ -233,6 +240,8 @@ typedef struct {
   uint32_t lanczos_steps;       /* Krylov dimension (reference default 20)    */
   uint64_t lanczos_seed;
   int      fixed_passes;        /* 1: run exactly max_passes passes           */
+  int      fp64_apply;          /* 0: FP64 FMA cell products; 1: the sliced
+                                   tensor-core FP64 product where available   */
   int      faithful_passes;     /* 1: every pass repeats the reference's call
                                    sequence (filter with its own A X, B X;
                                    Cholesky-GS; Rayleigh-Ritz; residual with
