@@ -517,6 +517,20 @@ def run_serving(args):
     print(json.dumps(line))
 
 
+def aggregate_replicas(t_total: float, steps: int, world: int):
+    """Replicas only (no data-path collective): every rank solves its own copy;
+    the job's time is the slowest rank's (max over ranks through the process
+    group), and the value counts the steps of all ranks."""
+    if world > 1:
+        import torch
+
+        t = torch.tensor([t_total], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(t.item())
+    t_step = t_total / steps
+    return world / t_step, t_step
+
+
 def pct(v, q):
     return float(np.percentile(np.asarray(v), q))
 
@@ -578,14 +592,7 @@ def main():
         torch.distributed.init_process_group("gloo")
     r = run_gpu(args, args.config, rank, world)
     prob = r["prob"]
-    t_step = r["t_total"] / args.steps
-    if world > 1:
-        import torch
-
-        t = torch.tensor([r["t_total"]], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(t.item()) / args.steps
-    value = world / t_step  # replicas: every rank solves its own copy
+    value, t_step = aggregate_replicas(r["t_total"], args.steps, world)
     fp64_sps = 1.0 / float(np.median(r["fp64_times"]))
     cand = {"cell_apply_f64": r["st_f64"], "cell_apply_mixed": r["st_mixed"], "cell_apply_f64_oz": r["st_oz"]}
     dom = max(cand, key=lambda k: cand[k]["ms"])

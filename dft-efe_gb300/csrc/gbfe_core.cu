@@ -491,6 +491,12 @@ int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode) {
   return GBFE_OK;
 }
 
+int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on) {
+  if (!ctx) return GBFE_ERR_ARG;
+  ctx->use_graphs = on ? 1 : 0;
+  return GBFE_OK;
+}
+
 int gbfe_ctx_set_fp64_apply(gbfe_ctx *ctx, int mode) {
   if (!ctx || mode < 0 || mode > 1) return GBFE_ERR_ARG;
   ctx->fp64_tc = mode;

@@ -117,9 +117,18 @@ struct KernelStat {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
 };
 
+// one timed kernel inside a captured graph (event-record nodes around it)
+struct GraphProf {
+  std::string name;
+  cudaEvent_t e0, e1;
+  double flops, bytes;
+};
+
 struct gbfe_ctx {
   int device = 0;
   int profiling = 0;
+  std::vector<GraphProf> *capture_prof = nullptr;  // set while a graph is captured with profiling on
+  int use_graphs = 1;        // capture the Chebyshev recurrence into a CUDA graph
   std::map<std::string, KernelStat> kstats;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
@@ -226,17 +235,28 @@ struct ProfScope {
   gbfe_ctx *ctx;
   KernelStat *st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  ProfScope(gbfe_ctx *c, const char *name, double flops, double bytes) : ctx(c) {
+  const char *nm = nullptr;
+  double fl = 0, by = 0;
+  ProfScope(gbfe_ctx *c, const char *name, double flops, double bytes) : ctx(c), nm(name), fl(flops), by(bytes) {
     if (!ctx->profiling) return;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    if (ctx->capture_prof) {  // inside a graph: an event-record node, read after each replay
+      cudaEventRecordWithFlags(e0, ctx->stream, cudaEventRecordExternal);
+      return;
+    }
     st = &ctx->kstats[name];
     st->flops += flops;
     st->bytes += bytes;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
     cudaEventRecord(e0, ctx->stream);
   }
   ~ProfScope() {
-    if (!st) return;
+    if (!ctx->profiling || !e0) return;
+    if (ctx->capture_prof && !st) {
+      cudaEventRecordWithFlags(e1, ctx->stream, cudaEventRecordExternal);
+      ctx->capture_prof->push_back(GraphProf{nm, e0, e1, fl, by});
+      return;
+    }
     cudaEventRecord(e1, ctx->stream);
     st->pending.emplace_back(e0, e1);
     st->launches++;

@@ -400,7 +400,11 @@ void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc) {
   count_launch(ctx, 2);
   const uint32_t vt = (m + OZ_N - 1) / OZ_N;
   const uint32_t smem = OZ_STAGES * OZ_STAGE + 1024 + 512;
-  GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static bool attr_set = false;  // once: not a stream operation, so it stays out of graph captures
+  if (!attr_set) {
+    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
   for (uint32_t mts = 1; mts <= 2; ++mts) {
     uint32_t b0 = UINT32_MAX, b1 = 0;
     for (uint32_t b = 0; b < me->bin_nd.size(); ++b)

@@ -57,6 +57,21 @@ __global__ void k_cheb_step(uint64_t n, uint32_t m, double alpha1, double c, dou
   }
 }
 
+// the same step with its scalars read from a device table {alpha1, c, alpha2},
+// so one captured graph serves every pass
+template <class T>
+__global__ void k_cheb_step_dev(uint64_t n, uint32_t m, const double *__restrict__ coef, const T *__restrict__ AS,
+                                const T *__restrict__ RN, T *__restrict__ R, const double *__restrict__ eF2,
+                                const T *__restrict__ Y) {
+  const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t j = (uint32_t)(t % m);
+    T s1 = (T)alpha1 * AS[t] + (T)(-c * alpha1) * RN[t];
+    T r = s1 + (T)alpha2 * R[t];
+    R[t] = r + (T)(alpha1 * eF2[j]) * Y[t];
+  }
+}
+
 // Y = R + eF2[j] * X, with R in FP32 and X, Y in FP64 (mixed filter epilogue)
 __global__ void k_cheb_final_mixed(uint64_t n, uint32_t m, const float *__restrict__ R, const double *__restrict__ eF2,
                                    const double *__restrict__ X, double *__restrict__ Y) {
@@ -340,25 +355,74 @@ void launch_cheb_step<float>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha
   check_launch(ctx, "cheb_step_f32");
 }
 
+// Persistent buffers of the filter across passes, and the captured graph of its
+// recurrence (valid for one operator pair, degree, width and precision).
+struct FilterWork {
+  std::unique_ptr<gbfe_mv> s1, s2, R, RN, Yf;
+  DBuf<double> tab, coef;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<GraphProf> prof;
+  uint64_t per_replay = 0;
+  const gbfe_op *A = nullptr, *BInv = nullptr;
+  uint32_t degree = 0, m = 0;
+  int prec = -1, uses = 0, graph_failed = 0;
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    for (auto &g : prof) {
+      cudaEventDestroy(g.e0);
+      cudaEventDestroy(g.e1);
+    }
+    prof.clear();
+  }
+  ~FilterWork() { drop_graph(); }
+};
+
 // precision GBFE_F64: the recurrence in FP64.  GBFE_F32: the initial residual
 // (A X - Lambda B X) and the final Y = B^-1 R + Lambda~ X stay FP64; the d-1
 // recurrence steps run on FP32 block vectors with split-BF16 tensor-core cell
 // products (the operator must carry GBFE_PREC_MIXED matrices).
 void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, const double *eig_h, gbfe_mv *X,
                      uint32_t degree, double wl, double wu, double uu, gbfe_mv *Y, int prec,
-                     const gbfe_mv *R0 = nullptr) {
+                     const gbfe_mv *R0 = nullptr, FilterWork *fw = nullptr) {
   gbfe_ctx *ctx = X->mesh->ctx;
   const uint32_t m = X->m;
   const bool mixed = prec == GBFE_F32;
   GBFE_REQUIRE(!mixed || (A->prec & GBFE_PREC_MIXED), "mixed filter: operator A was not built with GBFE_PREC_MIXED");
   const int rt = mixed ? GBFE_F32 : GBFE_F64;
   const ChebSchedule s = cheb_schedule(eig_h, m, degree, wl, wu, uu);
-  DevVec d_ones(m), d_eig(m), d_tab(s.eF2.size());
+  FilterWork local;
+  FilterWork &w = fw ? *fw : local;
+  if (!w.s1 || w.m != m || w.prec != prec || w.degree != degree || w.A != A || w.BInv != BInv) {
+    w.drop_graph();
+    w.s1 = make_like(X, rt);
+    w.s2 = make_like(X, rt);
+    w.R = make_like(X, rt);
+    w.RN = make_like(X, rt);
+    w.Yf = mixed ? make_like(X, GBFE_F32) : nullptr;
+    w.tab.alloc(s.eF2.size());
+    w.coef.alloc(3 * std::max<uint32_t>(1, degree));
+    w.A = A;
+    w.BInv = BInv;
+    w.m = m;
+    w.prec = prec;
+    w.degree = degree;
+    w.uses = 0;
+  }
+  std::vector<double> coef(3 * std::max<uint32_t>(1, degree), 0.0);
+  for (uint32_t k = 0; k + 2 <= degree; ++k) {
+    coef[3 * k] = s.alpha1[k];
+    coef[3 * k + 1] = s.c;
+    coef[3 * k + 2] = s.alpha2[k];
+  }
+  DevVec d_ones(m), d_eig(m);
   std::vector<double> ones(m, 1.0);
   d_ones.set(ctx, ones.data(), m);
   d_eig.set(ctx, eig_h, m);
-  d_tab.set(ctx, s.eF2.data(), s.eF2.size());
-  auto s1 = make_like(X, rt), s2 = make_like(X, rt), R = make_like(X, rt), RN = make_like(X, rt);
+  GBFE_CUDA(cudaMemcpyAsync(w.tab.p, s.eF2.data(), s.eF2.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  GBFE_CUDA(cudaMemcpyAsync(w.coef.p, coef.data(), coef.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  gbfe_mv *s1 = w.s1.get(), *s2 = w.s2.get();
+  std::unique_ptr<gbfe_mv> &R = w.R, &RN = w.RN;
   if (R0) {
     // the caller already holds A X - Lambda B X (the residual of the previous
     // Rayleigh-Ritz step), so the two initial applies are skipped
@@ -369,35 +433,96 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
     apply_op(A, X, s3.get());
     d_axpby_blocked(ctx, 1.0, d_ones.b.p, s3.get(), -1.0, d_eig.b.p, Y, Y);  // Y = AX - lambda BX
   }
-  std::unique_ptr<gbfe_mv> Yf;
   const gbfe_mv *Yr = Y;
   if (mixed) {
-    Yf = make_like(X, GBFE_F32);
-    convert_mv(ctx, Y, Yf.get());
-    Yr = Yf.get();
+    convert_mv(ctx, Y, w.Yf.get());
+    Yr = w.Yf.get();
   }
   d_axpby(ctx, s.alpha1_init, Yr, 0.0, Yr, RN.get());  // ResidualNew = alpha1 * Y
   fill_mv(ctx, R.get(), 0.0);
   const uint64_t n = X->count();
-  for (uint32_t deg = 2; deg <= degree; ++deg) {
-    const uint32_t k = deg - 2;
-    apply_op(BInv, RN.get(), s1.get());
-    apply_op(A, s1.get(), s2.get());
-    if (mixed)
-      launch_cheb_step<float>(ctx, n, m, s.alpha1[k], s.c, s.alpha2[k], s2.get(), RN.get(), R.get(),
-                              d_tab.b.p + (size_t)k * m, Yr);
-    else
-      launch_cheb_step<double>(ctx, n, m, s.alpha1[k], s.c, s.alpha2[k], s2.get(), RN.get(), R.get(),
-                               d_tab.b.p + (size_t)k * m, Yr);
-    std::swap(RN, R);
+  // the d-1 recurrence steps: pointers and table offsets are fixed for a given
+  // degree, the scalars come from device tables -> one graph for every pass
+  auto recurrence = [&]() {
+    for (uint32_t deg = 2; deg <= degree; ++deg) {
+      const uint32_t k = deg - 2;
+      gbfe_mv *rn = ((deg - 2) % 2 == 0) ? RN.get() : R.get();
+      gbfe_mv *r = ((deg - 2) % 2 == 0) ? R.get() : RN.get();
+      apply_op(BInv, rn, s1);
+      apply_op(A, s1, s2);
+      if (mixed)
+        k_cheb_step_dev<float><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, w.coef.p + 3 * k, s2->f.p, rn->f.p,
+                                                                        r->f.p, w.tab.p + (size_t)k * m, Yr->f.p);
+      else
+        k_cheb_step_dev<double><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, w.coef.p + 3 * k, s2->d.p, rn->d.p,
+                                                                         r->d.p, w.tab.p + (size_t)k * m, Yr->d.p);
+      check_launch(ctx, "cheb_step");
+    }
+  };
+  const bool can_graph = fw && ctx->use_graphs && !w.graph_failed && degree >= 2 && w.uses >= 1;
+  if (can_graph && !w.exec) {
+    // capture on the second use: every lazily sized buffer exists by then
+    const uint64_t l0 = ctx->launches;
+    std::vector<GraphProf> prof;
+    if (ctx->profiling) ctx->capture_prof = &prof;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      try {
+        recurrence();
+      } catch (...) {
+        e = cudaErrorStreamCaptureInvalidated;
+      }
+      const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+      if (e == cudaSuccess) e = e2;
+    }
+    ctx->capture_prof = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&w.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    w.per_replay = ctx->launches - l0;
+    ctx->launches = l0;
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      for (auto &g : prof) {
+        cudaEventDestroy(g.e0);
+        cudaEventDestroy(g.e1);
+      }
+      w.exec = nullptr;
+      w.graph_failed = 1;
+    } else {
+      w.prof = std::move(prof);
+    }
   }
-  apply_op(BInv, RN.get(), R.get());
-  const double *eF2_final = d_tab.b.p + (size_t)(degree - 1) * m;
+  if (can_graph && w.exec) {
+    GBFE_CUDA(cudaGraphLaunch(w.exec, ctx->stream));
+    ctx->launches += w.per_replay;
+    if (!w.prof.empty()) {
+      // kernel timings of this replay (event-record nodes inside the graph)
+      GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (auto &g : w.prof) {
+        float ms = 0.f;
+        GBFE_CUDA(cudaEventElapsedTime(&ms, g.e0, g.e1));
+        KernelStat &st = ctx->kstats[g.name];
+        st.ms += ms;
+        st.launches++;
+        st.flops += g.flops;
+        st.bytes += g.bytes;
+      }
+    }
+  } else {
+    recurrence();
+  }
+  w.uses++;
+  gbfe_mv *last = (degree >= 2 && (degree - 2) % 2 == 0) ? R.get() : RN.get();  // holds the newest iterate
+  gbfe_mv *other = last == R.get() ? RN.get() : R.get();
+  apply_op(BInv, last, other);
+  gbfe_mv *Rfin = other;
+  const double *eF2_final = w.tab.p + (size_t)(degree - 1) * m;
   if (mixed) {
-    k_cheb_final_mixed<<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, R->f.p, eF2_final, X->d.p, Y->d.p);
+    k_cheb_final_mixed<<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, Rfin->f.p, eF2_final, X->d.p, Y->d.p);
     check_launch(ctx, "cheb_final_mixed");
   } else {
-    d_axpby_blocked(ctx, 1.0, d_ones.b.p, R.get(), 1.0, eF2_final, X, Y);
+    d_axpby_blocked(ctx, 1.0, d_ones.b.p, Rfin, 1.0, eF2_final, X, Y);
   }
   GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
 }
@@ -519,6 +644,7 @@ int chfsi_pass_impl(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbf
 struct FusedState {
   std::unique_ptr<gbfe_mv> Y, MY, HY, HX, MX, R;
   DBuf<double> SM, SH, V;
+  FilterWork fw;
 };
 
 int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv *X, double *eig_h,
@@ -527,7 +653,7 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   gbfe_ctx *ctx = X->mesh->ctx;
   const int m = (int)X->m;
   const int N = (int)X->mesh->n_dofs;
-  residual_filter(A, B, BInv, eig_h, X, degree, wl, wu, uu, st.Y.get(), prec, st.R.get());
+  residual_filter(A, B, BInv, eig_h, X, degree, wl, wu, uu, st.Y.get(), prec, st.R.get(), &st.fw);
   apply_op(B, st.Y.get(), st.MY.get());
   apply_op(A, st.Y.get(), st.HY.get());
   gram(ctx, st.Y.get(), st.MY.get(), st.SM.p);

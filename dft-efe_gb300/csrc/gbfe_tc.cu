@@ -512,7 +512,11 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
   const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>((227 * 1024) / smem, 512 / cols));
   const uint32_t items = ncell * vt;
   const uint32_t grid = std::min<uint32_t>(items, per_sm * (uint32_t)ctx->sm_count);
-  GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static bool attr_set = false;
+  if (!attr_set) {
+    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr_set = true;
+  }
   Tc2Args args{X->f.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, vt, op->tc_aoff.p,
                op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p};
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,

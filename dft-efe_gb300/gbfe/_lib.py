@@ -55,6 +55,7 @@ SIGNATURES = {
     "gbfe_ctx_set_tensor_cores": (i32, [p, i32]),
     "gbfe_ctx_set_profiling": (i32, [p, i32]),
     "gbfe_ctx_set_fp64_apply": (i32, [p, i32]),
+    "gbfe_ctx_set_graphs": (i32, [p, i32]),
     "gbfe_ctx_kernel_stats": (i32, [p, C.c_char_p, C.POINTER(u64), pf64, pf64, pf64]),
     "gbfe_ctx_reset_kernel_stats": (i32, [p]),
     "gbfe_probe_fp64_peak": (i32, [p, pf64]),
@@ -70,6 +71,8 @@ SIGNATURES = {
     "gbfe_diag_block_upload": (i32, [p, p, p, u64, u64, p, C.POINTER(p)]),
     "gbfe_jacobi_upload": (i32, [p, p, C.POINTER(p)]),
     "gbfe_op_destroy": (i32, [p]),
+    "gbfe_op_assemble_local": (i32, [p, u32, p, p, p, f64]),
+    "gbfe_density": (i32, [p, p, u32, p, p]),
     "gbfe_mv_create": (i32, [p, u32, i32, C.POINTER(p)]),
     "gbfe_mv_wrap": (i32, [p, u32, i32, p, C.POINTER(p)]),
     "gbfe_mv_destroy": (i32, [p]),

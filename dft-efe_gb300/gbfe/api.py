@@ -67,6 +67,9 @@ class LinAlgOpContext:
         """2: persistent tcgen05 kernel (default), 1: one-CTA-per-cell tcgen05, 0: FP32 SIMT."""
         check(self.lib.gbfe_ctx_set_tensor_cores(self.h, int(mode)), self.h, "set_tensor_cores")
 
+    def set_graphs(self, on: bool) -> None:
+        check(self.lib.gbfe_ctx_set_graphs(self.h, 1 if on else 0), self.h, "set_graphs")
+
     def set_fp64_apply(self, mode: int) -> None:
         """0: FP64 FMA cell product; 1: FP64-accurate sliced tensor-core product."""
         check(self.lib.gbfe_ctx_set_fp64_apply(self.h, int(mode)), self.h, "set_fp64_apply")
@@ -240,6 +243,25 @@ class CellMatrixOperatorContext(OperatorContext):
               "cellmat_upload")
         self.h = h
         self.mixed = mixed
+
+
+def assemble_local(op: "OperatorContext", basis_values: np.ndarray, weights: np.ndarray,
+                   fixed_mats: Optional[np.ndarray] = None, alpha: float = 1.0) -> None:
+    """A_c = alpha F_c + B^T diag(w_c) B on the device (KohnShamOperatorContextFE::reinit)."""
+    B = np.ascontiguousarray(basis_values, dtype=np.float64)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    F = None if fixed_mats is None else np.ascontiguousarray(fixed_mats, dtype=np.float64)
+    check(op.ctx.lib.gbfe_op_assemble_local(op.h, B.shape[0], _ptr(B), _ptr(w), _ptr(F) if F is not None else None,
+                                            float(alpha)), op.ctx.h, "assemble_local")
+
+
+def density(Psi: "MultiVector", occupation, basis_values: np.ndarray) -> np.ndarray:
+    """rho[c][q] = sum_i 2 f_i psi_i(x_cq)^2 (DensityCalculator::computeRho)."""
+    B = np.ascontiguousarray(basis_values, dtype=np.float64)
+    f = np.ascontiguousarray(occupation, dtype=np.float64)
+    out = np.empty((Psi.basis.n_cells, B.shape[0]))
+    check(Psi.ctx.lib.gbfe_density(Psi.h, _ptr(f), B.shape[0], _ptr(B), _ptr(out)), Psi.ctx.h, "density")
+    return out
 
 
 class IndexedCellMatrixOperatorContext(OperatorContext):

@@ -227,7 +227,7 @@ def add_synthetic_hanging(cons: Constraints, n: int, p: int, rng: np.random.Gene
 
 def build_problem(n: int, p: int, length: float, atoms: np.ndarray, charges: np.ndarray, rc: float,
                   nq: Optional[int] = None, matrices: tuple = ("K", "M", "V", "H"),
-                  cell_chunk: int = 2048) -> FEProblem:
+                  cell_chunk: int = 2048, keep_quadrature: bool = False) -> FEProblem:
     """Assemble a uniform-hex FE problem (see module docstring)."""
     nq = nq or (p + 1)
     n1 = n * p + 1
@@ -275,11 +275,14 @@ def build_problem(n: int, p: int, length: float, atoms: np.ndarray, charges: np.
         V = np.empty(C * nd * nd) if "V" in matrices else None
         H = np.empty(C * nd * nd) if "H" in matrices else None
         halfK = 0.5 * Kc
+        quad_w = np.empty((C, nq ** 3)) if keep_quadrature else None
         for c0 in range(0, C, cell_chunk):
             c1 = min(C, c0 + cell_chunk)
             pts = corner[c0:c1, None, :] + (qloc[None, :, :] + 1.0) * jac
             vq = local_potential(pts.reshape(-1, 3), prob.atoms, prob.charges, rc).reshape(c1 - c0, -1)
             wv = vq * wq3[None, :]
+            if quad_w is not None:
+                quad_w[c0:c1] = wv
             Vc = np.matmul(B.T[None, :, :] * wv[:, None, :], B[None, :, :])  # [c, nd, nd] symmetric
             Vc = 0.5 * (Vc + np.transpose(Vc, (0, 2, 1)))
             seg = slice(c0 * nd * nd, c1 * nd * nd)
@@ -288,6 +291,10 @@ def build_problem(n: int, p: int, length: float, atoms: np.ndarray, charges: np.
             if H is not None:
                 H[seg] = np.transpose(Vc + halfK[None], (0, 2, 1)).ravel()
         prob.V, prob.H = V, H
+        if keep_quadrature:
+            # B[q][a] and w[c][q] = JxW * V_loc: H_c = 0.5 K_c + B^T diag(w_c) B
+            prob.extra.update(quad_B=np.ascontiguousarray(B), quad_w=quad_w, quad_JxW=wq3.copy(),
+                              K_cell=Kc.T.ravel().copy())
 
     # GLL-lumped mass diagonal: w_i w_j w_k jac^3 assembled over cells
     wl = np.einsum("k,j,i->kji", wg, wg, wg).ravel() * jac ** 3

@@ -76,6 +76,10 @@ int gbfe_ctx_check_status(gbfe_ctx *ctx);
  * SIMT kernel.  The environment variable GBFE_TENSOR_CORES=0|1 sets the
  * initial mode of a new context. */
 int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode);
+/* 1 (default): inside gbfe_ks_eigen_solve the d-1 steps of the Chebyshev
+ * recurrence are captured once into a CUDA graph (second pass) and replayed
+ * on every later pass; 0: launched one by one. */
+int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on);
 /* FP64 applies: 0 (default) FP64 FMA cell product; 1 the FP64-accurate
  * sliced tensor-core product (Ozaki-style splitting into eight 7-bit slices,
  * exact FP32 accumulation per level), for operators built with
@@ -154,6 +158,18 @@ int gbfe_diag_block_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double 
  * here from `diagonal` exactly as the reference constructor does). */
 int gbfe_jacobi_upload(gbfe_mesh *mesh, const double *diagonal, gbfe_op **out);
 int gbfe_op_destroy(gbfe_op *op);
+/* Rebuild a cell operator's matrices on the device (uniform nd):
+ *   A_c = alpha * F_c + B^T diag(w_c) B
+ * B: basis values at the nq quadrature points of the reference cell, row-major
+ * [nq][nd]; weights: [n_cells][nq] quadrature weight times Jacobian times the
+ * field (e.g. the local potential); fixed_mats: cell-concatenated column-major
+ * F_c (e.g. the Laplace matrices, alpha = 0.5 for the kinetic part) or NULL.
+ * This is KohnShamOperatorContextFE::reinit (KohnShamOperatorContextFE.t.cpp:
+ * 1253-1311) with KineticFE (KineticFE.t.cpp:90-97) and ElectrostaticLocalFE
+ * (ElectrostaticLocalFE.t.cpp:1625-1660) getLocal on the device.  The derived
+ * FP32, split-BF16 and sliced copies are rebuilt. */
+int gbfe_op_assemble_local(gbfe_op *op, uint32_t nq, const double *basis_values, const double *weights,
+                           const double *fixed_mats, double alpha);
 
 /* ---- block vectors (MultiVector) -------------------------------------------- */
 int gbfe_mv_create(gbfe_mesh *mesh, uint32_t m, int dtype, gbfe_mv **out);
@@ -225,6 +241,13 @@ int gbfe_rayleigh_ritz(const gbfe_op *A, gbfe_mv *X, double *eigenvalues_host, g
  * (KohnShamEigenSolver.t.cpp:574-684): ||A x_i - eps_i B x_i||_2. */
 int gbfe_eigen_residual_norms(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X,
                               const double *eigenvalues, double *norms_host);
+
+/* Electron density at the quadrature points (uniform nd):
+ * rho[c][q] = sum_i 2 f_i (sum_a B[q][a] Psi[ids_c[a]][i])^2 with B row-major
+ * [nq][nd] (DensityCalculator::computeRho, ksdft/DensityCalculator.t.cpp:
+ * 37-100, 283-345).  rho_host: [n_cells][nq]. */
+int gbfe_density(const gbfe_mv *Psi, const double *occupation, uint32_t nq, const double *basis_values,
+                 double *rho_host);
 
 /* ---- ChFSI ---------------------------------------------------------------- */
 typedef struct {

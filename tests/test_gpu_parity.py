@@ -363,3 +363,31 @@ def test_mixed_ks_solve_eigenvalues(gpu_ctx, small_problem):
     gpu_ctx.check_status()
     assert rc64 == 0 and rc32 == 0
     assert np.abs(e32[:nw] - e64[:nw]).max() <= 1e-6
+
+
+def test_graph_replayed_filter_matches_eager(gpu_ctx, small_problem):
+    """KS solves with the Chebyshev recurrence captured into a CUDA graph
+    (replayed from the second pass on) give bitwise the same eigenvalues as
+    the eagerly launched recurrence, FP64 and mixed."""
+    from gbfe import api
+
+    p = small_problem
+    basis = api.FEBasisManager.from_problem(gpu_ctx, p)
+    H = api.KohnShamOperatorContextFE(basis, p.H, mixed=True)
+    Mo = api.CFEOverlapOperatorContext(basis, p.M, mixed=True)
+    Mi = api.CFEOverlapInverseOpContextGLL(basis, p.m_gll_diag)
+    X0 = M.random_block(p.n_dofs, 8, 21)
+    b = api.lanczos_bounds(H, Mo, Mi)
+    bounds = (b[0], b[0] + 0.1 * (b[1] - b[0]), b[1] + b[2] / 10)
+    for mixed in (False, True):
+        out = []
+        for graphs in (False, True):
+            gpu_ctx.set_graphs(graphs)
+            X = api.MultiVector(basis, 8, init=X0)
+            l0 = gpu_ctx.kernel_launches()
+            rc, eig, res, passes = api.KohnShamEigenSolver(4, 10, 6, 1e-12, mixed=mixed, bounds=bounds,
+                                                           fixed_passes=True).solve(H, X, Mo, Mi)
+            out.append((eig, X.numpy(), gpu_ctx.kernel_launches() - l0))
+        gpu_ctx.set_graphs(True)
+        assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+        assert out[0][2] == out[1][2]  # replays count the kernels they contain
