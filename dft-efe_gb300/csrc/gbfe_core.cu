@@ -421,6 +421,18 @@ int gbfe_ctx_create(int device, gbfe_ctx **out) {
     GBFE_CUSOLVER(cusolverDnSetStream(ctx->cusolver, ctx->stream));
     ctx->status.alloc(4);
     GBFE_CUDA(cudaMemsetAsync(ctx->status.p, 0, 4 * sizeof(int), ctx->stream));
+    if (const char *cache = getenv("GBFE_AUTOTUNE_CACHE")) {
+      ctx->tune_cache = cache;
+      FILE *f = fopen(cache, "r");
+      if (f) {
+        char kind[16];
+        unsigned nd, mt, mm, N, st;
+        float ms;
+        while (fscanf(f, "%15s %u %u %u %u %u %f", kind, &nd, &mt, &mm, &N, &st, &ms) == 7)
+          if (std::string(kind) == "tc2") ctx->tc_tune[std::make_tuple(nd, mt, mm)] = TcTune{N, st, ms};
+        fclose(f);
+      }
+    }
     const char *tc = getenv("GBFE_TENSOR_CORES");
     if (tc && tc[0] == '0') ctx->use_tc = 0;
     if (tc && tc[0] == '1') ctx->tc_version = 1;
@@ -489,6 +501,25 @@ int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode) {
   ctx->use_tc = mode ? 1 : 0;
   if (mode) ctx->tc_version = mode;
   return GBFE_OK;
+}
+
+int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len) {
+  if (!op) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = op->mesh->ctx;
+  return gbfe_guard(ctx, [&] {
+    std::vector<std::string> log;
+    autotune_tc(op, m, log);
+    std::string all;
+    for (auto &l : log) all += l + "\n";
+    if (report && report_len) snprintf(report, report_len, "%s", all.c_str());
+    if (!ctx->tune_cache.empty()) {
+      FILE *f = fopen(ctx->tune_cache.c_str(), "a");
+      if (f) {
+        fputs(all.c_str(), f);
+        fclose(f);
+      }
+    }
+  });
 }
 
 int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on) {

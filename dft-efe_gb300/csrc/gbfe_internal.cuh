@@ -26,6 +26,7 @@
 #include <cstdio>
 #include <atomic>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <string>
 #include <vector>
@@ -124,8 +125,17 @@ struct GraphProf {
   double flops, bytes;
 };
 
+// autotuned launch shape of the persistent tensor-core kernel, keyed by
+// (largest cell size of the launch group, 128-row tiles, vectors)
+struct TcTune {
+  uint32_t N = 0, stages = 0;
+  float ms = 0.f;
+};
+
 struct gbfe_ctx {
   int device = 0;
+  std::map<std::tuple<uint32_t, uint32_t, uint32_t>, TcTune> tc_tune;
+  std::string tune_cache;    // file the tuned shapes are read from / appended to
   int profiling = 0;
   std::vector<GraphProf> *capture_prof = nullptr;  // set while a graph is captured with profiling on
   int use_graphs = 1;        // capture the Chebyshev recurrence into a CUDA graph
@@ -277,6 +287,7 @@ void build_mixed_mats(gbfe_op *op);
 void build_tc_mats(gbfe_op *op);
 bool tc_supported(const gbfe_mesh *me);
 void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc);
+void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log);
 bool oz_supported(const gbfe_mesh *me);
 void build_oz_mats(gbfe_op *op);
 void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc);

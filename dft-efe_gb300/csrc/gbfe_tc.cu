@@ -491,17 +491,26 @@ void build_tc_mats(gbfe_op *op) {
 
 bool tc_supported(const gbfe_mesh *me) { return me->nd_max <= 256; }
 
-// v2 launch: persistent grid over (cell, vector tile) items of one M-tile group
+// v2 launch: persistent grid over (cell, vector tile) items of one M-tile group.
+// N_req / stages_req = 0: the tuned shape if one exists, else the heuristic.
 static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg, uint32_t ncell,
-                       uint32_t mtiles, double frac) {
+                       uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0, uint32_t stages_req = 0) {
   gbfe_mesh *me = op->mesh;
   const uint32_t m = X->m;
+  if (!N_req) {
+    auto it = ctx->tc_tune.find(std::make_tuple(nd_max, mtiles, m));
+    if (it != ctx->tc_tune.end()) {
+      N_req = it->second.N;
+      stages_req = it->second.stages;
+    }
+  }
   uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
+  if (N_req) N = std::min<uint32_t>(N, N_req);
   const uint32_t vt = (m + N - 1) / N;
   N = ((m + vt - 1) / vt + 15) / 16 * 16;
   const uint32_t a_part = mtiles * 128 * KC * 2, b_part = N * KC * 2;
   const uint32_t stage_bytes = 2 * a_part + 2 * b_part;
-  uint32_t stages = MAX_STAGES;
+  uint32_t stages = stages_req ? std::min<uint32_t>(stages_req, MAX_STAGES) : MAX_STAGES;
   const uint32_t reserve = 1024 + 512;
   while (stages > 2 && stages * stage_bytes + reserve > 227 * 1024) --stages;
   GBFE_REQUIRE(stages * stage_bytes + reserve <= 227 * 1024, "tensor-core tile does not fit in shared memory");
@@ -546,7 +555,7 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc) {
     const uint32_t cbeg = me->bin_begin[b0], cend = me->bin_begin[b1];
     const uint32_t ncell = cend - cbeg;
     if (ctx->tc_version == 2) {
-      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells);
+      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1]);
       continue;
     }
     uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
@@ -564,6 +573,64 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc) {
                                                                    ctx->status.p);
     check_launch(ctx, "cell_apply_tc");
   }
+}
+
+// Time every (vector tile, stages) shape of the persistent kernel on this
+// operator with m vectors and keep the fastest per launch group.
+void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
+  gbfe_mesh *me = op->mesh;
+  gbfe_ctx *ctx = me->ctx;
+  GBFE_REQUIRE(op->tc_aoff.p, "autotune: operator has no tensor-core tiles (build it with GBFE_PREC_MIXED)");
+  gbfe_mv X;
+  X.mesh = me;
+  X.m = m;
+  X.dtype = GBFE_F32;
+  X.f.alloc(X.count());
+  GBFE_CUDA(cudaMemsetAsync(X.f.p, 0, X.count() * 4, ctx->stream));
+  DBuf<float> Yc;
+  Yc.alloc((size_t)me->total_cell_dofs * m);
+  const int was_prof = ctx->profiling;
+  ctx->profiling = 0;
+  cudaEvent_t e0, e1;
+  GBFE_CUDA(cudaEventCreate(&e0));
+  GBFE_CUDA(cudaEventCreate(&e1));
+  for (uint32_t mtiles = 1; mtiles <= 2; ++mtiles) {
+    uint32_t b0 = UINT32_MAX, b1 = 0;
+    for (uint32_t b = 0; b < me->bin_nd.size(); ++b)
+      if ((me->bin_nd[b] + 127) / 128 == mtiles) {
+        b0 = std::min(b0, b);
+        b1 = b + 1;
+      }
+    if (b0 == UINT32_MAX) continue;
+    const uint32_t cbeg = me->bin_begin[b0], ncell = me->bin_begin[b1] - cbeg;
+    const uint32_t nd_max = me->bin_nd[b1 - 1];
+    TcTune best;
+    best.ms = 1e30f;
+    for (uint32_t N : {16u, 32u, 64u, 128u, 256u}) {
+      if (N > std::max<uint32_t>(16, (m + 15) / 16 * 16) && N != 16) continue;
+      for (uint32_t st : {2u, 3u, 4u}) {
+        launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st);  // warm
+        GBFE_CUDA(cudaEventRecord(e0, ctx->stream));
+        for (int r = 0; r < 3; ++r) launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st);
+        GBFE_CUDA(cudaEventRecord(e1, ctx->stream));
+        GBFE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        GBFE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= 3.f;
+        if (ms < best.ms) {
+          best.ms = ms;
+          best.N = N;
+          best.stages = st;
+        }
+      }
+    }
+    ctx->tc_tune[std::make_tuple(nd_max, mtiles, m)] = best;
+    log.push_back("tc2 " + std::to_string(nd_max) + " " + std::to_string(mtiles) + " " + std::to_string(m) + " " +
+                  std::to_string(best.N) + " " + std::to_string(best.stages) + " " + std::to_string(best.ms));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->profiling = was_prof;
 }
 
 }  // namespace gbfe

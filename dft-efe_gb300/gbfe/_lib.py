@@ -56,6 +56,7 @@ SIGNATURES = {
     "gbfe_ctx_set_profiling": (i32, [p, i32]),
     "gbfe_ctx_set_fp64_apply": (i32, [p, i32]),
     "gbfe_ctx_set_graphs": (i32, [p, i32]),
+    "gbfe_autotune": (i32, [p, u32, C.c_char_p, C.c_size_t]),
     "gbfe_ctx_kernel_stats": (i32, [p, C.c_char_p, C.POINTER(u64), pf64, pf64, pf64]),
     "gbfe_ctx_reset_kernel_stats": (i32, [p]),
     "gbfe_probe_fp64_peak": (i32, [p, pf64]),

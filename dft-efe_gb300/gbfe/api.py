@@ -245,6 +245,13 @@ class CellMatrixOperatorContext(OperatorContext):
         self.mixed = mixed
 
 
+def autotune(op: "OperatorContext", m: int) -> list:
+    """Tune the tensor-core kernel's launch shape for `op` with m vectors."""
+    buf = C.create_string_buffer(4096)
+    check(op.ctx.lib.gbfe_autotune(op.h, int(m), buf, 4096), op.ctx.h, "autotune")
+    return [ln for ln in buf.value.decode().splitlines() if ln.strip()]
+
+
 def assemble_local(op: "OperatorContext", basis_values: np.ndarray, weights: np.ndarray,
                    fixed_mats: Optional[np.ndarray] = None, alpha: float = 1.0) -> None:
     """A_c = alpha F_c + B^T diag(w_c) B on the device (KohnShamOperatorContextFE::reinit)."""

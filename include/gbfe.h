@@ -76,6 +76,13 @@ int gbfe_ctx_check_status(gbfe_ctx *ctx);
  * SIMT kernel.  The environment variable GBFE_TENSOR_CORES=0|1 sets the
  * initial mode of a new context. */
 int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode);
+/* Autotuner of the persistent split-BF16 tensor-core kernel: times every
+ * (vector tile, pipeline stages) shape on `op` (built with GBFE_PREC_MIXED)
+ * with m vectors, per launch group of cell sizes, and keeps the fastest on the
+ * context.  `report` receives one line per group ("tc2 nd_max tiles m N
+ * stages ms").  With GBFE_AUTOTUNE_CACHE=<file> in the environment, new
+ * contexts load earlier lines from that file and tuning appends to it. */
+int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len);
 /* 1 (default): inside gbfe_ks_eigen_solve the d-1 steps of the Chebyshev
  * recurrence are captured once into a CUDA graph (second pass) and replayed
  * on every later pass; 0: launched one by one. */

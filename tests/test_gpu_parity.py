@@ -391,3 +391,43 @@ def test_graph_replayed_filter_matches_eager(gpu_ctx, small_problem):
         gpu_ctx.set_graphs(True)
         assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
         assert out[0][2] == out[1][2]  # replays count the kernels they contain
+
+
+def test_autotuned_tensor_core_shape(gpu_ctx, tmp_path, monkeypatch):
+    """The autotuner picks a (vector tile, stages) shape per cell-size group;
+    every shape gives the split-BF16 result (TC_TOL against FP64), and the
+    chosen shapes are written to and read back from the cache file."""
+    from gbfe import api
+
+    prob = M.ks_box(4, 4, 8.0, 1, 4.0, 0.5, seed=44)
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("GBFE_AUTOTUNE_CACHE", str(cache))
+    ctx = api.LinAlgOpContext(0)
+    try:
+        basis = api.FEBasisManager.from_problem(ctx, prob)
+        H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=True)
+        X0 = M.random_block(prob.n_dofs, 40, 5)
+        X = api.MultiVector(basis, 40, init=X0)
+        Y = api.MultiVector(basis, 40)
+        H.apply(X, Y)
+        Xf = api.MultiVector(basis, 40, dtype=np.float32, init=X0.astype(np.float32))
+        Yf = api.MultiVector(basis, 40, dtype=np.float32)
+        lines = api.autotune(H, 40)
+        assert lines and all(ln.split()[0] == "tc2" and len(ln.split()) == 7 for ln in lines)
+        H.apply(Xf, Yf)
+        ctx.check_status()
+        assert rel_maxnorm(Yf.numpy(), Y.numpy()) <= TC_TOL
+        assert cache.read_text().strip().splitlines() == lines
+    finally:
+        ctx.close()
+    ctx2 = api.LinAlgOpContext(0)  # loads the cache
+    try:
+        basis = api.FEBasisManager.from_problem(ctx2, prob)
+        H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=True)
+        Xf = api.MultiVector(basis, 40, dtype=np.float32, init=X0.astype(np.float32))
+        Yf2 = api.MultiVector(basis, 40, dtype=np.float32)
+        H.apply(Xf, Yf2)
+        ctx2.check_status()
+        assert np.array_equal(Yf2.numpy(), Yf.numpy())
+    finally:
+        ctx2.close()
