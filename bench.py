@@ -147,27 +147,27 @@ class ClockSampler:
 
 # ----------------------------------------------------------------------------- CPU side
 def _cpu_worker(args):
-    """One oracle process: a bounded sample of FP64 ChFSI passes on the workload."""
-    cfg_name, passes, m_override = args
-    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    """One oracle process: a bounded sample of FP64 ChFSI passes on the
+    workload whose arrays the parent wrote to `path`."""
+    path, passes = args
     sys.path.insert(0, str(ROOT / "dft-efe_gb300"))
     sys.path.insert(0, str(ROOT))
     import gbfe.mesh as M
     from oracle import oracle as O
 
-    cfg = dict(CONFIGS[cfg_name])
-    if m_override:
-        cfg["m"] = m_override
-    prob = make_problem(cfg)
-    s = O.OracleSystem.from_problem(prob)
-    H, Mo = s.cell_op(prob.H), s.cell_op(prob.M)
-    if "enr_block_inv" in prob.extra:
-        Mi = s.diag_block_op(1.0 / prob.m_gll_diag, prob.extra["enr_begin"], prob.extra["enr_block_inv"])
+    z = np.load(path)
+    cons = M.Constraints(row_ids=z["c_rows"], row_sizes=z["c_sizes"], col_ids=z["c_cols"], row_acc=z["c_acc"],
+                         col_values=z["c_vals"], inhomogeneities=z["c_inh"])
+    s = O.OracleSystem(z["nd"], z["ids"], int(z["n_dofs"]), cons)
+    H, Mo = s.cell_op(z["H"]), s.cell_op(z["M"])
+    if "blk" in z.files:
+        Mi = s.diag_block_op(1.0 / z["mdiag"], int(z["blk_begin"]), z["blk"])
     else:
-        Mi = s.diag_op(1.0 / prob.m_gll_diag)
-    (wl, wu, uu), deg = lanczos_setup(prob, cfg, lambda: s.lanczos_bounds(H, Mo, Mi, 20, 7))
-    X = M.random_block(prob.n_dofs, cfg["m"], cfg["seed"] + 1)
-    eig = np.zeros(cfg["m"])
+        Mi = s.diag_op(1.0 / z["mdiag"])
+    wl, wu, uu = (float(v) for v in z["bounds"])
+    deg = int(z["deg"])
+    X = np.ascontiguousarray(z["X0"])
+    eig = np.zeros(X.shape[1])
     t0 = time.perf_counter()
     for _ in range(passes):
         eig, X = s.chfsi_pass(H, Mo, Mi, X, eig, deg, wl, wu, uu)
@@ -176,21 +176,64 @@ def _cpu_worker(args):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(cfg_name: str, passes_per_solve: float, procs: int, sample_passes: int = 1):
-    """Time `sample_passes` FP64 ChFSI passes in `procs` concurrent oracle
-    processes; solves/s = procs / (time per pass * passes per solve)."""
-    import multiprocessing as mp
+# passes timed per oracle process: about 5-15 s of single-core work
+SAMPLE_PASSES = {"cfg1": 20, "cfg2": 1, "cfg2c": 1, "cfg3": 1}
 
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(procs) as pool:
+
+class CpuBaseline:
+    """FP64 ChFSI passes of the oracle in `procs` single-threaded processes on
+    the host cores.  The workload arrays are generated once, written to a
+    scratch file and read by every worker (spawned, so no GPU state is
+    inherited); BLAS threading is pinned to one thread per process."""
+
+    def __init__(self, prob, cfg, bounds, deg, procs):
+        import multiprocessing as mp
+        import tempfile
+
+        self.procs = procs
+        self.tmp = tempfile.TemporaryDirectory(prefix="gbfe_cpu_")
+        self.path = os.path.join(self.tmp.name, "workload.npz")
+        c = prob.constraints
+        arrays = dict(nd=prob.nd_per_cell, ids=prob.cell_dof_ids, n_dofs=prob.n_dofs, H=prob.H, M=prob.M,
+                      mdiag=prob.m_gll_diag, c_rows=c.row_ids, c_sizes=c.row_sizes, c_cols=c.col_ids,
+                      c_acc=c.row_acc, c_vals=c.col_values, c_inh=c.inhomogeneities,
+                      bounds=np.array(bounds, dtype=np.float64), deg=deg,
+                      X0=random_block_for(prob, cfg))
+        if "enr_block_inv" in prob.extra:
+            arrays.update(blk=prob.extra["enr_block_inv"], blk_begin=prob.extra["enr_begin"])
+        np.savez(self.path, **arrays)
+        saved = {k: os.environ.get(k) for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
+        os.environ.update(OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+        try:
+            self.pool = mp.get_context("spawn").Pool(procs)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+
+    def measure(self, passes_per_solve: float, sample_passes: int = 1) -> dict:
         t0 = time.perf_counter()
-        times = pool.map(_cpu_worker, [(cfg_name, sample_passes, None)] * procs)
+        times = self.pool.map(_cpu_worker, [(self.path, sample_passes)] * self.procs)
         wall = time.perf_counter() - t0
-    per_pass = max(times) / sample_passes
-    return {"value": procs / (per_pass * passes_per_solve), "unit": "solves/s", "cores": procs, "kind": "port",
-            "sample": f"{sample_passes} FP64 ChFSI pass(es) + residual check of {cfg_name} in each of {procs} "
-                      f"single-threaded oracle processes ({per_pass:.2f} s/pass), extrapolated to "
-                      f"{passes_per_solve:g} passes per solve; wall {wall:.1f} s"}
+        per_pass = max(times) / sample_passes
+        return {"value": self.procs / (per_pass * passes_per_solve), "unit": "solves/s", "cores": self.procs,
+                "kind": "port",
+                "sample": f"{sample_passes} FP64 ChFSI pass(es) + residual check in each of {self.procs} "
+                          f"single-threaded oracle processes ({per_pass:.2f} s/pass), extrapolated to "
+                          f"{passes_per_solve:g} passes per solve; wall {wall:.1f} s"}
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+        self.tmp.cleanup()
+
+
+def random_block_for(prob, cfg):
+    import gbfe.mesh as M
+
+    return M.random_block(prob.n_dofs, cfg["m"], cfg["seed"] + 1)
 
 
 # ----------------------------------------------------------------------------- GPU side
@@ -211,7 +254,7 @@ def run_gpu(args, cfg_name, rank, world):
         Mi = api.CFEOverlapInverseOpContextGLL(basis, prob.m_gll_diag)
     m, nw = cfg["m"], cfg["n_wanted"]
     (wl, wu, uu), deg = lanczos_setup(prob, cfg, lambda: api.lanczos_bounds(H, Mo, Mi, 20, 7))
-    X0 = M.random_block(prob.n_dofs, m, cfg["seed"] + 1)
+    X0 = random_block_for(prob, cfg)
     X0dev = api.MultiVector(basis, m, init=X0)
     X = api.MultiVector(basis, m)
 
@@ -568,13 +611,26 @@ def main():
         # passes per solve: the pass count the FP64 solve of the same inputs
         # needs (measured on the GPU path, which matches the oracle pass for
         # pass), so that the CPU arm is timed on a bounded sample of passes.
-        passes = {"cfg1": 20, "cfg2": 24, "cfg2c": 24, "cfg3": 24}[args.config]
+        passes = {"cfg1": 20, "cfg2": 21, "cfg2c": 24, "cfg3": 24}[args.config]
+        sys.path.insert(0, str(ROOT))
+        from oracle import oracle as O
+
+        prob = make_problem(cfg)
+        s0 = O.OracleSystem.from_problem(prob)
+        H0, M0 = s0.cell_op(prob.H), s0.cell_op(prob.M)
+        if "enr_block_inv" in prob.extra:
+            Mi0 = s0.diag_block_op(1.0 / prob.m_gll_diag, prob.extra["enr_begin"], prob.extra["enr_block_inv"])
+        else:
+            Mi0 = s0.diag_op(1.0 / prob.m_gll_diag)
+        bounds, deg = lanczos_setup(prob, cfg, lambda: s0.lanczos_bounds(H0, M0, Mi0, 20, 7))
+        cpu = CpuBaseline(prob, cfg, bounds, deg, procs)
         vals = []
         for _ in range(args.warmup):
             pass
         for _ in range(max(1, args.steps)):
-            b = cpu_baseline(args.config, passes, procs)
+            b = cpu.measure(passes, sample_passes=SAMPLE_PASSES.get(args.config, 1))
             vals.append(b["value"])
+        cpu.close()
         v = float(np.median(vals))
         b["value"] = v
         print(json.dumps({"impl": "reference", "metric": metric, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
@@ -637,7 +693,9 @@ def main():
         "gpu_launches": r["launches"],
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.config, r["passes64"], procs)
+        cpu = CpuBaseline(prob, r["cfg"], r["bounds"], r["deg"], procs)
+        line["cpu_baseline"] = cpu.measure(r["passes64"], sample_passes=SAMPLE_PASSES.get(args.config, 1))
+        cpu.close()
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -336,29 +336,38 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
     return;
   }
   op->cellbuf.ensure((size_t)me->total_cell_dofs * m);
+  if (op->nl) nonlocal_project(op->nl, X);
   if (ctx->fp64_tc && op->oz_aoff.p)
     cell_apply_oz(op, X, op->cellbuf.p);
   else
     cell_apply_f64(op, X, op->cellbuf.p);
-  const uint8_t *isr = c ? c->is_row.p : nullptr;
-  k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
-      op->cellbuf.p, m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr, has_par ? c->par_ptr.p : nullptr,
-      has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->d.p);
-  check_launch(ctx, "assemble_f64");
+  if (op->nl) nonlocal_add(op->nl, m, GBFE_F64, op->cellbuf.p);
+  assemble_cells(me, c, GBFE_F64, op->cellbuf.p, Y);
 }
 
-// assembly entry used by the mixed path (FP32 cell buffer -> FP32 Y)
-void assemble_f32(const gbfe_op *op, const float *Yc, gbfe_mv *Y) {
-  gbfe_mesh *me = op->mesh;
+void assemble_cells(gbfe_mesh *me, const gbfe_cons *c, int dtype, const void *Yc, gbfe_mv *Y) {
   gbfe_ctx *ctx = me->ctx;
-  const gbfe_cons *c = op->cons;
   const bool has_par = c && !c->pure_dirichlet;
   const uint64_t n = (uint64_t)me->n_dofs * Y->m;
   const uint8_t *isr = c ? c->is_row.p : nullptr;
-  k_assemble<float, float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
-      Yc, Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr, has_par ? c->par_ptr.p : nullptr,
-      has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->f.p);
-  check_launch(ctx, "assemble_f32");
+  if (dtype == GBFE_F64) {
+    k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+        static_cast<const double *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
+        has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->d.p);
+    check_launch(ctx, "assemble_f64");
+  } else {
+    k_assemble<float, float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+        static_cast<const float *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
+        has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->f.p);
+    check_launch(ctx, "assemble_f32");
+  }
+}
+
+// assembly entry used by the mixed path (FP32 cell buffer -> FP32 Y), with
+// the fused nonlocal block added first
+void assemble_f32(const gbfe_op *op, float *Yc, gbfe_mv *Y) {
+  if (op->nl) nonlocal_add(op->nl, Y->m, GBFE_F32, Yc);
+  assemble_cells(op->mesh, op->cons, GBFE_F32, Yc, Y);
 }
 
 void convert_mv(gbfe_ctx *ctx, const gbfe_mv *src, gbfe_mv *dst) {

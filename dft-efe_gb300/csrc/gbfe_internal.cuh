@@ -192,9 +192,31 @@ struct gbfe_cons {
 
 enum OpKind { OP_CELL = 0, OP_DIAG = 1, OP_JACOBI = 2, OP_DIAG_BLOCK = 3 };
 
+// Separable nonlocal part C^T V C (AtomCenterNonLocalOpContextFE): per cell
+// c with np_c projectors the matrix C_c (np_c x nd_c, column-major, projector
+// index fastest), a projector id per (cell, projector) slot, and a diagonal
+// coupling V per projector.  Only cells with np_c > 0 are stored.
+struct gbfe_nl {
+  gbfe_mesh *mesh = nullptr;
+  uint32_t n_proj = 0, n_cells_nl = 0, np_max = 0, n_slots = 0;
+  gbfe::DBuf<uint32_t> cells;      // [n_cells_nl] cell index
+  gbfe::DBuf<uint32_t> slot_off;   // [n_cells_nl + 1] first slot of each cell
+  gbfe::DBuf<uint64_t> c_off;      // [n_cells_nl] offset of C_c in cmat
+  gbfe::DBuf<uint32_t> pids;       // [n_slots] projector of each slot
+  gbfe::DBuf<uint32_t> pslot_ptr;  // [n_proj + 1] slots of each projector, ascending
+  gbfe::DBuf<uint32_t> pslot;      // [n_slots]
+  gbfe::DBuf<double> cmat, v;
+  gbfe::DBuf<float> cmat_f32, v_f32;
+  mutable gbfe::DBuf<double> cx, w;  // [n_slots][m], [n_proj][m]
+  mutable gbfe::DBuf<float> cx_f32, w_f32;
+  mutable gbfe::DBuf<double> ycell;  // cell-wise result of the standalone apply
+  mutable gbfe::DBuf<float> ycell_f32;
+};
+
 struct gbfe_op {
   gbfe_mesh *mesh = nullptr;
   const gbfe_cons *cons = nullptr;
+  const gbfe_nl *nl = nullptr;  // fused nonlocal part (cell operators)
   int kind = OP_CELL;
   int prec = GBFE_PREC_FP64;
   gbfe::DBuf<double> mats;            // f64 col-major per cell (or per distinct matrix)
@@ -287,6 +309,11 @@ void build_mixed_mats(gbfe_op *op);
 void build_tc_mats(gbfe_op *op);
 bool tc_supported(const gbfe_mesh *me);
 void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc);
+// nonlocal part: W = V * (sum over slots of C_c X_c) and Yc += C_c^T W
+// Y = assembled cell-wise buffer Yc with the constraint epilogue of `cons`
+void assemble_cells(gbfe_mesh *me, const gbfe_cons *cons, int dtype, const void *Yc, gbfe_mv *Y);
+void nonlocal_project(const gbfe_nl *nl, const gbfe_mv *X);
+void nonlocal_add(const gbfe_nl *nl, uint32_t m, int dtype, void *Yc);
 void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log);
 bool oz_supported(const gbfe_mesh *me);
 void build_oz_mats(gbfe_op *op);

@@ -15,7 +15,7 @@
 using namespace gbfe;
 
 namespace gbfe {
-void assemble_f32(const gbfe_op *op, const float *Yc, gbfe_mv *Y);
+void assemble_f32(const gbfe_op *op, float *Yc, gbfe_mv *Y);
 void convert_mv(gbfe_ctx *ctx, const gbfe_mv *src, gbfe_mv *dst);
 void fill_mv(gbfe_ctx *ctx, gbfe_mv *x, double v);
 }  // namespace gbfe

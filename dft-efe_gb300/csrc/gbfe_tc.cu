@@ -32,7 +32,7 @@
 using namespace gbfe;
 
 namespace gbfe {
-void assemble_f32(const gbfe_op *op, const float *Yc, gbfe_mv *Y);
+void assemble_f32(const gbfe_op *op, float *Yc, gbfe_mv *Y);
 }
 
 namespace {

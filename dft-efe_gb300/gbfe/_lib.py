@@ -57,6 +57,10 @@ SIGNATURES = {
     "gbfe_ctx_set_fp64_apply": (i32, [p, i32]),
     "gbfe_ctx_set_graphs": (i32, [p, i32]),
     "gbfe_autotune": (i32, [p, u32, C.c_char_p, C.c_size_t]),
+    "gbfe_nonlocal_upload": (i32, [p, u32, p, p, p, p, C.POINTER(p)]),
+    "gbfe_nonlocal_destroy": (i32, [p]),
+    "gbfe_nonlocal_apply": (i32, [p, p, p, p]),
+    "gbfe_op_attach_nonlocal": (i32, [p, p]),
     "gbfe_ctx_kernel_stats": (i32, [p, C.c_char_p, C.POINTER(u64), pf64, pf64, pf64]),
     "gbfe_ctx_reset_kernel_stats": (i32, [p]),
     "gbfe_probe_fp64_peak": (i32, [p, pf64]),

@@ -233,7 +233,8 @@ class OperatorContext:
 
 class CellMatrixOperatorContext(OperatorContext):
     def __init__(self, basis: FEBasisManager, cell_matrices: np.ndarray, mixed: bool = False,
-                 use_constraints: bool = True, fp64_tensor: bool = False):
+                 use_constraints: bool = True, fp64_tensor: bool = False,
+                 nonlocal_part: Optional["AtomCenterNonLocalOpContextFE"] = None):
         self.basis, self.ctx = basis, basis.ctx
         mats = np.ascontiguousarray(cell_matrices, dtype=np.float64)
         h = C.c_void_p()
@@ -243,6 +244,43 @@ class CellMatrixOperatorContext(OperatorContext):
               "cellmat_upload")
         self.h = h
         self.mixed = mixed
+        self.nonlocal_part = None
+        if nonlocal_part is not None:
+            self.attach_nonlocal(nonlocal_part)
+
+    def attach_nonlocal(self, nl: Optional["AtomCenterNonLocalOpContextFE"]) -> None:
+        """Fuse C^T V C into this operator's apply (None detaches)."""
+        check(self.ctx.lib.gbfe_op_attach_nonlocal(self.h, nl.h if nl is not None else None), self.ctx.h,
+              "attach_nonlocal")
+        self.nonlocal_part = nl  # keeps the projector data alive while attached
+
+
+class AtomCenterNonLocalOpContextFE(OperatorContext):
+    """Separable nonlocal pseudopotential part, Y = sum_atoms C^T V C X
+    (basis/AtomCenterNonLocalOpContextFE.h); `data` carries the per-cell
+    projector blocks (gbfe.nonlocal_psp.NonLocalData)."""
+
+    def __init__(self, basis: FEBasisManager, data, use_constraints: bool = True):
+        self.basis, self.ctx = basis, basis.ctx
+        self._keep = [np.ascontiguousarray(data.proj_per_cell, dtype=np.uint32),
+                      np.ascontiguousarray(data.proj_ids, dtype=np.uint32),
+                      np.ascontiguousarray(data.cell_c, dtype=np.float64),
+                      np.ascontiguousarray(data.coupling, dtype=np.float64)]
+        ppc, pid, cc, v = self._keep
+        h = C.c_void_p()
+        check(self.ctx.lib.gbfe_nonlocal_upload(basis.h, int(data.n_proj), _ptr(ppc), _ptr(pid), _ptr(cc), _ptr(v),
+                                                C.byref(h)), self.ctx.h, "nonlocal_upload")
+        self.h = h
+        self._keep = None
+        self.cons_h = basis.cons_h if use_constraints else None
+
+    def apply(self, X: MultiVector, Y: MultiVector, updateGhostX: bool = False, updateGhostY: bool = False) -> None:
+        check(self.ctx.lib.gbfe_nonlocal_apply(self.h, self.cons_h, X.h, Y.h), self.ctx.h, "nonlocal_apply")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.ctx.lib.gbfe_nonlocal_destroy(self.h)
+            self.h = None
 
 
 def autotune(op: "OperatorContext", m: int) -> list:

@@ -58,6 +58,7 @@ typedef struct gbfe_mesh gbfe_mesh;
 typedef struct gbfe_cons gbfe_cons;
 typedef struct gbfe_op gbfe_op;
 typedef struct gbfe_mv gbfe_mv;
+typedef struct gbfe_nl gbfe_nl;
 
 /* ---- lifecycle ------------------------------------------------------------
  * Replaces the LinAlgOpContext<DEVICE> / BlasQueue / LapackQueue bundle
@@ -76,6 +77,32 @@ int gbfe_ctx_check_status(gbfe_ctx *ctx);
  * SIMT kernel.  The environment variable GBFE_TENSOR_CORES=0|1 sets the
  * initial mode of a new context. */
 int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode);
+/* ---- nonlocal pseudopotential part ---------------------------------------
+ * Replaces basis::AtomCenterNonLocalOpContextFE
+ * (basis/AtomCenterNonLocalOpContextFE.h:47-179): Y = sum_atoms C^T V C X.
+ * The arrays are what its constructor computes from the atom data
+ * (AtomCenterNonLocalOpContextFE.t.cpp:410-632):
+ *   n_proj              projectors on this mesh (d_CX rows)
+ *   proj_per_cell[C]    d_numProjsInCells
+ *   proj_ids[sum np_c]  d_locallyOwnedCellLocalProjectorIds (projector of each
+ *                       (cell, local projector) slot, cell-major)
+ *   cell_c[sum np_c*nd_c] d_cellWiseC: per cell np_c x nd_c, column-major
+ *                       (projector index fastest), cells concatenated
+ *   coupling[n_proj]    d_V, the diagonal coupling constant of each projector
+ * Cells with np_c = 0 take no work. */
+int gbfe_nonlocal_upload(gbfe_mesh *mesh, uint32_t n_proj, const uint32_t *proj_per_cell, const uint32_t *proj_ids,
+                         const double *cell_c, const double *coupling, gbfe_nl **out);
+int gbfe_nonlocal_destroy(gbfe_nl *nl);
+/* Standalone AtomCenterNonLocalOpContextFE::apply (.t.cpp:715-849): X gets the
+ * parent-to-child constraints, Y = assembled C^T V C X with child-to-parent. */
+int gbfe_nonlocal_apply(const gbfe_nl *nl, const gbfe_cons *cons, gbfe_mv *X, gbfe_mv *Y);
+/* Fuse the nonlocal part into a cell operator's apply (FP64 and FP32 paths):
+ * the Kohn-Sham apply with an ONCV component
+ * (ksdft/KohnShamOperatorContextFE.t.cpp:1022-1080, 1177-1180) adds C_c^T W
+ * into each cell's block before the scatter.  nl = NULL detaches; the
+ * operator keeps a pointer, so nl must outlive it or be detached first. */
+int gbfe_op_attach_nonlocal(gbfe_op *op, const gbfe_nl *nl);
+
 /* Autotuner of the persistent split-BF16 tensor-core kernel: times every
  * (vector tile, pipeline stages) shape on `op` (built with GBFE_PREC_MIXED)
  * with m vectors, per launch group of cell sizes, and keeps the fastest on the

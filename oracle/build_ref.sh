@@ -21,6 +21,23 @@ BLASLIB="$(ls "$BLASDIR"/libscipy_openblas*.so | head -1)"
 
 sed '334s/;$//' "$SRC/utils/MPIWrapper.cpp" > "$OUT/patched/MPIWrapper.cpp"
 
+# The apply-side member functions of basis::AtomCenterNonLocalOpContextFE
+# (apply .. applyCOnVCconjtransX) and its AtomCenterNonLocalOpContextFEInternal
+# cell-wise GEMM helpers, cut from the reference's .t.cpp.  Its constructor
+# needs UPF data and deal.II quadrature and is left out: the harness
+# declaration ref_harness/shadow/basis/AtomCenterNonLocalOpContextFE.h takes
+# the arrays that constructor would compute.
+NLSRC="$SRC/basis/AtomCenterNonLocalOpContextFE.t.cpp"
+NLOUT="$OUT/patched/AtomCenterNonLocalOpContextFE.members.t.cpp"
+if sed -n '265p' "$NLSRC" | grep -q 'namespace AtomCenterNonLocalOpContextFEInternal' &&
+   sed -n '724p' "$NLSRC" | grep -q '::apply(' && sed -n '1048p' "$NLSRC" | grep -q 'namespace dftefe'; then
+  { sed -n '1,265p' "$NLSRC"; sed -n '714,1048p' "$NLSRC"; } > "$NLOUT.tmp"
+  if ! cmp -s "$NLOUT.tmp" "$NLOUT"; then mv "$NLOUT.tmp" "$NLOUT"; else rm -f "$NLOUT.tmp"; fi
+else
+  echo "AtomCenterNonLocalOpContextFE.t.cpp layout differs from the expected one; nonlocal case left out" >&2
+  rm -f "$NLOUT"
+fi
+
 CXXFLAGS="-std=c++17 -O2 -DNDEBUG -w -I$HERE/ref_harness/shadow -I$SRC"
 SOURCES=(
   utils/Exceptions.cpp utils/MemoryTransfer.cpp utils/MPITypes.cpp utils/MPIRequestersNBX.cpp
@@ -43,8 +60,13 @@ done
 o="$OUT/obj/MPIWrapper.o"; OBJS+=("$o")
 [ -f "$o" ] || { g++ $CXXFLAGS -I"$SRC/utils" -c "$OUT/patched/MPIWrapper.cpp" -o "$o" & pids+=($!); }
 o="$OUT/obj/ref_driver.o"; OBJS+=("$o")
-if [ ! -f "$o" ] || [ "$HERE/ref_harness/ref_driver.cpp" -nt "$o" ]; then
-  g++ $CXXFLAGS -c "$HERE/ref_harness/ref_driver.cpp" -o "$o" & pids+=($!)
+stale=0
+[ -f "$o" ] || stale=1
+for dep in "$HERE/ref_harness/ref_driver.cpp" $(find "$HERE/ref_harness/shadow" -name '*.h') "$OUT/patched/"*.t.cpp; do
+  [ -e "$dep" ] && [ "$dep" -nt "$o" ] && stale=1
+done
+if [ "$stale" = 1 ]; then
+  g++ $CXXFLAGS -I"$OUT/patched" -c "$HERE/ref_harness/ref_driver.cpp" -o "$o" & pids+=($!)
 fi
 for p in "${pids[@]}"; do wait "$p"; done
 

@@ -19,6 +19,16 @@
  *                and the scatter of FECellWiseDataOperations.t.cpp:87-151;
  *                the same structure is CFEOverlapOperatorContext.t.cpp:587-640
  *                and LaplaceOperatorContextFE.t.cpp:397-467.
+ *   orc_apply with a nonlocal part (orc_nl)
+ *                the fused Kohn-Sham apply with an ONCV component,
+ *                ksdft/KohnShamOperatorContextFE.t.cpp:1022-1080, :1177-1180:
+ *                CX = sum_c scatter(Xc * C_c^T) (gemm 'N','C', beta 0), CX *= V,
+ *                then per cell Yc = Xc * H_c and Yc += CXc * C_c (gemm
+ *                'N','N', beta 1) before the scatter -- the member functions
+ *                of basis/AtomCenterNonLocalOpContextFE.t.cpp:883-1045 and
+ *                the cellWiseGEMM of :43-152.  Without cell matrices (mats =
+ *                NULL) it is the standalone AtomCenterNonLocalOpContextFE::apply
+ *                (:715-849).
  *   orc_apply (diagonal kind)
  *                basis/CFEOverlapInverseOpContextGLL.t.cpp:528-559
  *                (p2c, Y = d o X, c2p) and, without constraints,
@@ -62,6 +72,16 @@ typedef struct {
 } orc_cons;
 
 typedef struct {
+  uint32_t n_proj;
+  const uint32_t *np;     /* [n_cells] projectors per cell */
+  const uint32_t *pids;   /* [sum np] projector of each (cell, projector) slot */
+  const uint64_t *p_off;  /* [n_cells+1] prefix sum of np */
+  const uint64_t *c_off;  /* [n_cells+1] prefix sum of np * nd */
+  const double *cmat;     /* per cell np x nd column-major (projector fastest) */
+  const double *v;        /* [n_proj] diagonal coupling */
+} orc_nl;
+
+typedef struct {
   int kind; /* 0: cell matrices, 1: diagonal with constraints, 2: diagonal without,
                3: diagonal + dense block on [blk_begin, blk_begin + blk_n) with constraints */
   const orc_mesh *mesh;
@@ -71,6 +91,7 @@ typedef struct {
   uint64_t blk_begin;
   uint64_t blk_n;
   const double *blk; /* kind 3: column-major blk_n x blk_n */
+  const orc_nl *nl;  /* kind 0: nonlocal part (NULL: none) */
 } orc_op;
 
 static orc_dgemm_fn g_dgemm = 0;
@@ -126,6 +147,26 @@ static void cell_gemm(int m, int nd, const double *Xc, const double *Hc, double 
   }
 }
 
+/* C(m x n) = A(m x k, ld m) * op(B) + beta C; op(B) = B (k x n, ld k) or
+   B^T with B stored n x k (ld n) -- the two products of the nonlocal part */
+static void small_gemm(int transb, int m, int n, int k, const double *A, const double *B, double beta, double *Cm) {
+  if (g_dgemm) {
+    const double one = 1.0;
+    const int ldb = transb ? n : k;
+    g_dgemm("N", transb ? "T" : "N", &m, &n, &k, &one, A, &m, B, &ldb, &beta, Cm, &m);
+    return;
+  }
+  for (int j = 0; j < n; ++j) {
+    double *cj = Cm + (size_t)j * m;
+    for (int v = 0; v < m; ++v) cj[v] = beta == 0.0 ? 0.0 : beta * cj[v];
+    for (int q = 0; q < k; ++q) {
+      const double b = transb ? B[j + (size_t)n * q] : B[q + (size_t)k * j];
+      const double *aq = A + (size_t)q * m;
+      for (int v = 0; v < m; ++v) cj[v] += aq[v] * b;
+    }
+  }
+}
+
 static uint32_t max_nd(const orc_mesh *me) {
   uint32_t mx = 0;
   for (uint32_t c = 0; c < me->n_cells; ++c)
@@ -144,11 +185,43 @@ int orc_apply(const orc_op *op, double *X, double *Y, uint32_t m) {
     double *Xc = (double *)malloc(sizeof(double) * (size_t)ndm * m);
     double *Yc = (double *)malloc(sizeof(double) * (size_t)ndm * m);
     if (!Xc || !Yc) { free(Xc); free(Yc); return 3; }
+    const orc_nl *nl = op->nl;
+    double *CX = 0, *CXc = 0;
+    if (nl) {
+      uint32_t npm = 1;
+      for (uint32_t c = 0; c < me->n_cells; ++c)
+        if (nl->np[c] > npm) npm = nl->np[c];
+      CX = (double *)calloc((size_t)nl->n_proj * m + 1, sizeof(double));
+      CXc = (double *)malloc(sizeof(double) * (size_t)npm * m);
+      if (!CX || !CXc) { free(Xc); free(Yc); free(CX); free(CXc); return 3; }
+      /* CX = sum over cells of Xc * C_c^T, scattered in cell order */
+      for (uint32_t c = 0; c < me->n_cells; ++c) {
+        const uint32_t nd = me->nd[c], np = nl->np[c];
+        if (!np) continue;
+        const uint32_t *ids = me->ids + me->cell_off[c];
+        for (uint32_t i = 0; i < nd; ++i) memcpy(Xc + (size_t)i * m, X + (uint64_t)ids[i] * m, sizeof(double) * m);
+        small_gemm(1, (int)m, (int)np, (int)nd, Xc, nl->cmat + nl->c_off[c], 0.0, CXc);
+        const uint32_t *pid = nl->pids + nl->p_off[c];
+        for (uint32_t b = 0; b < np; ++b)
+          for (uint32_t v = 0; v < m; ++v) CX[(uint64_t)pid[b] * m + v] += CXc[(size_t)b * m + v];
+      }
+      for (uint32_t p = 0; p < nl->n_proj; ++p)
+        for (uint32_t v = 0; v < m; ++v) CX[(uint64_t)p * m + v] = nl->v[p] * CX[(uint64_t)p * m + v];
+    }
     for (uint32_t c = 0; c < me->n_cells; ++c) {
       const uint32_t nd = me->nd[c];
       const uint32_t *ids = me->ids + me->cell_off[c];
       for (uint32_t i = 0; i < nd; ++i) memcpy(Xc + (size_t)i * m, X + (uint64_t)ids[i] * m, sizeof(double) * m);
-      cell_gemm((int)m, (int)nd, Xc, op->mats + me->mat_off[c], Yc);
+      if (op->mats)
+        cell_gemm((int)m, (int)nd, Xc, op->mats + me->mat_off[c], Yc);
+      else
+        memset(Yc, 0, sizeof(double) * (size_t)nd * m);
+      if (nl && nl->np[c]) {
+        const uint32_t np = nl->np[c];
+        const uint32_t *pid = nl->pids + nl->p_off[c];
+        for (uint32_t b = 0; b < np; ++b) memcpy(CXc + (size_t)b * m, CX + (uint64_t)pid[b] * m, sizeof(double) * m);
+        small_gemm(0, (int)m, (int)nd, (int)np, CXc, nl->cmat + nl->c_off[c], 1.0, Yc);
+      }
       for (uint32_t i = 0; i < nd; ++i) {
         double *y = Y + (uint64_t)ids[i] * m;
         const double *yc = Yc + (size_t)i * m;
@@ -157,6 +230,8 @@ int orc_apply(const orc_op *op, double *X, double *Y, uint32_t m) {
     }
     free(Xc);
     free(Yc);
+    free(CX);
+    free(CXc);
     if (op->cons) orc_c2p(op->cons, Y, m);
     return 0;
   }

@@ -54,7 +54,13 @@ class _Cons(C.Structure):
 
 class _Op(C.Structure):
     _fields_ = [("kind", C.c_int), ("mesh", C.c_void_p), ("cons", C.c_void_p), ("mats", C.c_void_p),
-                ("diag", C.c_void_p), ("blk_begin", C.c_uint64), ("blk_n", C.c_uint64), ("blk", C.c_void_p)]
+                ("diag", C.c_void_p), ("blk_begin", C.c_uint64), ("blk_n", C.c_uint64), ("blk", C.c_void_p),
+                ("nl", C.c_void_p)]
+
+
+class _NonLocal(C.Structure):
+    _fields_ = [("n_proj", C.c_uint32), ("np", C.c_void_p), ("pids", C.c_void_p), ("p_off", C.c_void_p),
+                ("c_off", C.c_void_p), ("cmat", C.c_void_p), ("v", C.c_void_p)]
 
 
 _lib = None
@@ -134,8 +140,36 @@ class OracleSystem:
         self.keep.append(op)
         return op
 
-    def cell_op(self, mats, use_cons=True):
-        return self._op(0, mats=mats, use_cons=use_cons)
+    def cell_op(self, mats, use_cons=True, nonlocal_part=None):
+        op = self._op(0, mats=mats, use_cons=use_cons)
+        if nonlocal_part is not None:
+            op.nl = C.addressof(nonlocal_part)
+        return op
+
+    def nonlocal_part(self, data):
+        """Projector data (gbfe.nonlocal_psp.NonLocalData) as an oracle structure."""
+        nd = self.keep[0].astype(np.uint64)
+        npc = np.ascontiguousarray(data.proj_per_cell, dtype=np.uint32)
+        poff = np.zeros(npc.size + 1, np.uint64)
+        np.cumsum(npc.astype(np.uint64), out=poff[1:])
+        coff = np.zeros(npc.size + 1, np.uint64)
+        np.cumsum(npc.astype(np.uint64) * nd, out=coff[1:])
+        pids = np.ascontiguousarray(data.proj_ids, dtype=np.uint32)
+        cm = np.ascontiguousarray(data.cell_c, dtype=np.float64)
+        v = np.ascontiguousarray(data.coupling, dtype=np.float64)
+        self.keep += [npc, poff, coff, pids, cm, v]
+        nl = _NonLocal(int(data.n_proj), _p(npc).value, _p(pids).value, _p(poff).value, _p(coff).value,
+                       _p(cm).value, _p(v).value)
+        self.keep.append(nl)
+        return nl
+
+    def nonlocal_op(self, nonlocal_part, use_cons=True):
+        """AtomCenterNonLocalOpContextFE::apply alone (no cell matrices)."""
+        op = _Op(0, C.addressof(self.mesh), C.addressof(self.cons) if (self.cons is not None and use_cons) else None,
+                 None, None)
+        op.nl = C.addressof(nonlocal_part)
+        self.keep.append(op)
+        return op
 
     def diag_op(self, diag, use_cons=True):
         return self._op(1, diag=diag, use_cons=use_cons)

@@ -11,6 +11,10 @@
 //   linearAlgebra::ChebyshevFilter (ChebyshevFilter.t.cpp:39-135)
 //   linearAlgebra::CGLinearSolver::solve (CGLinearSolver.t.cpp:68-313)
 //   linearAlgebra::PreconditionerJacobi (PreconditionerJacobi.t.cpp)
+//   basis::AtomCenterNonLocalOpContextFE apply-side members
+//       (AtomCenterNonLocalOpContextFE.t.cpp:36-265, :714-1045), standalone
+//       and fused into the KS apply through an ONCV component
+//       (KohnShamOperatorContextFE.t.cpp:1022-1080, :1177-1180)
 // The M^-1 (GLL) operator below repeats the three calls of
 // CFEOverlapInverseOpContextGLL::apply's diagonal branch
 // (CFEOverlapInverseOpContextGLL.t.cpp:528-559) because that class's
@@ -20,8 +24,11 @@
 //   inputs : meta.txt, nd.u32, ids.u32, H.f64, M.f64, K.f64, minv.f64,
 //            jacdiag.f64, cons_rows.u32, cons_sizes.u32, cons_cols.u32,
 //            cons_acc.u32, cons_vals.f64, cons_inh.f64, X.f64, eig.f64, b.f64
+//            optional nonlocal part: nl_meta.txt (n_proj), nl_np.u32,
+//            nl_pids.u32, nl_c.f64, nl_v.f64
 //   outputs: Y_H.f64, X_after.f64, Y_M.f64, Y_Minv.f64, Y_rfilter.f64,
-//            Y_filter.f64, x_cg.f64, cg.txt
+//            Y_filter.f64, x_cg.f64, cg.txt; with the nonlocal inputs also
+//            Y_nl.f64 (standalone) and Y_Hnl.f64 (H + nonlocal, fused)
 #include <fstream>
 #include <ksdft/KohnShamOperatorContextFE.h>
 #include <basis/ConstraintsInternal.h>
@@ -214,6 +221,33 @@ int main(int argc, char **argv) {
     opMinv.apply(X, Y, true, false);
     write_bin(d + "Y_Minv.f64", Y.data(), (size_t)N * m);
   }
+#ifdef GBFE_REF_HAS_NONLOCAL
+  {  // nonlocal part: standalone and fused into the KS apply
+    std::ifstream nm(d + "nl_meta.txt");
+    size_type nProj = 0;
+    if (nm >> nProj) {
+      auto np = read_bin<uint32_t>(d + "nl_np.u32");
+      auto pids = read_bin<uint32_t>(d + "nl_pids.u32");
+      std::vector<size_type> np_st(np.begin(), np.end()), pid_st(pids.begin(), pids.end());
+      auto cc = read_bin<double>(d + "nl_c.f64");
+      auto vv = read_bin<double>(d + "nl_v.f64");
+      using NLOp = basis::AtomCenterNonLocalOpContextFE<double, double, HOST, 3>;
+      auto nl = std::make_shared<const NLOp>(basis, nProj, np_st, pid_st, cc, vv, 1, std::max<size_type>(m, nrhs), ctx);
+      MV X(basis.pattern, ctx, m, 0.0), Y(basis.pattern, ctx, m, 0.0);
+      load_mv(X, X0);
+      nl->apply(X, Y, true, false);
+      write_bin(d + "Y_nl.f64", Y.data(), (size_t)N * m);
+      auto oncv = std::make_shared<ksdft::ElectrostaticONCVNonLocFE<double, double, double, double, HOST, 3>>();
+      oncv->localMats = read_bin<double>(d + "H.f64");
+      oncv->nonLocal = nl;
+      std::vector<KSOp::HamiltonianPtrVariant> hv{std::shared_ptr<ksdft::Hamiltonian<double, HOST>>(oncv)};
+      KSOp opHnl(basis, hv, ctx, 1, std::max<size_type>(m, nrhs), true);
+      load_mv(X, X0);
+      opHnl.apply(X, Y, true, false);
+      write_bin(d + "Y_Hnl.f64", Y.data(), (size_t)N * m);
+    }
+  }
+#endif
   {  // residual Chebyshev filter
     MV X(basis.pattern, ctx, m, 0.0), Y(basis.pattern, ctx, m, 0.0);
     load_mv(X, X0);

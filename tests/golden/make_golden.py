@@ -10,9 +10,11 @@ and the reference outputs:
   Y_rfilter      ResidualChebyshevFilterGEP(H, M, M^-1)
   Y_filter       ChebyshevFilter(H, M^-1)
   x_cg, cg_ok    Jacobi-preconditioned CGLinearSolver on K
+  Y_nl, Y_Hnl    (nonlocal cases) AtomCenterNonLocalOpContextFE::apply alone,
+                 and the KS apply of H with the nonlocal part fused in
 
 Run (in a checkout where the reference sources exist):
-    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py [case names]
 """
 from __future__ import annotations
 
@@ -32,7 +34,7 @@ HERE = Path(__file__).resolve().parent
 
 
 def run_case(name, nd, ids, N, cons, H, Mm, K, minv, jacdiag, X, eig, b, degree, wl, wu, uu,
-             max_iter=3000, abs_tol=1e-14, rel_tol=1e-11, div_tol=1e8):
+             max_iter=3000, abs_tol=1e-14, rel_tol=1e-11, div_tol=1e8, nl=None):
     m = X.shape[1]
     nrhs = b.shape[1]
     with tempfile.TemporaryDirectory() as d:
@@ -48,17 +50,29 @@ def run_case(name, nd, ids, N, cons, H, Mm, K, minv, jacdiag, X, eig, b, degree,
                                ("cons_inh.f64", cons.inhomogeneities, np.float64), ("X.f64", X, np.float64),
                                ("eig.f64", eig, np.float64), ("b.f64", b, np.float64)]:
             np.ascontiguousarray(arr, dtype=dt).tofile(d / fname)
+        extra = {}
+        if nl is not None:
+            (d / "nl_meta.txt").write_text(f"{nl.n_proj}\n")
+            for fname, arr, dt in [("nl_np.u32", nl.proj_per_cell, np.uint32), ("nl_pids.u32", nl.proj_ids, np.uint32),
+                                   ("nl_c.f64", nl.cell_c, np.float64), ("nl_v.f64", nl.coupling, np.float64)]:
+                np.ascontiguousarray(arr, dtype=dt).tofile(d / fname)
+            extra = dict(nl_n_proj=np.array(nl.n_proj), nl_np=nl.proj_per_cell, nl_pids=nl.proj_ids,
+                         nl_c=nl.cell_c, nl_v=nl.coupling)
         subprocess.run([str(DRIVER), str(d)], check=True)
         rd = lambda f, shape: np.fromfile(d / f, dtype=np.float64).reshape(shape)  # noqa: E731
         out = dict(Y_H=rd("Y_H.f64", (N, m)), X_after=rd("X_after.f64", (N, m)), Y_M=rd("Y_M.f64", (N, m)),
                    Y_Minv=rd("Y_Minv.f64", (N, m)), Y_rfilter=rd("Y_rfilter.f64", (N, m)),
                    Y_filter=rd("Y_filter.f64", (N, m)), x_cg=rd("x_cg.f64", (N, nrhs)),
                    cg_ok=np.array(int((d / "cg.txt").read_text().split()[0]) == 0))
+        if nl is not None:
+            if not (d / "Y_nl.f64").exists():
+                sys.exit("ref_driver was built without the nonlocal part (see oracle/build_ref.sh)")
+            out.update(Y_nl=rd("Y_nl.f64", (N, m)), Y_Hnl=rd("Y_Hnl.f64", (N, m)))
     np.savez_compressed(HERE / f"{name}.npz", nd=nd.astype(np.uint32), ids=ids.astype(np.uint32), n_dofs=np.array(N),
                         cons_rows=cons.row_ids, cons_sizes=cons.row_sizes, cons_cols=cons.col_ids,
                         cons_acc=cons.row_acc, cons_vals=cons.col_values, cons_inh=cons.inhomogeneities,
                         H=H, M=Mm, K=K, minv=minv, jacdiag=jacdiag, X=X, eig=eig, b=b,
-                        params=np.array([degree, wl, wu, uu, max_iter, abs_tol, rel_tol, div_tol]), **out)
+                        params=np.array([degree, wl, wu, uu, max_iter, abs_tol, rel_tol, div_tol]), **out, **extra)
     print(f"{name}: N={N} cells={nd.size} m={m} -> {HERE / (name + '.npz')}")
 
 
@@ -75,7 +89,7 @@ def jacobi_diag(nd, ids, K, N, cons):
     return diag
 
 
-def fe_case(name, n, p, L, atoms, seed, m, degree, hanging=False):
+def fe_case(name, n, p, L, atoms, seed, m, degree, hanging=False, nonlocal_part=False):
     prob = M.ks_box(n, p, L, atoms, 4.0, 0.5, seed=seed)
     if hanging:
         prob.constraints = M.add_synthetic_hanging(prob.constraints, n, p, np.random.default_rng(seed), 0.1,
@@ -87,9 +101,14 @@ def fe_case(name, n, p, L, atoms, seed, m, degree, hanging=False):
     b[prob.constraints.row_ids] = 0.0
     # bounds from the spectrum of M_GLL^-1 H estimated with a dense solve (small case)
     wl, wu, uu = -4.0, 1.0, 40.0 * p * p / (L / n) ** 2
+    nl = None
+    if nonlocal_part:
+        from gbfe import nonlocal_psp
+
+        nl = nonlocal_psp.projectors(prob)
     run_case(name, prob.nd_per_cell, prob.cell_dof_ids, prob.n_dofs, prob.constraints, prob.H, prob.M, prob.K,
              1.0 / prob.m_gll_diag, jacobi_diag(prob.nd_per_cell, prob.cell_dof_ids, prob.K, prob.n_dofs,
-                                                prob.constraints), X, eig, b, degree, wl, wu, uu)
+                                                prob.constraints), X, eig, b, degree, wl, wu, uu, nl=nl)
 
 
 def variable_case(name, seed):
@@ -123,7 +142,14 @@ def variable_case(name, seed):
 if __name__ == "__main__":
     if not DRIVER.exists():
         sys.exit("build oracle/_ref first: bash oracle/build_ref.sh")
-    fe_case("case_dirichlet_p2", 2, 2, 6.0, 1, 101, 4, 6)
-    fe_case("case_dirichlet_p3", 2, 3, 8.0, 2, 102, 5, 8)
-    fe_case("case_hanging_p2", 3, 2, 6.0, 2, 103, 3, 5, hanging=True)
-    variable_case("case_variable_nd", 104)
+    cases = {
+        "case_dirichlet_p2": lambda n: fe_case(n, 2, 2, 6.0, 1, 101, 4, 6),
+        "case_dirichlet_p3": lambda n: fe_case(n, 2, 3, 8.0, 2, 102, 5, 8),
+        "case_hanging_p2": lambda n: fe_case(n, 3, 2, 6.0, 2, 103, 3, 5, hanging=True),
+        "case_variable_nd": lambda n: variable_case(n, 104),
+        "case_nonlocal_p3": lambda n: fe_case(n, 2, 3, 8.0, 2, 105, 5, 6, nonlocal_part=True),
+        "case_nonlocal_hanging_p2": lambda n: fe_case(n, 3, 2, 6.0, 2, 106, 4, 5, hanging=True,
+                                                      nonlocal_part=True),
+    }
+    for name in (sys.argv[1:] or list(cases)):
+        cases[name](name)

@@ -93,3 +93,50 @@ def test_gpu_matches_reference(gpu_ctx, path):
     assert (rc == 0) == bool(z["cg_ok"])
     if np.abs(z["x_cg"]).max() > 0:
         assert rel_maxnorm(x.numpy(), z["x_cg"]) <= 1e-9
+
+
+NONLOCAL = [p for p in GOLDEN if "nonlocal" in p.stem]
+
+
+class _NL:
+    """Nonlocal arrays of a fixture in the shape gbfe.nonlocal_psp.NonLocalData has."""
+
+    def __init__(self, z):
+        self.n_proj = int(z["nl_n_proj"])
+        self.proj_per_cell, self.proj_ids = z["nl_np"], z["nl_pids"]
+        self.cell_c, self.coupling = z["nl_c"], z["nl_v"]
+
+
+def test_nonlocal_fixtures_present():
+    assert len(NONLOCAL) >= 2
+
+
+@pytest.mark.parametrize("path", NONLOCAL, ids=[p.stem for p in NONLOCAL])
+def test_oracle_nonlocal_matches_reference(path):
+    """AtomCenterNonLocalOpContextFE::apply and the KS apply with the
+    nonlocal part fused in, as the reference computes them."""
+    z = load(path)
+    s = O.OracleSystem(z["nd"], z["ids"], int(z["n_dofs"]), z["cons"])
+    nl = s.nonlocal_part(_NL(z))
+    assert rel_maxnorm(s.apply(s.nonlocal_op(nl), z["X"].copy()), z["Y_nl"]) <= 1e-13
+    assert rel_maxnorm(s.apply(s.cell_op(z["H"], nonlocal_part=nl), z["X"].copy()), z["Y_Hnl"]) <= 1e-13
+    # the nonlocal term is not negligible in these cases
+    assert rel_maxnorm(z["Y_Hnl"], z["Y_H"]) > 1e-3
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", NONLOCAL, ids=[p.stem for p in NONLOCAL])
+def test_gpu_nonlocal_matches_reference(gpu_ctx, path):
+    from gbfe import api
+
+    z = load(path)
+    basis = api.FEBasisManager(gpu_ctx, z["nd"], z["ids"], int(z["n_dofs"]), z["cons"])
+    nl = api.AtomCenterNonLocalOpContextFE(basis, _NL(z))
+    H = api.KohnShamOperatorContextFE(basis, z["H"], nonlocal_part=nl)
+    m = z["X"].shape[1]
+    X, Y = api.MultiVector(basis, m, init=z["X"]), api.MultiVector(basis, m)
+    nl.apply(X, Y)
+    assert rel_maxnorm(Y.numpy(), z["Y_nl"]) <= 1e-12
+    X.copy_from(z["X"])
+    H.apply(X, Y)
+    assert rel_maxnorm(Y.numpy(), z["Y_Hnl"]) <= 1e-12

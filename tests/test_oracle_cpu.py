@@ -111,3 +111,32 @@ def test_residual_filter_reduces_unwanted(small_problem):
     X = M.random_block(p.n_dofs, 6, 5)
     Y = s.residual_filter(H, Mo, Mi, np.zeros(6), X.copy(), 8, b[0], b[0] + 0.2 * (b[1] - b[0]), b[1] + b[2] / 10)
     assert np.isfinite(Y).all() and np.abs(Y).max() > 0
+
+
+@pytest.mark.parametrize("use_blas", [True, False])
+def test_nonlocal_matches_dense_projector_form(use_blas):
+    """The oracle's nonlocal part (cell-wise C_c blocks, scatter, V scale,
+    beta = 1 add) equals the dense form P^T C^T diag(V) C P X on a Dirichlet
+    box, standalone and fused into the Kohn-Sham apply."""
+    from gbfe import nonlocal_psp as NL
+
+    p = M.ks_box(3, 3, 8.0, 2, 4.0, 0.5, seed=31)
+    d = NL.projectors(p)
+    assert d.n_proj == 2 * d.per_atom and d.proj_per_cell.max() > 0
+    s = O.OracleSystem.from_problem(p, use_blas=use_blas)
+    nl = s.nonlocal_part(d)
+    X0 = M.random_block(p.n_dofs, 5, 3)
+    Cg = d.dense(p.nd_per_cell, p.cell_dof_ids, p.n_dofs)
+    rows = p.constraints.row_ids.astype(np.int64)
+    Xp = X0.copy()
+    Xp[rows] = 0.0
+    Yd = Cg.T @ (d.coupling[:, None] * (Cg @ Xp))
+    Yd[rows] = 0.0
+    Ynl = s.apply(s.nonlocal_op(nl), X0.copy())
+    assert np.abs(Ynl - Yd).max() <= 1e-13 * np.abs(Yd).max()
+    Yloc = s.apply(s.cell_op(p.H), X0.copy())
+    Yfused = s.apply(s.cell_op(p.H, nonlocal_part=nl), X0.copy())
+    assert np.abs(Yfused - (Yloc + Yd)).max() <= 1e-13 * np.abs(Yfused).max()
+    # symmetric: the projected operator is Hermitian
+    G = Xp.T @ Ynl
+    assert np.abs(G - G.T).max() <= 1e-13 * np.abs(G).max()
