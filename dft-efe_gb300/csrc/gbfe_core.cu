@@ -330,13 +330,14 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
     check_launch(ctx, "diag_apply");
     return;
   }
-  // cell operator
+  // cell operator; the nonlocal projection (if any) reads X after p2c and
+  // is added into the cell-wise result before the assembly
+  if (op->nl) nonlocal_project(op->nl, X);
   if (X->dtype == GBFE_F32) {
     apply_cell_mixed(op, X, Y);
     return;
   }
   op->cellbuf.ensure((size_t)me->total_cell_dofs * m);
-  if (op->nl) nonlocal_project(op->nl, X);
   if (ctx->fp64_tc && op->oz_aoff.p)
     cell_apply_oz(op, X, op->cellbuf.p);
   else
@@ -1084,6 +1085,7 @@ extern "C" int gbfe_apply_f64_noalloc(const gbfe_op *op, double *X_dev, double *
       GBFE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_cell_scratch));
       g_noalloc_ptr[dev] = (double *)p;
     }
+    GBFE_REQUIRE(!op->nl, "apply_f64_noalloc: operators with a nonlocal part need gbfe_apply");
     double *Yc = g_noalloc_ptr[dev];
     const uint32_t Nn = (uint32_t)me->n_dofs;
     (void)Nn;

@@ -170,12 +170,17 @@ void nonlocal_project(const gbfe_nl *nl, const gbfe_mv *X) {
   }
 }
 
+// W must come from nonlocal_project of the same X (same precision and m)
 void nonlocal_add(const gbfe_nl *nl, uint32_t m, int dtype, void *Yc) {
   if (!nl->n_cells_nl || !m) return;
-  if (dtype == GBFE_F64)
+  const size_t need = (size_t)nl->n_proj * m;
+  if (dtype == GBFE_F64) {
+    GBFE_REQUIRE(nl->w.p && nl->w.n >= need, "nonlocal: add without a projection of this block");
     add_t<double>(nl, m, static_cast<double *>(Yc), nl->cmat.p, nl->w.p);
-  else
+  } else {
+    GBFE_REQUIRE(nl->w_f32.p && nl->w_f32.n >= need, "nonlocal: add without a projection of this block");
     add_t<float>(nl, m, static_cast<float *>(Yc), nl->cmat_f32.p, nl->w_f32.p);
+  }
 }
 
 }  // namespace gbfe
