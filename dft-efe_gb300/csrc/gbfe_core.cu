@@ -421,6 +421,7 @@ int gbfe_ctx_create(int device, gbfe_ctx **out) {
     GBFE_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device));
     GBFE_REQUIRE(major == 10 && minor == 3, "libgbfe is built for sm_103a (GB300) only");
     ctx->device = device;
+    ctx->cc_major = major;
     GBFE_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
     GBFE_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
     ctx->stream = ctx->own_stream;
@@ -539,8 +540,9 @@ int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on) {
 }
 
 int gbfe_ctx_set_fp64_apply(gbfe_ctx *ctx, int mode) {
-  if (!ctx || mode < 0 || mode > 1) return GBFE_ERR_ARG;
-  ctx->fp64_tc = mode;
+  if (!ctx || mode < 0 || mode > 2) return GBFE_ERR_ARG;
+  ctx->fp64_tc = mode ? 1 : 0;
+  ctx->fp64_tc_dense = mode == 1 ? 1 : 0;
   return GBFE_OK;
 }
 

@@ -157,6 +157,11 @@ struct gbfe_ctx {
   int tc_version = 2;        // 2: persistent warp-specialised kernel; 1: one CTA per cell
   std::atomic<int> *cancel = nullptr;  // polled between passes / iterations when set
   int fp64_tc = 0;           // 1: FP64 applies use the sliced tensor-core product when built
+  int fp64_tc_dense = 1;     // with fp64_tc: the Gram / rotation stages use the sliced products too
+  int cc_major = 0;          // compute capability of the device
+  gbfe::DBuf<int> oz_exp, oz_rexp;  // sliced products: column / row exponents
+  gbfe::DBuf<double> oz_part;       // per-item Gram partials
+  gbfe::DBuf<__nv_bfloat16> oz_tdig;  // slices of the rotation factor
 };
 
 struct gbfe_mesh {
@@ -316,6 +321,12 @@ void nonlocal_project(const gbfe_nl *nl, const gbfe_mv *X);
 void nonlocal_add(const gbfe_nl *nl, uint32_t m, int dtype, void *Yc);
 void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log);
 bool oz_supported(const gbfe_mesh *me);
+// FP64-accurate sliced tensor-core products of the subspace stages (gbfe_ozgemm.cu)
+bool oz_gemm_supported(gbfe_ctx *ctx, uint32_t m);
+void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, const double *B, uint32_t mb,
+             uint64_t N, double *const *S);
+void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const double *const *Y, double *const *out,
+               uint32_t nops, uint64_t N);
 void build_oz_mats(gbfe_op *op);
 void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc);
 

@@ -1,0 +1,68 @@
+// gbfe_oz.cuh -- shared pieces of the FP64-accurate sliced tensor-core
+// products (the splitting scheme of Ozaki, Ogita, Oishi & Rump, Numer.
+// Algorithms 59, 2012):
+//
+//   v = 2^(e+1) * sum_{s=1..8} d_s 2^(-7 s),   |v| < 2^e,  d_s integers in [-64, 64]
+//
+// The value is scaled to a 55-bit signed fixed-point integer (truncated:
+// error below 2^(e-55)) and cut into balanced base-128 digits.  Every digit
+// product is at most 2^12 in magnitude, so a level sum
+// L_g = sum_{s+t=g} sum_k a_s x_t (at most 8 digit pairs) over K <= 512 terms
+// stays within 2^24 and FP32 tensor-core accumulation of it is exact.
+#pragma once
+#include <cstdint>
+
+namespace gbfe {
+namespace oz {
+
+constexpr int S = 8;       // slices per operand
+constexpr int LEVELS = 8;  // g = s + t = 2..9 (36 digit pairs); g >= 10 is below 2^-63 and dropped
+constexpr int K_EXACT = 512;  // longest exact FP32 accumulation of one level
+
+// smallest e with |v| < 2^e (0 for v == 0)
+__device__ __forceinline__ int exponent_of(double vmax) {
+  if (!(vmax > 0.0)) return 0;
+  int e;
+  frexp(vmax, &e);
+  return e;
+}
+
+// balanced digits of v (|v| < 2^e): d[0] most significant
+__device__ __forceinline__ void digits(double v, int e, int *d) {
+  const uint64_t bits = (uint64_t)__double_as_longlong(v);
+  const int ex = (int)((bits >> 52) & 0x7ff);
+  int64_t X = 0;
+  if (ex != 0) {
+    const uint64_t mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = ex - 1075 + 55 - e;  // v 2^(55-e) = mant 2^sh and |v| < 2^e: sh <= 2
+    uint64_t fx = 0;
+    if (sh >= 0)
+      fx = mant << sh;
+    else if (sh > -64)
+      fx = mant >> (-sh);
+    X = (bits >> 63) ? -(int64_t)fx : (int64_t)fx;
+  }
+#pragma unroll
+  for (int s = S - 1; s >= 1; --s) {
+    const int r = (int)((X + 64) & 127) - 64;  // balanced remainder in [-64, 63]
+    d[s] = r;
+    X = (X - r) >> 7;  // exact division
+  }
+  d[0] = (int)X;  // |X| <= 64 after the seven low digits
+}
+
+// 2^k as a double (k within the normal range)
+__device__ __forceinline__ double pow2(int k) { return __longlong_as_double((long long)(uint64_t)(k + 1023) << 52); }
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// sum_g L_g 2^-7g of one accumulator column, smallest level first, as an
+// FP32 double-float (every term L_g 2^-7g is exact in FP32)
+__device__ __forceinline__ float level_weight(int g) { return __int_as_float((127 - 7 * g) << 23); }
+
+}  // namespace oz
+}  // namespace gbfe

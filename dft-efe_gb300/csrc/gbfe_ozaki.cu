@@ -4,21 +4,21 @@
 // multiplication", Numer. Algorithms 59, 2012).
 //
 // GB300 runs FP64 FMA at ~1.25 TFLOP/s, so the FP64 cell product of the plain
-// path is bound by the FP64 pipe.  Here each operand is cut into eight signed
-// 7-bit integer slices, which BF16 represents exactly:
-//     A_op[j][k] = 2^ea_j  sum_s a_s[j][k] 2^-7s      (per-row exponent ea_j)
-//     X[i][v]    = 2^ex_v  sum_t x_t[i][v] 2^-7t      (per-vector exponent ex_v)
-// with |digits| <= 127 and a truncation error below 2^-56 of the row / vector
+// path is bound by the FP64 pipe.  Here each operand is cut into eight
+// balanced base-128 digit slices (gbfe_oz.cuh), which BF16 represents exactly:
+//     A_op[j][k] = 2^(ea_j+1) sum_s a_s[j][k] 2^-7s     (per-row exponent ea_j)
+//     X[i][v]    = 2^(ex_v+1) sum_t x_t[i][v] 2^-7t     (per-vector exponent ex_v)
+// with |digits| <= 64 and a truncation error below 2^-55 of the row / vector
 // maximum.  For every level g = s + t (2..9) the tensor cores accumulate
 //     L_g[j][v] = sum_{s+t=g} sum_k a_s[j][k] x_t[k][v]
 // in its own FP32 TMEM accumulator (8 levels x 64 vectors = all 512 columns).
-// Every partial sum is an integer below 2^24 for cells of up to 256 dofs
-// (level 2: 127^2 * 256 < 2^22; higher levels: at most 8 products of
-// 127 * 64 each), so the accumulation is exact.  The epilogue forms
-// sum_g L_g 2^-7g as an FP32 double-float (error-free TwoSum), converts once to
-// FP64 and applies 2^(ea_j + ex_v).  Products with s + t > 9 are below 2^-63
-// and are dropped.  Result: the FP64 product to ~2^-52 relative to
-// |A| |X| per entry, with 36 tensor-core MMAs per K step.
+// A level holds at most 8 digit pairs of products <= 2^12, so for cells of up
+// to 256 dofs every partial sum stays below 2^23 and the accumulation is
+// exact.  The epilogue forms sum_g L_g 2^-7g as an FP32 double-float
+// (error-free TwoSum), converts once to FP64 and applies 2^(ea_j + ex_v + 2).
+// Products with s + t > 9 are below 2^-63 and are dropped.  Result: the FP64
+// product to ~2^-48 relative per entry (normwise), with 36 tensor-core MMAs
+// per K step.
 //
 // Data movement follows the persistent split-BF16 kernel: A slices are
 // pre-laid-out in HBM (per cell, per K chunk of 32, 8 slices in the canonical
@@ -27,6 +27,7 @@
 // instructions; one thread issues tcgen05.mma; warps 0-3 run the epilogue.
 // Cells with more than 128 dofs are processed as two 128-row work items.
 #include "gbfe_internal.cuh"
+#include "gbfe_oz.cuh"
 #include "gbfe_tc_ptx.cuh"
 
 #include <algorithm>
@@ -45,34 +46,8 @@ constexpr uint32_t OZ_A_PART = 128 * KC * 2;  // one slice of a 128-row A chunk 
 constexpr uint32_t OZ_B_PART = OZ_N * KC * 2;  // one slice of a B chunk
 constexpr uint32_t OZ_STAGE = OZ_S * (OZ_A_PART + OZ_B_PART);
 
-// digits of v / 2^e (|v| < 2^e) as 8 signed 7-bit integers, by bit manipulation
-__device__ __forceinline__ void oz_digits(double v, int e, int *d) {
-  const uint64_t bits = (uint64_t)__double_as_longlong(v);
-  const int ex = (int)((bits >> 52) & 0x7ff);
-  uint64_t fx = 0;
-  if (ex != 0) {
-    const uint64_t mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-    const int sh = ex - 1075 + 56 - e;  // v * 2^(56-e) = mant * 2^sh, sh < 4
-    if (sh >= 0)
-      fx = mant << sh;
-    else if (sh > -64)
-      fx = mant >> (-sh);
-  }
-  const bool neg = (bits >> 63) != 0;
-#pragma unroll
-  for (int s = 1; s <= OZ_S; ++s) {
-    const int dd = (int)((fx >> (56 - 7 * s)) & 127u);
-    d[s - 1] = neg ? -dd : dd;
-  }
-}
-
-// smallest e with |v| < 2^e
-__device__ __forceinline__ int oz_exponent(double vmax) {
-  if (!(vmax > 0.0)) return 0;
-  int e;
-  frexp(vmax, &e);
-  return e;
-}
+__device__ __forceinline__ void oz_digits(double v, int e, int *d) { oz::digits(v, e, d); }
+__device__ __forceinline__ int oz_exponent(double vmax) { return oz::exponent_of(vmax); }
 
 // A_op = A_c^T slices: per (cell, chunk) [slice][MT8 x KC] canonical tiles,
 // and per-row exponents (one per cell dof).
@@ -142,11 +117,7 @@ struct OzArgs {
   int *status;
 };
 
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
+using oz::two_sum;
 
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -343,7 +314,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
           for (int q2 = 0; q2 < 16; ++q2) {
             const uint32_t v = v0 + col + q2;
             if (v < m) {
-              const int sc = er + a.x_exp[v];
+              const int sc = er + a.x_exp[v] + 2;
               const double scale = __longlong_as_double((long long)(uint64_t)(sc + 1023) << 52);
               dst[q2] = ((double)hi[q2] + (double)lo[q2]) * scale;
             }

@@ -1,0 +1,642 @@
+// gbfe_ozgemm.cu -- FP64-accurate tall-skinny products of the subspace
+// stages on the BF16 tensor cores (sliced as in gbfe_oz.cuh).
+//
+// The Rayleigh-Ritz / Cholesky-GS stages of a ChFSI pass spend their FP64
+// flops in two shapes (ChebyshevFilteredEigenSolver.t.cpp:194-437 through
+// OrthonormalizationFunctions.t.cpp:356-415 and
+// RayleighRitzEigenSolver.t.cpp:233-301):
+//   * Gram matrices  S_o = A_o^T B      (A_o, B: N x m blocks, K = N long)
+//   * rotations      out_o = Y_o T     (Y_o: N x m, T: m x m, K = m short)
+// GB300's FP64 pipe caps both near 1.1 TFLOP/s.  Here:
+//   k_oz_gram: work item = (128 rows of the stacked A_o columns, 64 columns of
+//     B, a range of 512-row K chunks).  Eight producer warps read FP64 rows
+//     (coalesced across columns), cut them into 8 balanced digit slices with
+//     per-column exponents and store canonical K-major tiles; one thread
+//     issues 36 tcgen05.mma per 16-row K step into 8 level accumulators (all
+//     512 TMEM columns).  After every 512 rows (the exact FP32 range) the
+//     producers drain TMEM into FP64 registers.  Each item writes its partial;
+//     k_oz_gram_final sums the partials in a fixed order (deterministic).
+//   * k_oz_rot: work item = (operand, 128 rows, 64 output columns); the m x m
+//     factor is sliced once per call (k_oz_build_t) and lands by bulk copies;
+//     Y rows are sliced by the producers with per-row exponents; one TMEM pass
+//     covers K = m <= 512.
+// Every wait is bounded (error status, no hang); TMEM is freed on every exit.
+#include "gbfe_internal.cuh"
+#include "gbfe_oz.cuh"
+#include "gbfe_tc_ptx.cuh"
+
+#include <algorithm>
+
+using namespace gbfe;
+using namespace gbfe::tc;
+
+namespace {
+
+constexpr int PW = 8;                      // producer / epilogue warps
+constexpr int OG_THREADS = (PW + 2) * 32;  // + TMA warp + MMA warp
+constexpr int OG_N = 64;                   // output columns per item (8 levels x 64 = 512 TMEM columns)
+constexpr int OG_STAGES = 2;
+constexpr uint32_t A_PART = 128 * KC * 2;  // one slice of a 128 x KC tile (bytes)
+constexpr uint32_t B_PART = OG_N * KC * 2;
+constexpr uint32_t OG_STAGE = oz::S * (A_PART + B_PART);
+constexpr uint32_t OG_SMEM = OG_STAGES * OG_STAGE + 1024 + 512;
+constexpr uint32_t CHUNK = oz::K_EXACT;    // Gram rows per exact TMEM accumulation
+constexpr uint32_t STAGES_PER_CHUNK = CHUNK / KC;
+constexpr uint32_t TILE = 128 * OG_N;      // elements of one partial tile
+
+// write the 8 slices of 8 consecutive K values (one 16-byte core row each)
+__device__ __forceinline__ void store_core_rows(uint8_t *tile, uint32_t part, uint32_t pos, const double *v, int e) {
+  uint32_t packed[oz::S][4];
+#pragma unroll
+  for (int kk = 0; kk < 8; kk += 2) {
+    int d0[oz::S], d1[oz::S];
+    oz::digits(v[kk], e, d0);
+    oz::digits(v[kk + 1], e, d1);
+#pragma unroll
+    for (int s = 0; s < oz::S; ++s) {
+      const __nv_bfloat162 pr = __halves2bfloat162(__int2bfloat16_rn(d0[s]), __int2bfloat16_rn(d1[s]));
+      packed[s][kk / 2] = *reinterpret_cast<const uint32_t *>(&pr);
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < oz::S; ++s)
+    *(uint4 *)(tile + s * part + pos) = make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+}
+
+// 36 digit-pair MMAs of one 16-row K step into the 8 level accumulators
+__device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t abase, uint32_t bbase, uint32_t ks,
+                                             bool first) {
+  const uint32_t idesc = instr_desc(128, OG_N);
+#pragma unroll
+  for (int g = 2; g <= oz::S + 1; ++g) {
+    const uint32_t d = tmem + (g - 2) * OG_N;
+    const int s_lo = g - oz::S > 1 ? g - oz::S : 1;
+    const int s_hi = g - 1 < oz::S ? g - 1 : oz::S;
+#pragma unroll
+    for (int sl = s_lo; sl <= s_hi; ++sl) {
+      const int tl = g - sl;
+      const uint64_t ad = smem_desc(abase + (sl - 1) * A_PART + ks * 2 * LBO);
+      const uint64_t bd = smem_desc(bbase + (tl - 1) * B_PART + ks * 2 * LBO);
+      umma(d, ad, bd, idesc, (!first || sl != s_lo) ? 1u : 0u);
+    }
+  }
+}
+
+// sum_g L_g 2^-7g for 16 columns of this thread's TMEM lane
+__device__ __forceinline__ void combine16(uint32_t taddr, float *hi, float *lo) {
+#pragma unroll
+  for (int q = 0; q < 16; ++q) hi[q] = lo[q] = 0.f;
+  for (int g = oz::S + 1; g >= 2; --g) {  // smallest level first
+    float L[16];
+    tmem_ld16(taddr + (g - 2) * OG_N, L);
+    const float w = oz::level_weight(g);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      float s2, e2;
+      oz::two_sum(hi[q], L[q] * w, s2, e2);
+      hi[q] = s2;
+      lo[q] += e2;
+    }
+  }
+}
+
+struct Barriers {
+  uint64_t *full, *full_b, *empty, *tfull, *tempty;
+  uint32_t *tmem_slot;
+  volatile int *abort_flag;
+};
+
+// barrier block after the stages: full[S], full_b[S], empty[S], tfull, tempty,
+// then the TMEM address and the abort flag
+__device__ __forceinline__ Barriers carve(uint8_t *smem) {
+  Barriers b;
+  uint64_t *bars = (uint64_t *)(smem + OG_STAGES * OG_STAGE);
+  b.full = bars;
+  b.full_b = bars + OG_STAGES;
+  b.empty = bars + 2 * OG_STAGES;
+  b.tfull = bars + 3 * OG_STAGES;
+  b.tempty = b.tfull + 1;
+  b.tmem_slot = (uint32_t *)(b.tempty + 1);
+  b.abort_flag = (volatile int *)(b.tmem_slot + 1);
+  return b;
+}
+
+// ---------------------------------------------------------------- Gram
+struct GramArgs {
+  const double *A0, *A1;  // stacked operands: rows R < ma from A0, then A1
+  uint32_t na, ma;
+  const double *B;
+  uint32_t mb;
+  uint64_t N;
+  const int *aexp;  // [na * ma]
+  const int *bexp;  // [mb]
+  uint32_t row_tiles, col_tiles, splits, chunks, chunks_per_split;
+  double *part;  // [items][OG_N][128] unscaled partial sums
+  int *status;
+};
+
+__global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const Barriers br = carve(smem);
+  const uint32_t tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+  const uint32_t n_items = a.row_tiles * a.col_tiles * a.splits;
+  if (tid == 0) {
+    for (int s = 0; s < OG_STAGES; ++s) {
+      mbar_init(&br.full[s], PW);
+      mbar_init(&br.empty[s], 1);
+    }
+    mbar_init(br.tfull, 1);
+    mbar_init(br.tempty, PW);
+    *br.abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == PW + 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(br.tmem_slot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *br.tmem_slot;
+  auto wait = [&](uint64_t *bar, uint32_t parity, int code) -> bool {
+    if (*br.abort_flag) return false;
+    if (mbar_wait(bar, parity, a.status, code)) return true;
+    *br.abort_flag = 1;
+    return false;
+  };
+  auto chunk_range = [&](uint32_t it, uint32_t &c0, uint32_t &c1) {
+    const uint32_t sp = it % a.splits;
+    c0 = sp * a.chunks_per_split;
+    c1 = min(a.chunks, c0 + a.chunks_per_split);
+  };
+
+  if (warp == PW + 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      uint32_t q = 0, nchunk = 0;
+      bool ok = true;
+      for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
+        uint32_t c0, c1;
+        chunk_range(it, c0, c1);
+        for (uint32_t c = c0; c < c1 && ok; ++c, ++nchunk) {
+          if (nchunk >= 1 && !wait(br.tempty, (nchunk - 1) & 1, 41)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          for (uint32_t st = 0; st < STAGES_PER_CHUNK; ++st, ++q) {
+            const uint32_t s = q % OG_STAGES;
+            if (!wait(&br.full[s], (q / OG_STAGES) & 1, 42)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t abase = smem_u32(smem + s * OG_STAGE);
+            const uint32_t bbase = abase + oz::S * A_PART;
+            for (uint32_t ks = 0; ks < KC / 16; ++ks) issue_levels(tmem, abase, bbase, ks, st == 0 && ks == 0);
+            umma_commit(&br.empty[s]);
+          }
+          if (ok) umma_commit(br.tfull);
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp < PW) {
+    // ---------------- producers: FP64 rows -> digit tiles; drains
+    const uint32_t ar = tid % 128, ah = tid / 128;  // A: row of the tile, half of the K chunk
+    const uint32_t bj = tid % OG_N, bq = tid / OG_N;  // B: row (column of B), quarter of the K chunk
+    const uint32_t quad = warp % 4, colh = warp / 4;
+    uint32_t q = 0, nchunk = 0;
+    bool ok = true;
+    for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
+      const uint32_t tile = it / a.splits;
+      const uint32_t rt = tile / a.col_tiles, ct = tile % a.col_tiles;
+      uint32_t c0, c1;
+      chunk_range(it, c0, c1);
+      // this thread's A row and B row
+      const uint32_t R = rt * 128 + ar;
+      const bool arow = R < a.na * a.ma;
+      const double *Asrc = arow ? ((R < a.ma ? a.A0 : a.A1) + (R % a.ma)) : nullptr;
+      const uint32_t am = a.ma;
+      const int ae = arow ? a.aexp[R] : 0;
+      const uint32_t J = ct * OG_N + bj;
+      const bool brow = J < a.mb;
+      const int be = brow ? a.bexp[J] : 0;
+      double acc[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) acc[i] = 0.0;
+      for (uint32_t c = c0; c < c1 && ok; ++c, ++nchunk) {
+        for (uint32_t st = 0; st < STAGES_PER_CHUNK; ++st, ++q) {
+          const uint32_t s = q % OG_STAGES;
+          if (q >= OG_STAGES) {
+            ok = __all_sync(0xffffffffu, wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 43));
+            if (!ok) break;
+          }
+          uint8_t *At = smem + s * OG_STAGE;
+          uint8_t *Bt = At + oz::S * A_PART;
+          const uint64_t k0 = (uint64_t)c * CHUNK + st * KC;
+          // A: 16 K values of row ar (two core rows)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const uint32_t kb = ah * 2 + h;
+            double v[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+              const uint64_t k = k0 + kb * 8 + kk;
+              v[kk] = (arow && k < a.N) ? __ldg(Asrc + k * am) : 0.0;
+            }
+            store_core_rows(At, A_PART, (ar / 8) * SBO + kb * LBO + (ar % 8) * 16, v, ae);
+          }
+          // B: 8 K values of row bj (one core row)
+          {
+            double v[8];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+              const uint64_t k = k0 + bq * 8 + kk;
+              v[kk] = (brow && k < a.N) ? __ldg(a.B + k * a.mb + J) : 0.0;
+            }
+            store_core_rows(Bt, B_PART, (bj / 8) * SBO + bq * LBO + (bj % 8) * 16, v, be);
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&br.full[s]);
+        }
+        if (!ok) break;
+        // drain this chunk's level sums into the FP64 accumulators
+        ok = __all_sync(0xffffffffu, wait(br.tfull, nchunk & 1, 44));
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+        for (int cg = 0; cg < 2; ++cg) {
+          float hi[16], lo[16];
+          combine16(tmem + ((quad * 32) << 16) + colh * 32 + cg * 16, hi, lo);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) acc[cg * 16 + i] += (double)hi[i] + (double)lo[i];
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(br.tempty);
+      }
+      if (!ok) break;
+      // partial of this item: [col][row], rows across lanes (coalesced)
+      double *dst = a.part + (uint64_t)it * TILE;
+      const uint32_t row = quad * 32 + lane;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) dst[(uint64_t)(colh * 32 + i) * 128 + row] = acc[i];
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == PW + 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+  }
+}
+
+// S_o[i + ma j] = 2^(aexp + bexp + 2) * sum over splits (fixed order)
+__global__ void k_oz_gram_final(const double *__restrict__ part, uint32_t na, uint32_t ma, uint32_t mb,
+                                uint32_t col_tiles, uint32_t splits, const int *__restrict__ aexp,
+                                const int *__restrict__ bexp, double *S0, double *S1) {
+  const uint64_t total = (uint64_t)na * ma * mb;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t R = (uint32_t)(t % (na * ma));
+    const uint32_t j = (uint32_t)(t / (na * ma));
+    const uint32_t rt = R / 128, r = R % 128, ct = j / OG_N, cj = j % OG_N;
+    const double *p = part + ((uint64_t)(rt * col_tiles + ct) * splits) * TILE + (uint64_t)cj * 128 + r;
+    double s = 0.0;
+    for (uint32_t sp = 0; sp < splits; ++sp) s += p[(uint64_t)sp * TILE];
+    const double v = s * oz::pow2(aexp[R] + bexp[j] + 2);
+    const uint32_t i = R % ma;
+    (R < ma ? S0 : S1)[i + (uint64_t)ma * j] = v;
+  }
+}
+
+// ---------------------------------------------------------------- rotation
+struct RotArgs {
+  const double *Y[3];
+  double *out[3];
+  uint32_t nops, m, mo;  // K = m inputs, mo output columns
+  uint64_t N;
+  const int *rexp;  // [nops][N] row exponents
+  const __nv_bfloat16 *Tdig;  // [col tile][K chunk][slice][OG_N x KC]
+  const int *texp;            // [mo]
+  uint32_t row_tiles, col_tiles, kchunks;
+  int *status;
+};
+
+__global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const Barriers br = carve(smem);
+  uint64_t *full_b = br.full_b;
+  const uint32_t tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+  const uint32_t n_items = a.nops * a.row_tiles * a.col_tiles;
+  if (tid == 0) {
+    for (int s = 0; s < OG_STAGES; ++s) {
+      mbar_init(&br.full[s], PW);
+      mbar_init(&full_b[s], 1);
+      mbar_init(&br.empty[s], 1);
+    }
+    mbar_init(br.tfull, 1);
+    mbar_init(br.tempty, PW);
+    *br.abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == PW + 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(br.tmem_slot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *br.tmem_slot;
+  auto wait = [&](uint64_t *bar, uint32_t parity, int code) -> bool {
+    if (*br.abort_flag) return false;
+    if (mbar_wait(bar, parity, a.status, code)) return true;
+    *br.abort_flag = 1;
+    return false;
+  };
+  auto decode = [&](uint32_t it, uint32_t &op, uint32_t &rt, uint32_t &ct) {
+    ct = it % a.col_tiles;
+    const uint32_t r = it / a.col_tiles;
+    rt = r % a.row_tiles;
+    op = r / a.row_tiles;
+  };
+
+  if (warp == PW) {
+    // ---------------- bulk copies of the sliced factor
+    if (lane == 0) {
+      uint32_t q = 0;
+      for (uint32_t it = blockIdx.x; it < n_items && !*br.abort_flag; it += gridDim.x) {
+        uint32_t op, rt, ct;
+        decode(it, op, rt, ct);
+        for (uint32_t kc = 0; kc < a.kchunks; ++kc, ++q) {
+          const uint32_t s = q % OG_STAGES;
+          if (q >= OG_STAGES && !wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 51)) break;
+          uint8_t *Bt = smem + s * OG_STAGE + oz::S * A_PART;
+          mbar_arrive_expect_tx(&full_b[s], oz::S * B_PART);
+          const __nv_bfloat16 *src = a.Tdig + ((uint64_t)(ct * a.kchunks + kc) * oz::S) * (OG_N * KC);
+          for (int sl = 0; sl < oz::S; ++sl) bulk_g2s(Bt + sl * B_PART, src + (uint64_t)sl * OG_N * KC, B_PART, &full_b[s]);
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp == PW + 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      uint32_t q = 0, li = 0;
+      bool ok = true;
+      for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
+        if (li >= 1 && !wait(br.tempty, (li - 1) & 1, 52)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (uint32_t kc = 0; kc < a.kchunks; ++kc, ++q) {
+          const uint32_t s = q % OG_STAGES;
+          if (!wait(&br.full[s], (q / OG_STAGES) & 1, 53) || !wait(&full_b[s], (q / OG_STAGES) & 1, 54)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t abase = smem_u32(smem + s * OG_STAGE);
+          const uint32_t bbase = abase + oz::S * A_PART;
+          for (uint32_t ks = 0; ks < KC / 16; ++ks) issue_levels(tmem, abase, bbase, ks, kc == 0 && ks == 0);
+          umma_commit(&br.empty[s]);
+        }
+        if (!ok) break;
+        umma_commit(br.tfull);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- producers: Y rows -> digit tiles (per-row exponents); epilogue
+    const uint32_t ar = tid % 128, ah = tid / 128;
+    const uint32_t quad = warp % 4, colh = warp / 4;
+    uint32_t q = 0, li = 0;
+    bool ok = true;
+    for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
+      uint32_t op, rt, ct;
+      decode(it, op, rt, ct);
+      const uint64_t row = (uint64_t)rt * 128 + ar;
+      const bool rin = row < a.N;
+      const double *src = rin ? a.Y[op] + row * a.m : nullptr;
+      const int re = rin ? a.rexp[(uint64_t)op * a.N + row] : 0;
+      for (uint32_t kc = 0; kc < a.kchunks; ++kc, ++q) {
+        const uint32_t s = q % OG_STAGES;
+        if (q >= OG_STAGES) {
+          ok = __all_sync(0xffffffffu, wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 55));
+          if (!ok) break;
+        }
+        uint8_t *At = smem + s * OG_STAGE;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t kb = ah * 2 + h;
+          double v[8];
+#pragma unroll
+          for (int kk = 0; kk < 8; ++kk) {
+            const uint32_t k = kc * KC + kb * 8 + kk;
+            v[kk] = (rin && k < a.m) ? __ldg(src + k) : 0.0;
+          }
+          store_core_rows(At, A_PART, (ar / 8) * SBO + kb * LBO + (ar % 8) * 16, v, re);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&br.full[s]);
+      }
+      if (!ok) break;
+      ok = __all_sync(0xffffffffu, wait(br.tfull, li & 1, 56));
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint64_t orow = (uint64_t)rt * 128 + quad * 32 + lane;
+      const int oe = orow < a.N ? a.rexp[(uint64_t)op * a.N + orow] : 0;
+#pragma unroll
+      for (int cg = 0; cg < 2; ++cg) {
+        float hi[16], lo[16];
+        combine16(tmem + ((quad * 32) << 16) + colh * 32 + cg * 16, hi, lo);
+        const uint32_t j0 = ct * OG_N + colh * 32 + cg * 16;
+        if (orow < a.N) {
+          double *dst = a.out[op] + orow * a.mo + j0;
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            if (j0 + i < a.mo) dst[i] = ((double)hi[i] + (double)lo[i]) * oz::pow2(oe + a.texp[j0 + i] + 2);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(br.tempty);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == PW + 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------- exponents and factor slices
+// per-column exponents of up to two N x m blocks (stacked), two-stage max
+__global__ void k_oz_colmax_partial(const double *__restrict__ A0, const double *__restrict__ A1, uint32_t na,
+                                    uint32_t m, uint64_t N, double *__restrict__ part) {
+  const uint64_t per = (N + gridDim.x - 1) / gridDim.x;
+  const uint64_t r0 = blockIdx.x * per, r1 = min(N, r0 + per);
+  for (uint32_t c = threadIdx.x; c < na * m; c += blockDim.x) {
+    const double *A = c < m ? A0 : A1;
+    const uint32_t j = c % m;
+    double mx = 0.0;
+    for (uint64_t i = r0; i < r1; ++i) mx = fmax(mx, fabs(A[i * m + j]));
+    part[(uint64_t)blockIdx.x * na * m + c] = mx;
+  }
+}
+
+__global__ void k_oz_colmax_final(const double *__restrict__ part, uint32_t nb, uint32_t cols, int *__restrict__ ex) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
+    double mx = 0.0;
+    for (uint32_t b = 0; b < nb; ++b) mx = fmax(mx, part[(uint64_t)b * cols + c]);
+    ex[c] = oz::exponent_of(mx);
+  }
+}
+
+// per-row exponents of the rotation inputs: one warp per row
+__global__ void k_oz_rowexp(const double *__restrict__ Y0, const double *__restrict__ Y1,
+                            const double *__restrict__ Y2, uint32_t nops, uint32_t m, uint64_t N,
+                            int *__restrict__ rexp) {
+  const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
+  const uint32_t lane = threadIdx.x % 32;
+  for (uint64_t w = blockIdx.x * (uint64_t)(blockDim.x / 32) + threadIdx.x / 32; w < (uint64_t)nops * N; w += nw) {
+    const uint32_t op = (uint32_t)(w / N);
+    const uint64_t row = w % N;
+    const double *Y = op == 0 ? Y0 : (op == 1 ? Y1 : Y2);
+    double mx = 0.0;
+    for (uint32_t j = lane; j < m; j += 32) mx = fmax(mx, fabs(Y[row * m + j]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) rexp[w] = oz::exponent_of(mx);
+  }
+}
+
+// slices of the m x mo column-major factor T as the B operand (rows = output
+// columns j, K = input index i) with per-column exponents
+__global__ void k_oz_build_t(const double *__restrict__ T, uint32_t m, uint32_t mo, uint32_t kchunks,
+                             int *__restrict__ texp, __nv_bfloat16 *__restrict__ out) {
+  const uint32_t ct = blockIdx.x;  // one block per 64-column tile
+  for (uint32_t jr = threadIdx.x; jr < OG_N; jr += blockDim.x) {
+    const uint32_t j = ct * OG_N + jr;
+    double mx = 0.0;
+    if (j < mo)
+      for (uint32_t i = 0; i < m; ++i) mx = fmax(mx, fabs(T[i + (uint64_t)m * j]));
+    if (j < mo) texp[j] = oz::exponent_of(mx);
+  }
+  __syncthreads();
+  const uint32_t per_slice = OG_N * KC;
+  for (uint32_t idx = threadIdx.x; idx < kchunks * per_slice; idx += blockDim.x) {
+    const uint32_t kc = idx / per_slice, rem = idx % per_slice;
+    const uint32_t jr = rem / KC, kk = rem % KC;
+    const uint32_t j = ct * OG_N + jr, i = kc * KC + kk;
+    int d[oz::S] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (j < mo && i < m) oz::digits(T[i + (uint64_t)m * j], texp[j], d);
+    const uint32_t pos = (jr / 8) * (KC / 8) * 64 + (kk / 8) * 64 + (jr % 8) * 8 + (kk % 8);
+    __nv_bfloat16 *base = out + ((uint64_t)(ct * kchunks + kc) * oz::S) * per_slice;
+#pragma unroll
+    for (int s = 0; s < oz::S; ++s) base[(uint64_t)s * per_slice + pos] = __int2bfloat16_rn(d[s]);
+  }
+}
+
+void set_attrs_once() {
+  static bool done = false;  // not a stream operation: stays out of graph captures
+  if (!done) {
+    GBFE_CUDA(cudaFuncSetAttribute(k_oz_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OG_SMEM));
+    GBFE_CUDA(cudaFuncSetAttribute(k_oz_rot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OG_SMEM));
+    done = true;
+  }
+}
+
+}  // namespace
+
+namespace gbfe {
+
+bool oz_gemm_supported(gbfe_ctx *ctx, uint32_t m) {
+  return ctx->cc_major >= 10 && m > 0 && m <= (uint32_t)oz::K_EXACT;
+}
+
+// S_o (ma x mb, column-major) = A_o^T B for o < na (na <= 2); A_o: N x ma, B: N x mb, row-major blocks
+void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, const double *B, uint32_t mb,
+             uint64_t N, double *const *S) {
+  GBFE_REQUIRE(na >= 1 && na <= 2 && ma > 0 && mb > 0, "oz_gram: bad shape");
+  set_attrs_once();
+  const uint32_t rows = na * ma;
+  const uint32_t row_tiles = (rows + 127) / 128, col_tiles = (mb + OG_N - 1) / OG_N;
+  const uint32_t chunks = (uint32_t)std::max<uint64_t>(1, (N + CHUNK - 1) / CHUNK);
+  const uint32_t tiles = row_tiles * col_tiles;
+  const uint32_t want = std::max<uint32_t>(1, (2 * (uint32_t)ctx->sm_count + tiles - 1) / tiles);
+  const uint32_t splits_req = std::min(chunks, want);
+  const uint32_t cps = (chunks + splits_req - 1) / splits_req;
+  const uint32_t splits = (chunks + cps - 1) / cps;
+  const uint32_t items = tiles * splits;
+  // exponents
+  const unsigned nb = (unsigned)std::min<uint64_t>(304, std::max<uint64_t>(1, N));
+  ctx->oz_exp.ensure((size_t)rows + mb);
+  ctx->red.ensure((size_t)nb * std::max(rows, mb));
+  k_oz_colmax_partial<<<nb, 256, 0, ctx->stream>>>(A[0], na > 1 ? A[1] : A[0], na, ma, N, ctx->red.p);
+  k_oz_colmax_final<<<(rows + 255) / 256, 256, 0, ctx->stream>>>(ctx->red.p, nb, rows, ctx->oz_exp.p);
+  k_oz_colmax_partial<<<nb, 256, 0, ctx->stream>>>(B, B, 1, mb, N, ctx->red.p);
+  k_oz_colmax_final<<<(mb + 255) / 256, 256, 0, ctx->stream>>>(ctx->red.p, nb, mb, ctx->oz_exp.p + rows);
+  count_launch(ctx, 4);
+  ctx->oz_part.ensure((size_t)items * TILE);
+  GramArgs args{A[0], na > 1 ? A[1] : A[0], na, ma, B, mb, N, ctx->oz_exp.p, ctx->oz_exp.p + rows, row_tiles,
+                col_tiles, splits, chunks, cps, ctx->oz_part.p, ctx->status.p};
+  const uint32_t grid = std::min<uint32_t>(items, (uint32_t)ctx->sm_count);
+  {
+    ProfScope prof(ctx, "gram_f64_oz", 2.0 * (double)N * rows * mb, 8.0 * (double)N * (rows + mb));
+    k_oz_gram<<<grid, OG_THREADS, OG_SMEM, ctx->stream>>>(args);
+    check_launch(ctx, "oz_gram");
+  }
+  const uint64_t total = (uint64_t)rows * mb;
+  k_oz_gram_final<<<grid_for(total, 256), 256, 0, ctx->stream>>>(ctx->oz_part.p, na, ma, mb, col_tiles, splits,
+                                                               ctx->oz_exp.p, ctx->oz_exp.p + rows, S[0],
+                                                               na > 1 ? S[1] : S[0]);
+  check_launch(ctx, "oz_gram_final");
+}
+
+// out_o (N x mo, row-major) = Y_o (N x m, row-major) T (m x mo, column-major) for o < nops (<= 3)
+void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const double *const *Y, double *const *out,
+               uint32_t nops, uint64_t N) {
+  GBFE_REQUIRE(nops >= 1 && nops <= 3 && m > 0 && m <= (uint32_t)oz::K_EXACT && mo > 0, "oz_rotate: bad shape");
+  set_attrs_once();
+  const uint32_t kchunks = (m + KC - 1) / KC, col_tiles = (mo + OG_N - 1) / OG_N;
+  const uint32_t row_tiles = (uint32_t)((N + 127) / 128);
+  ctx->oz_rexp.ensure((size_t)nops * N);
+  ctx->oz_exp.ensure(mo);
+  ctx->oz_tdig.ensure((size_t)col_tiles * kchunks * oz::S * OG_N * KC);
+  k_oz_rowexp<<<(unsigned)std::min<uint64_t>((nops * N + 7) / 8, (uint64_t)ctx->sm_count * 32), 256, 0,
+                ctx->stream>>>(Y[0], nops > 1 ? Y[1] : Y[0], nops > 2 ? Y[2] : Y[0], nops, m, N, ctx->oz_rexp.p);
+  k_oz_build_t<<<col_tiles, 256, 0, ctx->stream>>>(T, m, mo, kchunks, ctx->oz_exp.p, ctx->oz_tdig.p);
+  count_launch(ctx, 2);
+  RotArgs args{};
+  for (uint32_t o = 0; o < nops; ++o) {
+    args.Y[o] = Y[o];
+    args.out[o] = out[o];
+  }
+  args.nops = nops;
+  args.m = m;
+  args.mo = mo;
+  args.N = N;
+  args.rexp = ctx->oz_rexp.p;
+  args.Tdig = ctx->oz_tdig.p;
+  args.texp = ctx->oz_exp.p;
+  args.row_tiles = row_tiles;
+  args.col_tiles = col_tiles;
+  args.kchunks = kchunks;
+  args.status = ctx->status.p;
+  const uint32_t items = nops * row_tiles * col_tiles;
+  const uint32_t grid = std::min<uint32_t>(items, (uint32_t)ctx->sm_count);
+  ProfScope prof(ctx, "rotate_f64_oz", 2.0 * (double)N * m * mo * nops, 8.0 * (double)N * (m + mo) * nops);
+  k_oz_rot<<<grid, OG_THREADS, OG_SMEM, ctx->stream>>>(args);
+  check_launch(ctx, "oz_rotate");
+}
+
+}  // namespace gbfe

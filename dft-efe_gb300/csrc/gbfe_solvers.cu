@@ -656,8 +656,18 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   residual_filter(A, B, BInv, eig_h, X, degree, wl, wu, uu, st.Y.get(), prec, st.R.get(), &st.fw);
   apply_op(B, st.Y.get(), st.MY.get());
   apply_op(A, st.Y.get(), st.HY.get());
-  gram(ctx, st.Y.get(), st.MY.get(), st.SM.p);
-  gram(ctx, st.Y.get(), st.HY.get(), st.SH.p);
+  // FP64 Gram matrices and rotations: the sliced tensor-core products when
+  // the FP64 applies use them, else DGEMM
+  const bool oz_dense = ctx->fp64_tc && ctx->fp64_tc_dense && oz_gemm_supported(ctx, (uint32_t)m);
+  if (oz_dense) {
+    // S = (MY|HY)^T Y: the transposes of Y^T MY and Y^T HY (both symmetric)
+    const double *As[2] = {st.MY->d.p, st.HY->d.p};
+    double *Ss[2] = {st.SM.p, st.SH.p};
+    oz_gram(ctx, As, 2, (uint32_t)m, st.Y->d.p, (uint32_t)m, (uint64_t)N, Ss);
+  } else {
+    gram(ctx, st.Y.get(), st.MY.get(), st.SM.p);
+    gram(ctx, st.Y.get(), st.HY.get(), st.SH.p);
+  }
   int lwork = 0;
   GBFE_CUSOLVER(cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, &lwork));
   ctx->lwork.ensure(std::max(lwork, 1));
@@ -704,13 +714,20 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
                           m, &one, st.SM.p, m, st.SH.p, m));
   count_launch(ctx);
   const double *T = st.SH.p;
-  // rows times T: col-major (m x N) out = T^T * in
-  GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.Y->d.p, m, &zero, X->d.p, m));
-  GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.HY->d.p, m, &zero,
-                          st.HX->d.p, m));
-  GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.MY->d.p, m, &zero,
-                          st.MX->d.p, m));
-  count_launch(ctx, 3);
+  if (oz_dense) {
+    const double *in[3] = {st.Y->d.p, st.HY->d.p, st.MY->d.p};
+    double *out[3] = {X->d.p, st.HX->d.p, st.MX->d.p};
+    oz_rotate(ctx, T, (uint32_t)m, (uint32_t)m, in, out, 3, (uint64_t)N);
+  } else {
+    // rows times T: col-major (m x N) out = T^T * in
+    GBFE_CUBLAS(
+        cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.Y->d.p, m, &zero, X->d.p, m));
+    GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.HY->d.p, m, &zero,
+                            st.HX->d.p, m));
+    GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.MY->d.p, m, &zero,
+                            st.MX->d.p, m));
+    count_launch(ctx, 3);
+  }
   std::vector<double> nOnes(m, -1.0);
   DevVec d_no(m), d_e(m);
   d_no.set(ctx, nOnes.data(), m);
@@ -878,6 +895,52 @@ int gbfe_rayleigh_ritz(const gbfe_op *A, gbfe_mv *X, double *eigenvalues_host, g
   return rc != GBFE_OK ? rc : status;
 }
 
+int gbfe_mv_gram(const gbfe_mv *X, const gbfe_mv *Y, double *S_host) {
+  if (!X || !Y || !S_host) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = CTX_OF(X);
+  return gbfe_guard(ctx, [&] {
+    GBFE_REQUIRE(X->mesh == Y->mesh && X->dtype == GBFE_F64 && Y->dtype == GBFE_F64,
+                 "gram: X and Y must be FP64 blocks of one mesh");
+    const uint32_t mx = X->m, my = Y->m;
+    ctx->small.ensure((size_t)mx * my);
+    if (ctx->fp64_tc && ctx->fp64_tc_dense && oz_gemm_supported(ctx, mx)) {
+      const double *As[1] = {X->d.p};
+      double *Ss[1] = {ctx->small.p};
+      oz_gram(ctx, As, 1, mx, Y->d.p, my, X->mesh->n_dofs, Ss);
+    } else {
+      const double one = 1.0, zero = 0.0;
+      GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)mx, (int)my, (int)X->mesh->n_dofs, &one,
+                              X->d.p, (int)mx, Y->d.p, (int)my, &zero, ctx->small.p, (int)mx));
+      count_launch(ctx);
+    }
+    GBFE_CUDA(cudaMemcpyAsync(S_host, ctx->small.p, (size_t)mx * my * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int gbfe_mv_rotate(const gbfe_mv *X, const double *T_host, gbfe_mv *Y) {
+  if (!X || !T_host || !Y) return GBFE_ERR_ARG;
+  gbfe_ctx *ctx = CTX_OF(X);
+  return gbfe_guard(ctx, [&] {
+    GBFE_REQUIRE(X->mesh == Y->mesh && X->dtype == GBFE_F64 && Y->dtype == GBFE_F64 && X != Y,
+                 "rotate: X and Y must be distinct FP64 blocks of one mesh");
+    const uint32_t m = X->m, mo = Y->m;
+    DBuf<double> T;
+    T.upload(T_host, (size_t)m * mo, ctx->stream);
+    if (ctx->fp64_tc && ctx->fp64_tc_dense && oz_gemm_supported(ctx, m)) {
+      const double *in[1] = {X->d.p};
+      double *out[1] = {Y->d.p};
+      oz_rotate(ctx, T.p, m, mo, in, out, 1, X->mesh->n_dofs);
+    } else {
+      const double one = 1.0, zero = 0.0;
+      GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, (int)mo, (int)X->mesh->n_dofs, (int)m, &one,
+                              T.p, (int)m, X->d.p, (int)m, &zero, Y->d.p, (int)mo));
+      count_launch(ctx);
+    }
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
 int gbfe_eigen_residual_norms(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X, const double *eigenvalues,
                               double *norms_host) {
   if (!A || !B || !X || !eigenvalues || !norms_host) return GBFE_ERR_ARG;
@@ -932,13 +995,16 @@ int gbfe_ks_eigen_solve(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
     }
     uint32_t pass = 0;
     std::string msg;
-    const int saved_fp64 = ctx->fp64_tc;
-    ctx->fp64_tc = prm->fp64_apply ? 1 : 0;
     struct Restore {
       gbfe_ctx *c;
-      int v;
-      ~Restore() { c->fp64_tc = v; }
-    } restore{ctx, saved_fp64};
+      int tc, dense;
+      ~Restore() {
+        c->fp64_tc = tc;
+        c->fp64_tc_dense = dense;
+      }
+    } restore{ctx, ctx->fp64_tc, ctx->fp64_tc_dense};
+    ctx->fp64_tc = prm->fp64_apply ? 1 : 0;
+    ctx->fp64_tc_dense = prm->fp64_apply == 1 ? 1 : 0;
     if (!prm->faithful_passes) {
       status = ks_solve_fused(A, B, BInv, X, prm, wl, wu, uu, eigenvalues, residuals, passes_out, msg);
       if (status != GBFE_OK) ctx->last_error = msg.empty() ? "KS_MAX_PASS_ERROR: residual tolerance not reached" : msg;

@@ -58,6 +58,8 @@ SIGNATURES = {
     "gbfe_ctx_set_graphs": (i32, [p, i32]),
     "gbfe_autotune": (i32, [p, u32, C.c_char_p, C.c_size_t]),
     "gbfe_nonlocal_upload": (i32, [p, u32, p, p, p, p, C.POINTER(p)]),
+    "gbfe_mv_gram": (i32, [p, p, p]),
+    "gbfe_mv_rotate": (i32, [p, p, p]),
     "gbfe_nonlocal_destroy": (i32, [p]),
     "gbfe_nonlocal_apply": (i32, [p, p, p, p]),
     "gbfe_op_attach_nonlocal": (i32, [p, p]),

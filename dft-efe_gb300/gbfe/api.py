@@ -28,6 +28,7 @@ CPU.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from typing import Optional, Sequence
 
 import numpy as np
@@ -51,6 +52,10 @@ class LinAlgOpContext:
         if rc != 0:
             raise GBFEError(rc, f"gbfe_ctx_create(device={device}) failed")
         self.h = h
+        self._dependents = weakref.WeakSet()  # vectors / operators to free before the context
+
+    def _track(self, obj) -> None:
+        self._dependents.add(obj)
 
     def synchronize(self) -> None:
         check(self.lib.gbfe_ctx_synchronize(self.h), self.h, "synchronize")
@@ -71,7 +76,8 @@ class LinAlgOpContext:
         check(self.lib.gbfe_ctx_set_graphs(self.h, 1 if on else 0), self.h, "set_graphs")
 
     def set_fp64_apply(self, mode: int) -> None:
-        """0: FP64 FMA cell product; 1: FP64-accurate sliced tensor-core product."""
+        """0: FP64 FMA / DGEMM; 1: sliced tensor-core products for cell applies, Gram matrices and
+        rotations; 2: sliced cell products only."""
         check(self.lib.gbfe_ctx_set_fp64_apply(self.h, int(mode)), self.h, "set_fp64_apply")
 
     def set_profiling(self, on: bool) -> None:
@@ -96,6 +102,11 @@ class LinAlgOpContext:
 
     def close(self) -> None:
         if getattr(self, "h", None):
+            for obj in list(getattr(self, "_dependents", ())):
+                try:
+                    obj.close()
+                except Exception:
+                    pass
             self.lib.gbfe_ctx_destroy(self.h)
             self.h = None
 
@@ -161,6 +172,7 @@ class MultiVector:
         h = C.c_void_p()
         check(self.ctx.lib.gbfe_mv_create(basis.h, self.m, code, C.byref(h)), self.ctx.h, "mv_create")
         self.h = h
+        self.ctx._track(self)
         if init is not None:
             self.copy_from(init)
 
@@ -243,6 +255,7 @@ class CellMatrixOperatorContext(OperatorContext):
         check(self.ctx.lib.gbfe_cellmat_upload(basis.h, cons, _ptr(mats), flags, C.byref(h)), self.ctx.h,
               "cellmat_upload")
         self.h = h
+        self.ctx._track(self)
         self.mixed = mixed
         self.nonlocal_part = None
         if nonlocal_part is not None:
@@ -271,6 +284,7 @@ class AtomCenterNonLocalOpContextFE(OperatorContext):
         check(self.ctx.lib.gbfe_nonlocal_upload(basis.h, int(data.n_proj), _ptr(ppc), _ptr(pid), _ptr(cc), _ptr(v),
                                                 C.byref(h)), self.ctx.h, "nonlocal_upload")
         self.h = h
+        self.ctx._track(self)
         self._keep = None
         self.cons_h = basis.cons_h if use_constraints else None
 
@@ -281,6 +295,19 @@ class AtomCenterNonLocalOpContextFE(OperatorContext):
         if getattr(self, "h", None):
             self.ctx.lib.gbfe_nonlocal_destroy(self.h)
             self.h = None
+
+
+def gram(X: "MultiVector", Y: "MultiVector") -> np.ndarray:
+    """S = X^T Y (mx x my) on the device (DGEMM, or the sliced FP64 product in FP64 mode 1)."""
+    S = np.empty((Y.m, X.m))  # column-major mx x my == row-major my x mx
+    check(X.ctx.lib.gbfe_mv_gram(X.h, Y.h, _ptr(S)), X.ctx.h, "gram")
+    return S.T.copy()
+
+
+def rotate(X: "MultiVector", T: np.ndarray, Y: "MultiVector") -> None:
+    """Y = X T on the device, T of shape (X.m, Y.m)."""
+    Tc = np.asfortranarray(np.asarray(T, dtype=np.float64))
+    check(X.ctx.lib.gbfe_mv_rotate(X.h, C.c_void_p(Tc.ctypes.data), Y.h), X.ctx.h, "rotate")
 
 
 def autotune(op: "OperatorContext", m: int) -> list:
@@ -324,6 +351,7 @@ class IndexedCellMatrixOperatorContext(OperatorContext):
         check(self.ctx.lib.gbfe_cellmat_upload_indexed(basis.h, cons, n_mats, _ptr(mats), _ptr(idx), flags,
                                                        C.byref(h)), self.ctx.h, "cellmat_upload_indexed")
         self.h = h
+        self.ctx._track(self)
 
 
 class KohnShamOperatorContextFE(CellMatrixOperatorContext):
@@ -347,6 +375,7 @@ class CFEOverlapInverseOpContextGLL(OperatorContext):
         h = C.c_void_p()
         check(self.ctx.lib.gbfe_diag_upload(basis.h, basis.cons_h, _ptr(inv), C.byref(h)), self.ctx.h, "diag_upload")
         self.h = h
+        self.ctx._track(self)
 
 
 class OrthoEFEOverlapInverseOpContextGLL(OperatorContext):
@@ -361,6 +390,7 @@ class OrthoEFEOverlapInverseOpContextGLL(OperatorContext):
         check(self.ctx.lib.gbfe_diag_block_upload(basis.h, basis.cons_h, _ptr(inv), int(enr_begin), int(blk.shape[0]),
                                                   _ptr(blk), C.byref(h)), self.ctx.h, "diag_block_upload")
         self.h = h
+        self.ctx._track(self)
 
 
 class DiagonalOperatorContext(OperatorContext):
@@ -373,6 +403,7 @@ class DiagonalOperatorContext(OperatorContext):
         check(self.ctx.lib.gbfe_diag_upload(basis.h, basis.cons_h if use_constraints else None, _ptr(d), C.byref(h)),
               self.ctx.h, "diag_upload")
         self.h = h
+        self.ctx._track(self)
 
 
 class PreconditionerJacobi(OperatorContext):
@@ -384,6 +415,7 @@ class PreconditionerJacobi(OperatorContext):
         h = C.c_void_p()
         check(self.ctx.lib.gbfe_jacobi_upload(basis.h, _ptr(d), C.byref(h)), self.ctx.h, "jacobi_upload")
         self.h = h
+        self.ctx._track(self)
 
 
 def ResidualChebyshevFilterGEP(A, B, BInv, eigenvalues: Sequence[float], X: MultiVector, polynomialDegree: int,
@@ -460,7 +492,7 @@ class KohnShamEigenSolver:
         self.p.lanczos_steps, self.p.lanczos_seed = int(lanczos_steps), int(lanczos_seed)
         self.p.fixed_passes = 1 if fixed_passes else 0
         self.p.faithful_passes = 1 if faithful_passes else 0
-        self.p.fp64_apply = 1 if fp64_tensor else 0
+        self.p.fp64_apply = int(fp64_tensor)  # True / 1: sliced products everywhere; 2: cell products only
 
     def solve(self, H, X: MultiVector, M, MInv, eigenvalues: Optional[np.ndarray] = None):
         ev = np.zeros(X.m) if eigenvalues is None else np.ascontiguousarray(eigenvalues, dtype=np.float64).copy()

@@ -114,10 +114,13 @@ int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len
  * recurrence are captured once into a CUDA graph (second pass) and replayed
  * on every later pass; 0: launched one by one. */
 int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on);
-/* FP64 applies: 0 (default) FP64 FMA cell product; 1 the FP64-accurate
- * sliced tensor-core product (Ozaki-style splitting into eight 7-bit slices,
- * exact FP32 accumulation per level), for operators built with
- * GBFE_PREC_FP64_TENSOR. */
+/* FP64 arithmetic of the applies and subspace stages:
+ *   0 (default) FP64 FMA cell products, DGEMM Gram matrices and rotations;
+ *   1 FP64-accurate sliced tensor-core products (Ozaki-style splitting into
+ *     eight balanced 7-bit slices, exact FP32 accumulation per level): the
+ *     cell products of operators built with GBFE_PREC_FP64_TENSOR and the
+ *     Gram matrices / rotations of the fused ChFSI pass (m <= 512);
+ *   2 as 1 for the cell products only (Gram / rotations stay DGEMM). */
 int gbfe_ctx_set_fp64_apply(gbfe_ctx *ctx, int mode);
 /* number of kernels this context has launched so far */
 int gbfe_ctx_kernel_launches(const gbfe_ctx *ctx, uint64_t *count);
@@ -271,6 +274,14 @@ int gbfe_cholesky_gram_schmidt(const gbfe_op *B, gbfe_mv *X, gbfe_mv *X_ortho);
 /* RayleighRitzEigenSolver::solve, LAPACK branch
  * (RayleighRitzEigenSolver.t.cpp:233-301): X^T A X, syevd('V','L'), X Q. */
 int gbfe_rayleigh_ritz(const gbfe_op *A, gbfe_mv *X, double *eigenvalues_host, gbfe_mv *X_out);
+/* The two dense shapes of those stages, as building blocks:
+ * S = X^T Y (X: N x mx, Y: N x my; S mx x my column-major, host) -- the GEMM
+ * of computeXTransOpX (RayleighRitzEigenSolver.t.cpp:488-680) -- and
+ * Y = X T (T: m x mo column-major, host) -- the rotation gemm of
+ * RayleighRitzEigenSolver.t.cpp:233-301.  DGEMM, or with FP64 mode 1
+ * (gbfe_ctx_set_fp64_apply) the sliced tensor-core products (m <= 512). */
+int gbfe_mv_gram(const gbfe_mv *X, const gbfe_mv *Y, double *S_host);
+int gbfe_mv_rotate(const gbfe_mv *X, const double *T_host, gbfe_mv *Y);
 /* KohnShamEigenSolver::getLinearEigenSolveResidual
  * (KohnShamEigenSolver.t.cpp:574-684): ||A x_i - eps_i B x_i||_2. */
 int gbfe_eigen_residual_norms(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X,
@@ -297,8 +308,10 @@ typedef struct {
   uint32_t lanczos_steps;       /* Krylov dimension (reference default 20)    */
   uint64_t lanczos_seed;
   int      fixed_passes;        /* 1: run exactly max_passes passes           */
-  int      fp64_apply;          /* 0: FP64 FMA cell products; 1: the sliced
-                                   tensor-core FP64 product where available   */
+  int      fp64_apply;          /* as gbfe_ctx_set_fp64_apply, for this solve:
+                                   0 FP64 FMA / DGEMM; 1 sliced tensor-core
+                                   cell products, Gram matrices and rotations;
+                                   2 sliced cell products only                */
   int      faithful_passes;     /* 1: every pass repeats the reference's call
                                    sequence (filter with its own A X, B X;
                                    Cholesky-GS; Rayleigh-Ritz; residual with
