@@ -230,6 +230,41 @@ class CpuBaseline:
         self.tmp.cleanup()
 
 
+# BF16 tensor-core products per FP64-accurate sliced product (8 x 8 digit
+# pairs with s + t <= 9)
+SLICED_PRODUCTS = 36
+
+
+def roofline(name, st, fp64_peak_gflops):
+    """Roofline of one profiled kernel from its CUDA-event stats (algorithmic
+    flops / bytes per launch over the average launch time)."""
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() \
+        else {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+    n = max(1, st["launches"])
+    avg_ms = st["ms"] / n
+    flops = st["flops"] / n
+    tflops = flops / (avg_ms * 1e-3) / 1e12 if avg_ms > 0 else 0.0
+    gbs = st["bytes"] / n / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    base = {"kernel": name, "traffic": None, "launches": st["launches"], "avg_launch_ms": avg_ms,
+            "flops_per_launch": flops, "bytes_per_launch": st["bytes"] / n}
+    if name == "cell_apply_f64":
+        peak = fp64_peak_gflops / 1e3
+        return {**base, "bound": "fp64", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                "peak_source": "DFMA throughput probe run in this process (MEASURED_PEAKS.json has no FP64 figure)"}
+    if name.endswith("_oz"):
+        # FP64-accurate products on the BF16 tensor cores: the MMA work is
+        # SLICED_PRODUCTS BF16 products per algorithmic FP64 flop
+        # (timed inside a seconds-long solve: the sustained bf16 figure)
+        ach = tflops * SLICED_PRODUCTS
+        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0))
+        return {**base, "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "fp64_equivalent_tflops": tflops, "hbm_gbs": gbs,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (cuBLAS bf16 under the power cap)"}
+    peak = peaks["hbm_gbs"]
+    return {**base, "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "algorithmic_tflops": tflops, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"}
+
+
 def random_block_for(prob, cfg):
     import gbfe.mesh as M
 
@@ -319,6 +354,7 @@ def run_gpu(args, cfg_name, rank, world):
     st_mixed = ctx.kernel_stats("cell_apply_mixed")
     st_f64 = ctx.kernel_stats("cell_apply_f64")
     st_oz = ctx.kernel_stats("cell_apply_f64_oz")
+    st_dense = {k: ctx.kernel_stats(k) for k in ("gram_f64_oz", "rotate_f64_oz")}
     ctx.set_profiling(False)
 
     # e2e: the same solve through the C ABI with host buffers each step
@@ -338,7 +374,7 @@ def run_gpu(args, cfg_name, rank, world):
     fp64_peak = ctx.probe_fp64_peak()
     return dict(cfg=cfg, prob=prob, deg=deg, bounds=(wl, wu, uu), fp64_times=fp64_times, passes64=passes64,
                 rc64=rc64, lat=lat, errs=errs, passes=passes, ok=ok, t_total=t_total, launches=launches,
-                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
+                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, st_dense=st_dense, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
                 h2d=prob.n_dofs * m * 8, d2h=prob.n_dofs * m * 8 + 2 * m * 8)
 
 
@@ -650,26 +686,10 @@ def main():
     prob = r["prob"]
     value, t_step = aggregate_replicas(r["t_total"], args.steps, world)
     fp64_sps = 1.0 / float(np.median(r["fp64_times"]))
-    cand = {"cell_apply_f64": r["st_f64"], "cell_apply_mixed": r["st_mixed"], "cell_apply_f64_oz": r["st_oz"]}
+    cand = {"cell_apply_f64": r["st_f64"], "cell_apply_mixed": r["st_mixed"], "cell_apply_f64_oz": r["st_oz"],
+            **r["st_dense"]}
     dom = max(cand, key=lambda k: cand[k]["ms"])
-    st = cand[dom]
-    avg_ms = st["ms"] / max(1, st["launches"])
-    flops_per_launch = st["flops"] / max(1, st["launches"])
-    achieved = flops_per_launch / (avg_ms * 1e-3) / 1e12
-    if dom == "cell_apply_f64":
-        roof = {"kernel": dom, "bound": "fp64", "achieved": achieved, "peak": r["fp64_peak"] / 1e3,
-                "unit": "TFLOP/s", "frac": achieved / (r["fp64_peak"] / 1e3), "traffic": None,
-                "peak_source": "DFMA throughput probe run in this process (MEASURED_PEAKS.json has no FP64 figure)",
-                "launches": st["launches"], "avg_launch_ms": avg_ms, "flops_per_launch": flops_per_launch}
-    else:
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() \
-            else {"hbm_gbs": 6800.0}
-        gbs = st["bytes"] / max(1, st["launches"]) / (avg_ms * 1e-3) / 1e9
-        roof = {"kernel": dom, "bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": gbs / peaks["hbm_gbs"], "traffic": None, "launches": st["launches"],
-                "avg_launch_ms": avg_ms, "algorithmic_tflops": achieved,
-                "bytes_per_launch": st["bytes"] / max(1, st["launches"]),
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"}
+    roof = roofline(dom, cand[dom], r["fp64_peak"])
     others = {k: v for k, v in cand.items() if k != dom}
     e2e_sps = world / float(np.mean(r["e2e_lat"]))
     line = {

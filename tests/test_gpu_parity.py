@@ -418,8 +418,9 @@ def test_autotuned_tensor_core_shape(gpu_ctx, tmp_path, monkeypatch):
         ctx.check_status()
         assert rel_maxnorm(Yf.numpy(), Y.numpy()) <= TC_TOL
         assert cache.read_text().strip().splitlines() == lines
+        tuned = Yf.numpy()
     finally:
-        ctx.close()
+        ctx.close()  # also frees the vectors and operators made on it
     ctx2 = api.LinAlgOpContext(0)  # loads the cache
     try:
         basis = api.FEBasisManager.from_problem(ctx2, prob)
@@ -428,6 +429,6 @@ def test_autotuned_tensor_core_shape(gpu_ctx, tmp_path, monkeypatch):
         Yf2 = api.MultiVector(basis, 40, dtype=np.float32)
         H.apply(Xf, Yf2)
         ctx2.check_status()
-        assert np.array_equal(Yf2.numpy(), Yf.numpy())
+        assert np.array_equal(Yf2.numpy(), tuned)
     finally:
         ctx2.close()
