@@ -539,6 +539,12 @@ int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on) {
   return GBFE_OK;
 }
 
+int gbfe_ctx_set_small_eig(gbfe_ctx *ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 1) return GBFE_ERR_ARG;
+  ctx->small_eig_host = mode;
+  return GBFE_OK;
+}
+
 int gbfe_ctx_set_fp64_apply(gbfe_ctx *ctx, int mode) {
   if (!ctx || mode < 0 || mode > 2) return GBFE_ERR_ARG;
   ctx->fp64_tc = mode ? 1 : 0;

@@ -1,0 +1,167 @@
+// gbfe_host_eig.cpp -- dense symmetric eigen-decomposition on the host for
+// the small projected matrices of Rayleigh-Ritz (m x m, m <= a few hundred).
+//
+// The reference calls LAPACK dsyevd('V','L') here
+// (RayleighRitzEigenSolver.t.cpp:233-301).  On the GPU that routine is a long
+// chain of small launches with host round trips; for the m of the KS
+// workloads one host core finishes the same decomposition sooner.  Method
+// (Golub & Van Loan, Matrix Computations, sections 8.3.1 and 8.3.2):
+//   1. Householder reduction T = Q^T A Q to tridiagonal form, Q accumulated
+//      explicitly by applying the reflectors in reverse order;
+//   2. implicit symmetric QR steps with the Wilkinson shift on the unreduced
+//      trailing block, each a chase of Givens rotations G^T T G applied to the
+//      band of T and accumulated into Z = Q G_1 G_2 ...;
+//      an off-diagonal entry is set to zero once it is below
+//      eps (|t_ii| + |t_i+1,i+1|);
+//   3. eigenvalues ascending with their eigenvector columns.
+// Pure C++ (no intrinsics): identical code on x86 and Arm hosts.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <numeric>
+#include <vector>
+
+namespace gbfe {
+
+// a: n x n column-major; the lower triangle is read.  On success a holds the
+// orthonormal eigenvectors (column j belongs to w[j]) and w the eigenvalues in
+// ascending order.  Returns 0, or 1 if the QR iteration did not converge.
+int host_sym_eig(int n, double *a, double *w) {
+  if (n <= 0) return 0;
+  const size_t N = (size_t)n;
+  auto A = [&](std::vector<double> &M, int i, int j) -> double & { return M[(size_t)i + N * (size_t)j]; };
+  std::vector<double> T(N * N), Z(N * N, 0.0), v(N), p(N), q(N);
+  for (int j = 0; j < n; ++j)
+    for (int i = j; i < n; ++i) A(T, i, j) = A(T, j, i) = a[(size_t)i + N * j];
+
+  // ---- 1. Householder tridiagonalization; reflector k lives on rows k+1..n-1
+  std::vector<double> refl(N * N, 0.0), beta(N, 0.0);
+  for (int k = 0; k + 2 < n; ++k) {
+    const int L = n - k - 1;
+    double nx = 0.0;
+    for (int i = 0; i < L; ++i) {
+      v[i] = A(T, k + 1 + i, k);
+      nx += v[i] * v[i];
+    }
+    nx = std::sqrt(nx);
+    if (nx == 0.0) continue;
+    const double alpha = v[0] >= 0.0 ? -nx : nx;
+    v[0] -= alpha;
+    double vv = 0.0;
+    for (int i = 0; i < L; ++i) vv += v[i] * v[i];
+    if (vv == 0.0) continue;
+    const double b = 2.0 / vv;
+    // p = b A22 v;  q = p - (b/2)(v^T p) v;  A22 -= v q^T + q v^T
+    for (int i = 0; i < L; ++i) p[i] = 0.0;
+    for (int j = 0; j < L; ++j) {  // column-major: contiguous inner loop
+      const double vj = b * v[j];
+      const double *col = &A(T, k + 1, k + 1 + j);
+      for (int i = 0; i < L; ++i) p[i] += col[i] * vj;
+    }
+    double vp = 0.0;
+    for (int i = 0; i < L; ++i) vp += v[i] * p[i];
+    const double K = 0.5 * b * vp;
+    for (int i = 0; i < L; ++i) q[i] = p[i] - K * v[i];
+    for (int j = 0; j < L; ++j) {
+      double *col = &A(T, k + 1, k + 1 + j);
+      const double qj = q[j], vj = v[j];
+      for (int i = 0; i < L; ++i) col[i] -= v[i] * qj + q[i] * vj;
+    }
+    A(T, k + 1, k) = A(T, k, k + 1) = alpha;
+    for (int i = 1; i < L; ++i) A(T, k + 1 + i, k) = A(T, k, k + 1 + i) = 0.0;
+    for (int i = 0; i < L; ++i) refl[(size_t)k * N + i] = v[i];
+    beta[k] = b;
+  }
+  // Q = H_0 H_1 ... H_{n-3}, built as H_k Q for k descending
+  for (int i = 0; i < n; ++i) A(Z, i, i) = 1.0;
+  for (int k = n - 3; k >= 0; --k) {
+    if (beta[k] == 0.0) continue;
+    const int L = n - k - 1;
+    const double *vk = &refl[(size_t)k * N];
+    for (int j = k + 1; j < n; ++j) {
+      double s = 0.0;
+      for (int i = 0; i < L; ++i) s += vk[i] * A(Z, k + 1 + i, j);
+      s *= beta[k];
+      for (int i = 0; i < L; ++i) A(Z, k + 1 + i, j) -= s * vk[i];
+    }
+  }
+
+  // ---- 2. implicit symmetric QR with Wilkinson shifts
+  const double eps = std::ldexp(1.0, -53);
+  auto negligible = [&](int i) {  // t_{i+1,i}
+    return std::fabs(A(T, i + 1, i)) <= eps * (std::fabs(A(T, i, i)) + std::fabs(A(T, i + 1, i + 1)));
+  };
+  auto rotate = [&](int k, double c, double s, int lo, int hi) {
+    // T <- G^T T G on rows / columns k, k+1 (band entries lo..hi only); Z <- Z G
+    const int i0 = std::max(lo, k - 1), i1 = std::min(hi, k + 2);
+    for (int j = i0; j <= i1; ++j) {
+      const double x = A(T, k, j), y = A(T, k + 1, j);
+      A(T, k, j) = c * x - s * y;
+      A(T, k + 1, j) = s * x + c * y;
+    }
+    for (int i = i0; i <= i1; ++i) {
+      const double x = A(T, i, k), y = A(T, i, k + 1);
+      A(T, i, k) = c * x - s * y;
+      A(T, i, k + 1) = s * x + c * y;
+    }
+    for (int i = 0; i < n; ++i) {
+      const double x = A(Z, i, k), y = A(Z, i, k + 1);
+      A(Z, i, k) = c * x - s * y;
+      A(Z, i, k + 1) = s * x + c * y;
+    }
+  };
+  auto givens = [](double x, double z, double &c, double &s) {
+    // [c s; -s c]^T [x; z] = [r; 0]
+    if (z == 0.0) {
+      c = 1.0;
+      s = 0.0;
+    } else if (std::fabs(z) > std::fabs(x)) {
+      const double t = -x / z;
+      s = 1.0 / std::sqrt(1.0 + t * t);
+      c = s * t;
+    } else {
+      const double t = -z / x;
+      c = 1.0 / std::sqrt(1.0 + t * t);
+      s = c * t;
+    }
+  };
+  int hi = n - 1;
+  long iter = 0;
+  const long max_iter = 60L * n;
+  while (hi > 0) {
+    if (negligible(hi - 1)) {
+      A(T, hi, hi - 1) = A(T, hi - 1, hi) = 0.0;
+      --hi;
+      continue;
+    }
+    if (++iter > max_iter) return 1;
+    int lo = hi - 1;
+    while (lo > 0 && !negligible(lo - 1)) --lo;
+    if (lo > 0) A(T, lo, lo - 1) = A(T, lo - 1, lo) = 0.0;
+    const double tnn = A(T, hi, hi), tn1 = A(T, hi, hi - 1);
+    const double dd = 0.5 * (A(T, hi - 1, hi - 1) - tnn);
+    const double mu = tnn - tn1 * tn1 / (dd + (dd >= 0.0 ? 1.0 : -1.0) * std::hypot(dd, tn1));
+    double x = A(T, lo, lo) - mu, z = A(T, lo + 1, lo);
+    for (int k = lo; k < hi; ++k) {
+      double c, s;
+      givens(x, z, c, s);
+      rotate(k, c, s, lo, hi);
+      if (k + 1 < hi) {
+        x = A(T, k + 1, k);
+        z = A(T, k + 2, k);
+      }
+    }
+  }
+
+  // ---- 3. ascending order
+  std::vector<int> ord(N);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int i, int j) { return A(T, i, i) < A(T, j, j); });
+  for (int j = 0; j < n; ++j) {
+    w[j] = A(T, ord[j], ord[j]);
+    for (int i = 0; i < n; ++i) a[(size_t)i + N * j] = A(Z, i, ord[j]);
+  }
+  return 0;
+}
+
+}  // namespace gbfe

@@ -159,6 +159,7 @@ struct gbfe_ctx {
   int fp64_tc = 0;           // 1: FP64 applies use the sliced tensor-core product when built
   int fp64_tc_dense = 1;     // with fp64_tc: the Gram / rotation stages use the sliced products too
   int cc_major = 0;          // compute capability of the device
+  int small_eig_host = 1;    // m x m eigenproblems of Rayleigh-Ritz on the host (m <= 128)
   gbfe::DBuf<int> oz_exp, oz_rexp;  // sliced products: column / row exponents
   gbfe::DBuf<double> oz_part;       // per-item Gram partials
   gbfe::DBuf<__nv_bfloat16> oz_tdig;  // slices of the rotation factor
@@ -321,6 +322,8 @@ void nonlocal_project(const gbfe_nl *nl, const gbfe_mv *X);
 void nonlocal_add(const gbfe_nl *nl, uint32_t m, int dtype, void *Yc);
 void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log);
 bool oz_supported(const gbfe_mesh *me);
+// dense symmetric eigen-decomposition on the host (gbfe_host_eig.cpp)
+int host_sym_eig(int n, double *a, double *w);
 // FP64-accurate sliced tensor-core products of the subspace stages (gbfe_ozgemm.cu)
 bool oz_gemm_supported(gbfe_ctx *ctx, uint32_t m);
 void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, const double *B, uint32_t mb,

@@ -261,6 +261,46 @@ int cholesky_gs_impl(const gbfe_op *B, gbfe_mv *X, gbfe_mv *Xo, std::string &msg
   return GBFE_OK;
 }
 
+// Eigen-decomposition of the m x m symmetric device matrix dA (lower triangle
+// read), the syevd('V','L') of RayleighRitzEigenSolver.t.cpp:233-301: on
+// return dA holds the eigenvectors (columns) and eig_h the eigenvalues,
+// ascending.  For m <= SMALL_EIG_HOST_MAX and ctx->small_eig_host the
+// decomposition runs on the host (gbfe_host_eig.cpp: one copy down, one up),
+// else in cuSOLVER's syevd (a chain of small launches for small m).
+constexpr int SMALL_EIG_HOST_MAX = 128;
+
+int small_syevd(gbfe_ctx *ctx, int m, double *dA, double *eig_h, std::string &msg) {
+  if (ctx->small_eig_host && m <= SMALL_EIG_HOST_MAX) {
+    std::vector<double> h((size_t)m * m);
+    GBFE_CUDA(cudaMemcpyAsync(h.data(), dA, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (host_sym_eig(m, h.data(), eig_h) != 0) {
+      msg = "LAPACK_ERROR: FAILED_STANDARD_EIGENPROBLEM (QR iteration did not converge)";
+      return GBFE_ERR_LAPACK;
+    }
+    // pageable source: the call returns once the data is staged
+    GBFE_CUDA(cudaMemcpyAsync(dA, h.data(), h.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    return GBFE_OK;
+  }
+  DevVec W(m);
+  int lwork = 0;
+  GBFE_CUSOLVER(cusolverDnDsyevd_bufferSize(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, dA, m,
+                                            W.b.p, &lwork));
+  ctx->lwork.ensure(std::max(lwork, 1));
+  ctx->info.ensure(1);
+  GBFE_CUSOLVER(cusolverDnDsyevd(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, dA, m, W.b.p,
+                                 ctx->lwork.p, lwork, ctx->info.p));
+  count_launch(ctx);
+  int info = 0;
+  GBFE_CUDA(cudaMemcpyAsync(&info, ctx->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  W.get(ctx, eig_h, m);
+  if (info != 0) {
+    msg = "LAPACK_ERROR: FAILED_STANDARD_EIGENPROBLEM (syevd info " + std::to_string(info) + ")";
+    return GBFE_ERR_LAPACK;
+  }
+  return GBFE_OK;
+}
+
 int rayleigh_ritz_impl(const gbfe_op *A, gbfe_mv *X, double *eig_h, gbfe_mv *Xout, std::string &msg,
                        gbfe_mv *AX_keep = nullptr) {
   gbfe_ctx *ctx = X->mesh->ctx;
@@ -275,22 +315,8 @@ int rayleigh_ritz_impl(const gbfe_op *A, gbfe_mv *X, double *eig_h, gbfe_mv *Xou
   ctx->small.ensure((size_t)m * m);
   double *S = ctx->small.p;
   gram(ctx, X, AX, S);
-  DevVec W(m);
-  int lwork = 0;
-  GBFE_CUSOLVER(cusolverDnDsyevd_bufferSize(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)m,
-                                            S, (int)m, W.b.p, &lwork));
-  ctx->lwork.ensure(std::max(lwork, 1));
-  ctx->info.ensure(1);
-  GBFE_CUSOLVER(cusolverDnDsyevd(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)m, S, (int)m,
-                                 W.b.p, ctx->lwork.p, lwork, ctx->info.p));
-  count_launch(ctx);
-  int info = 0;
-  GBFE_CUDA(cudaMemcpyAsync(&info, ctx->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  W.get(ctx, eig_h, m);
-  if (info != 0) {
-    msg = "LAPACK_ERROR: FAILED_STANDARD_EIGENPROBLEM (syevd info " + std::to_string(info) + ")";
-    return GBFE_ERR_LAPACK;
-  }
+  const int rc = small_syevd(ctx, (int)m, S, eig_h, msg);
+  if (rc != GBFE_OK) return rc;
   // Psi (col-major m x N) = Q^T X   (gemm('T','N') of the reference)
   const double one = 1.0, zero = 0.0;
   GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, (int)m, (int)X->mesh->n_dofs, (int)m, &one, S,
@@ -665,9 +691,12 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
     double *Ss[2] = {st.SM.p, st.SH.p};
     oz_gram(ctx, As, 2, (uint32_t)m, st.Y->d.p, (uint32_t)m, (uint64_t)N, Ss);
   } else {
+    ProfScope prof(ctx, "gram_f64_dgemm", 4.0 * (double)N * m * m, 24.0 * (double)N * m);
     gram(ctx, st.Y.get(), st.MY.get(), st.SM.p);
     gram(ctx, st.Y.get(), st.HY.get(), st.SH.p);
   }
+  // potrf, L^-1 S_H L^-T, syevd, L^-T V: the m x m stages, timed as one block
+  auto eig_prof = std::make_unique<ProfScope>(ctx, "eig_small_f64", 0.0, 0.0);
   int lwork = 0;
   GBFE_CUSOLVER(cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, &lwork));
   ctx->lwork.ensure(std::max(lwork, 1));
@@ -696,29 +725,22 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, m,
                           m, &one, st.SM.p, m, st.SH.p, m));
   count_launch(ctx, 2);
-  DevVec W(m);
-  GBFE_CUSOLVER(cusolverDnDsyevd_bufferSize(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m,
-                                            st.SH.p, m, W.b.p, &lwork));
-  ctx->lwork.ensure(std::max(lwork, 1));
-  GBFE_CUSOLVER(cusolverDnDsyevd(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, st.SH.p, m,
-                                 W.b.p, ctx->lwork.p, lwork, ctx->info.p));
-  count_launch(ctx);
-  GBFE_CUDA(cudaMemcpyAsync(&info, ctx->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  W.get(ctx, eig_h, m);
-  if (info != 0) {
-    msg = "LAPACK_ERROR: FAILED_STANDARD_EIGENPROBLEM (syevd info " + std::to_string(info) + ")";
-    return GBFE_ERR_LAPACK;
+  {
+    const int rc = small_syevd(ctx, m, st.SH.p, eig_h, msg);
+    if (rc != GBFE_OK) return rc;
   }
   // T = L^-T V (in place in SH)
   GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, m,
                           m, &one, st.SM.p, m, st.SH.p, m));
   count_launch(ctx);
+  eig_prof.reset();
   const double *T = st.SH.p;
   if (oz_dense) {
     const double *in[3] = {st.Y->d.p, st.HY->d.p, st.MY->d.p};
     double *out[3] = {X->d.p, st.HX->d.p, st.MX->d.p};
     oz_rotate(ctx, T, (uint32_t)m, (uint32_t)m, in, out, 3, (uint64_t)N);
   } else {
+    ProfScope prof(ctx, "rotate_f64_dgemm", 6.0 * (double)N * m * m, 48.0 * (double)N * m);
     // rows times T: col-major (m x N) out = T^T * in
     GBFE_CUBLAS(
         cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.Y->d.p, m, &zero, X->d.p, m));

@@ -75,6 +75,10 @@ class LinAlgOpContext:
     def set_graphs(self, on: bool) -> None:
         check(self.lib.gbfe_ctx_set_graphs(self.h, 1 if on else 0), self.h, "set_graphs")
 
+    def set_small_eig(self, on_host: bool) -> None:
+        """Rayleigh-Ritz m x m eigenproblems on the host (m <= 128, default) or in cuSOLVER."""
+        check(self.lib.gbfe_ctx_set_small_eig(self.h, 1 if on_host else 0), self.h, "set_small_eig")
+
     def set_fp64_apply(self, mode: int) -> None:
         """0: FP64 FMA / DGEMM; 1: sliced tensor-core products for cell applies, Gram matrices and
         rotations; 2: sliced cell products only."""

@@ -34,7 +34,7 @@ def nvcc() -> str:
 
 
 def sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
 def _stale(target: Path, deps: list[Path]) -> bool:
@@ -48,7 +48,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     OBJDIR.mkdir(exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
     srcs = sources()
-    objs = [OBJDIR / (s.stem + ".o") for s in srcs]
+    objs = [OBJDIR / (s.name.replace(".", "_") + ".o") for s in srcs]
     nv = nvcc()
 
     def compile_one(pair):

@@ -114,6 +114,11 @@ int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len
  * recurrence are captured once into a CUDA graph (second pass) and replayed
  * on every later pass; 0: launched one by one. */
 int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on);
+/* The m x m symmetric eigenproblems of Rayleigh-Ritz (syevd('V','L') in
+ * RayleighRitzEigenSolver.t.cpp:233-301): 1 (default) on the host for
+ * m <= 128 (Householder tridiagonalization + implicit QR, one copy each way);
+ * 0 cuSOLVER syevd on the device. */
+int gbfe_ctx_set_small_eig(gbfe_ctx *ctx, int mode);
 /* FP64 arithmetic of the applies and subspace stages:
  *   0 (default) FP64 FMA cell products, DGEMM Gram matrices and rotations;
  *   1 FP64-accurate sliced tensor-core products (Ozaki-style splitting into

@@ -432,3 +432,32 @@ def test_autotuned_tensor_core_shape(gpu_ctx, tmp_path, monkeypatch):
         assert np.array_equal(Yf2.numpy(), tuned)
     finally:
         ctx2.close()
+
+
+def test_small_eigenproblem_host_and_cusolver_agree(gpu_ctx, small_problem):
+    """Rayleigh-Ritz with the m x m eigenproblem on the host (default) and in
+    cuSOLVER syevd: eigenvalues within 1e-12 Ha; fused KS solves within 1e-10 Ha."""
+    from gbfe import api
+
+    p = small_problem
+    basis, H, Mo, Mi, s, oH, oM, oMi = _setup(gpu_ctx, p)
+    X0 = M.random_block(p.n_dofs, 12, 7)
+    out = {}
+    for host in (True, False):
+        gpu_ctx.set_small_eig(host)
+        try:
+            X = api.MultiVector(basis, 12, init=X0)
+            Xo = api.MultiVector(basis, 12)
+            Xr = api.MultiVector(basis, 12)
+            api.OrthonormalizationFunctions.CholeskyGramSchmidt(X, Xo, Mo)
+            eig = api.RayleighRitzEigenSolver.solve(H, Xo, Xr)
+            X2 = api.MultiVector(basis, 12, init=X0)
+            b = s.lanczos_bounds(oH, oM, oMi)
+            bounds = (b[0], b[0] + 0.1 * (b[1] - b[0]), b[1] + b[2] / 10)
+            rc, eks, _, _ = api.KohnShamEigenSolver(8, 12, 40, 1e-9, bounds=bounds).solve(H, X2, Mo, Mi)
+            assert rc == 0
+            out[host] = (np.asarray(eig), eks)
+        finally:
+            gpu_ctx.set_small_eig(True)
+    assert np.abs(out[True][0] - out[False][0]).max() <= 1e-12
+    assert np.abs(out[True][1][:8] - out[False][1][:8]).max() <= 1e-10
