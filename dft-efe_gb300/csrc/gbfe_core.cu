@@ -139,6 +139,30 @@ __global__ void k_assemble(const TC *__restrict__ Yc, uint32_t m, uint64_t n_dof
   }
 }
 
+// Assembly of a FP32 cell-wise result with one Chebyshev recurrence step fused
+// in (homogeneous Dirichlet rows only): with S the assembled A B^-1 RN,
+//   R = alpha1 S + (-c alpha1) RN + alpha2 R + (alpha1 eF2[j]) Y
+// in the operation order of the separate step kernel.
+__global__ void k_assemble_cheb(const float *__restrict__ Yc, uint32_t m, uint64_t n_dofs,
+                                const uint32_t *__restrict__ slot_ptr, const uint32_t *__restrict__ slot,
+                                const uint8_t *__restrict__ is_row, const double *__restrict__ coef,
+                                const float *__restrict__ RN, float *__restrict__ R, const double *__restrict__ eF2,
+                                const float *__restrict__ Y) {
+  const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
+  const uint64_t total = n_dofs * m;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = t / m;
+    const uint32_t v = (uint32_t)(t - i * m);
+    float acc = 0.f;
+    if (!(is_row && is_row[i]))
+      for (uint32_t p = slot_ptr[i], e = slot_ptr[i + 1]; p < e; ++p) acc = acc + Yc[(uint64_t)slot[p] * m + v];
+    const float s1 = (float)alpha1 * acc + (float)(-c * alpha1) * RN[t];
+    const float r = s1 + (float)alpha2 * R[t];
+    R[t] = r + (float)(alpha1 * eF2[v]) * Y[t];
+  }
+}
+
 // Diagonal operator with the constraint epilogue fused in.
 template <class T>
 __global__ void k_diag_apply(const T *__restrict__ X, uint32_t m, uint64_t n_dofs, const double *__restrict__ d,
@@ -371,6 +395,27 @@ void assemble_f32(const gbfe_op *op, float *Yc, gbfe_mv *Y) {
   assemble_cells(op->mesh, op->cons, GBFE_F32, Yc, Y);
 }
 
+bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_mv *R, const double *coef,
+                       const double *eF2, const gbfe_mv *Y) {
+  gbfe_mesh *me = A->mesh;
+  gbfe_ctx *ctx = me->ctx;
+  const gbfe_cons *c = BInv->cons;
+  if (RN->dtype != GBFE_F32 || A->kind != OP_CELL || !(A->prec & GBFE_PREC_MIXED) || A->nl || !ctx->use_tc ||
+      ctx->tc_version != 2 || !A->tc_aoff.p || BInv->kind != OP_DIAG || BInv->mesh != me || A->cons != c ||
+      (c && !c->pure_dirichlet) || RN->m == 0)
+    return false;
+  const uint32_t m = RN->m;
+  constraints_p2c(ctx, c, RN);  // BInv's parent-to-child on its input, as apply_op does
+  A->cellbuf_f32.ensure((size_t)me->total_cell_dofs * m);
+  cell_apply_tc(A, RN, A->cellbuf_f32.p, BInv->diag.p, c ? c->is_row.p : nullptr);
+  const uint64_t n = (uint64_t)me->n_dofs * m;
+  k_assemble_cheb<<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p,
+                                                               me->slot.p, c ? c->is_row.p : nullptr, coef, RN->f.p,
+                                                               R->f.p, eF2, Y->f.p);
+  check_launch(ctx, "assemble_cheb");
+  return true;
+}
+
 void convert_mv(gbfe_ctx *ctx, const gbfe_mv *src, gbfe_mv *dst) {
   const uint64_t n = src->count();
   if (src->dtype == dst->dtype) {
@@ -536,6 +581,12 @@ int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len
 int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on) {
   if (!ctx) return GBFE_ERR_ARG;
   ctx->use_graphs = on ? 1 : 0;
+  return GBFE_OK;
+}
+
+int gbfe_ctx_set_fused_filter(gbfe_ctx *ctx, int on) {
+  if (!ctx || on < 0 || on > 1) return GBFE_ERR_ARG;
+  ctx->fuse_filter = on;
   return GBFE_OK;
 }
 

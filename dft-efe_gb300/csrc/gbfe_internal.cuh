@@ -160,7 +160,9 @@ struct gbfe_ctx {
   int fp64_tc_dense = 1;     // with fp64_tc: the Gram / rotation stages use the sliced products too
   int cc_major = 0;          // compute capability of the device
   int small_eig_host = 1;    // m x m eigenproblems of Rayleigh-Ritz on the host (m <= 128)
+  int fuse_filter = 1;       // mixed filter: B^-1 in the tensor-core gather, step fused into the assembly
   gbfe::DBuf<int> oz_exp, oz_rexp;  // sliced products: column / row exponents
+  gbfe::DBuf<int> oz_ipart;         // partial exponent maxima
   gbfe::DBuf<double> oz_part;       // per-item Gram partials
   gbfe::DBuf<__nv_bfloat16> oz_tdig;  // slices of the rotation factor
 };
@@ -314,7 +316,14 @@ void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
 void build_mixed_mats(gbfe_op *op);
 void build_tc_mats(gbfe_op *op);
 bool tc_supported(const gbfe_mesh *me);
-void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc);
+void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const double *xscale = nullptr,
+                   const uint8_t *xzero = nullptr);
+// one step of the mixed Chebyshev recurrence in two launches:
+//   R = alpha1 (A B^-1 RN - c RN) + alpha2 R + alpha1 eF2[j] Y
+// (B^-1 applied in the tensor-core gather, the step fused into the assembly);
+// returns false (nothing launched) where the operators do not allow it
+bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_mv *R, const double *coef,
+                       const double *eF2, const gbfe_mv *Y);
 // nonlocal part: W = V * (sum over slots of C_c X_c) and Yc += C_c^T W
 // Y = assembled cell-wise buffer Yc with the constraint epilogue of `cons`
 void assemble_cells(gbfe_mesh *me, const gbfe_cons *cons, int dtype, const void *Yc, gbfe_mv *Y);

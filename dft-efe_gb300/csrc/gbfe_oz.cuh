@@ -27,6 +27,17 @@ __device__ __forceinline__ int exponent_of(double vmax) {
   return e;
 }
 
+// exponent_of(|v|) from the bits alone (integer pipe): for a normal double of
+// biased exponent E, |v| = 1.f 2^(E-1023) < 2^(E-1022).  Zero / subnormal
+// give EXP_NONE, so max() over a set equals exponent_of(max |v|) whenever the
+// set has a normal entry; finish with exp_or_zero().
+constexpr int EXP_NONE = -100000;
+__device__ __forceinline__ int exp_bits(double v) {
+  const int E = (int)(((uint64_t)__double_as_longlong(v) >> 52) & 0x7ff);
+  return E == 0 ? EXP_NONE : E - 1022;
+}
+__device__ __forceinline__ int exp_or_zero(int e) { return e == EXP_NONE ? 0 : e; }
+
 // balanced digits of v (|v| < 2^e): d[0] most significant
 __device__ __forceinline__ void digits(double v, int e, int *d) {
   const uint64_t bits = (uint64_t)__double_as_longlong(v);

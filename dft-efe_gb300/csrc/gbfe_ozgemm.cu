@@ -479,25 +479,26 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
 }
 
 // ---------------------------------------------------------------- exponents and factor slices
-// per-column exponents of up to two N x m blocks (stacked), two-stage max
+// per-column exponents of up to two N x m blocks (stacked), two-stage max of
+// the exponent bits (integer instructions: the FP64 pipe is the slow one)
 __global__ void k_oz_colmax_partial(const double *__restrict__ A0, const double *__restrict__ A1, uint32_t na,
-                                    uint32_t m, uint64_t N, double *__restrict__ part) {
+                                    uint32_t m, uint64_t N, int *__restrict__ part) {
   const uint64_t per = (N + gridDim.x - 1) / gridDim.x;
   const uint64_t r0 = blockIdx.x * per, r1 = min(N, r0 + per);
   for (uint32_t c = threadIdx.x; c < na * m; c += blockDim.x) {
     const double *A = c < m ? A0 : A1;
     const uint32_t j = c % m;
-    double mx = 0.0;
-    for (uint64_t i = r0; i < r1; ++i) mx = fmax(mx, fabs(A[i * m + j]));
+    int mx = oz::EXP_NONE;
+    for (uint64_t i = r0; i < r1; ++i) mx = max(mx, oz::exp_bits(A[i * m + j]));
     part[(uint64_t)blockIdx.x * na * m + c] = mx;
   }
 }
 
-__global__ void k_oz_colmax_final(const double *__restrict__ part, uint32_t nb, uint32_t cols, int *__restrict__ ex) {
+__global__ void k_oz_colmax_final(const int *__restrict__ part, uint32_t nb, uint32_t cols, int *__restrict__ ex) {
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
-    double mx = 0.0;
-    for (uint32_t b = 0; b < nb; ++b) mx = fmax(mx, part[(uint64_t)b * cols + c]);
-    ex[c] = oz::exponent_of(mx);
+    int mx = oz::EXP_NONE;
+    for (uint32_t b = 0; b < nb; ++b) mx = max(mx, part[(uint64_t)b * cols + c]);
+    ex[c] = oz::exp_or_zero(mx);
   }
 }
 
@@ -509,13 +510,12 @@ __global__ void k_oz_rowexp(const double *__restrict__ Y0, const double *__restr
   const uint32_t lane = threadIdx.x % 32;
   for (uint64_t w = blockIdx.x * (uint64_t)(blockDim.x / 32) + threadIdx.x / 32; w < (uint64_t)nops * N; w += nw) {
     const uint32_t op = (uint32_t)(w / N);
-    const uint64_t row = w % N;
+    const uint64_t row = w - (uint64_t)op * N;
     const double *Y = op == 0 ? Y0 : (op == 1 ? Y1 : Y2);
-    double mx = 0.0;
-    for (uint32_t j = lane; j < m; j += 32) mx = fmax(mx, fabs(Y[row * m + j]));
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if (lane == 0) rexp[w] = oz::exponent_of(mx);
+    int mx = oz::EXP_NONE;
+    for (uint32_t j = lane; j < m; j += 32) mx = max(mx, oz::exp_bits(Y[row * m + j]));
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 0) rexp[w] = oz::exp_or_zero(mx);
   }
 }
 
@@ -580,11 +580,11 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
   // exponents
   const unsigned nb = (unsigned)std::min<uint64_t>(304, std::max<uint64_t>(1, N));
   ctx->oz_exp.ensure((size_t)rows + mb);
-  ctx->red.ensure((size_t)nb * std::max(rows, mb));
-  k_oz_colmax_partial<<<nb, 256, 0, ctx->stream>>>(A[0], na > 1 ? A[1] : A[0], na, ma, N, ctx->red.p);
-  k_oz_colmax_final<<<(rows + 255) / 256, 256, 0, ctx->stream>>>(ctx->red.p, nb, rows, ctx->oz_exp.p);
-  k_oz_colmax_partial<<<nb, 256, 0, ctx->stream>>>(B, B, 1, mb, N, ctx->red.p);
-  k_oz_colmax_final<<<(mb + 255) / 256, 256, 0, ctx->stream>>>(ctx->red.p, nb, mb, ctx->oz_exp.p + rows);
+  ctx->oz_ipart.ensure((size_t)nb * std::max(rows, mb));
+  k_oz_colmax_partial<<<nb, 256, 0, ctx->stream>>>(A[0], na > 1 ? A[1] : A[0], na, ma, N, ctx->oz_ipart.p);
+  k_oz_colmax_final<<<(rows + 255) / 256, 256, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, rows, ctx->oz_exp.p);
+  k_oz_colmax_partial<<<nb, 256, 0, ctx->stream>>>(B, B, 1, mb, N, ctx->oz_ipart.p);
+  k_oz_colmax_final<<<(mb + 255) / 256, 256, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, mb, ctx->oz_exp.p + rows);
   count_launch(ctx, 4);
   ctx->oz_part.ensure((size_t)items * TILE);
   GramArgs args{A[0], na > 1 ? A[1] : A[0], na, ma, B, mb, N, ctx->oz_exp.p, ctx->oz_exp.p + rows, row_tiles,

@@ -474,6 +474,9 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
       const uint32_t k = deg - 2;
       gbfe_mv *rn = ((deg - 2) % 2 == 0) ? RN.get() : R.get();
       gbfe_mv *r = ((deg - 2) % 2 == 0) ? R.get() : RN.get();
+      if (mixed && ctx->fuse_filter &&
+          filter_step_fused(A, BInv, rn, r, w.coef.p + 3 * k, w.tab.p + (size_t)k * m, Yr))
+        continue;
       apply_op(BInv, rn, s1);
       apply_op(A, s1, s2);
       if (mixed)

@@ -253,6 +253,10 @@ struct Tc2Args {
   float *Yc;
   uint32_t N, mtiles, tmem_cols, nbuf, stages;
   int *status;
+  // optional gather scale: X[i] -> is_zero[i] ? 0 : (float)scale[i] * X[i], the
+  // diagonal operator B^-1 (with homogeneous Dirichlet rows) applied on the fly
+  const double *xscale;
+  const uint8_t *xzero;
 };
 
 __global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a) {
@@ -433,7 +437,13 @@ __global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a)
 #pragma unroll
             for (int kk = 0; kk < 8; ++kk) {
               const uint32_t k = kc * KC + kb * 8 + kk;
-              xv[u][kk] = (vin && k < nd) ? __ldg(a.X + (uint64_t)a.ids[off + k] * m + v0 + vv[u]) : 0.f;
+              float x = 0.f;
+              if (vin && k < nd) {
+                const uint32_t id = a.ids[off + k];
+                x = __ldg(a.X + (uint64_t)id * m + v0 + vv[u]);
+                if (a.xscale) x = (a.xzero && a.xzero[id]) ? 0.f : (float)a.xscale[id] * x;
+              }
+              xv[u][kk] = x;
             }
           }
 #pragma unroll
@@ -494,7 +504,8 @@ bool tc_supported(const gbfe_mesh *me) { return me->nd_max <= 256; }
 // v2 launch: persistent grid over (cell, vector tile) items of one M-tile group.
 // N_req / stages_req = 0: the tuned shape if one exists, else the heuristic.
 static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg, uint32_t ncell,
-                       uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0, uint32_t stages_req = 0) {
+                       uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0, uint32_t stages_req = 0,
+                       const double *xscale = nullptr, const uint8_t *xzero = nullptr) {
   gbfe_mesh *me = op->mesh;
   const uint32_t m = X->m;
   if (!N_req) {
@@ -527,7 +538,7 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
     attr_set = true;
   }
   Tc2Args args{X->f.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, vt, op->tc_aoff.p,
-               op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p};
+               op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xscale, xzero};
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
   k_cell_apply_tc2<<<grid, THREADS2, smem, ctx->stream>>>(args);
@@ -536,10 +547,11 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
 
 // Yc (FP32 cell-wise buffer) = split-BF16 tensor-core products, size-binned by
 // the number of 128-row M tiles a cell needs.
-void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc) {
+void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const double *xscale, const uint8_t *xzero) {
   gbfe_mesh *me = op->mesh;
   gbfe_ctx *ctx = me->ctx;
   const uint32_t m = X->m;
+  GBFE_REQUIRE(!xscale || ctx->tc_version == 2, "scaled gather needs the persistent tensor-core kernel");
   // group bins (distinct nd) into launches by M-tile count
   for (uint32_t mtiles = 1; mtiles <= 2; ++mtiles) {
     uint32_t b0 = UINT32_MAX, b1 = 0;
@@ -555,7 +567,8 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc) {
     const uint32_t cbeg = me->bin_begin[b0], cend = me->bin_begin[b1];
     const uint32_t ncell = cend - cbeg;
     if (ctx->tc_version == 2) {
-      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1]);
+      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1], 0, 0, xscale,
+                 xzero);
       continue;
     }
     uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);

@@ -75,6 +75,10 @@ class LinAlgOpContext:
     def set_graphs(self, on: bool) -> None:
         check(self.lib.gbfe_ctx_set_graphs(self.h, 1 if on else 0), self.h, "set_graphs")
 
+    def set_fused_filter(self, on: bool) -> None:
+        """Mixed filter steps as two fused launches (default) or as separate applies."""
+        check(self.lib.gbfe_ctx_set_fused_filter(self.h, 1 if on else 0), self.h, "set_fused_filter")
+
     def set_small_eig(self, on_host: bool) -> None:
         """Rayleigh-Ritz m x m eigenproblems on the host (m <= 128, default) or in cuSOLVER."""
         check(self.lib.gbfe_ctx_set_small_eig(self.h, 1 if on_host else 0), self.h, "set_small_eig")

@@ -6,7 +6,8 @@ rotation X T of N x m blocks, DGEMM against the sliced tensor-core products.
 Prints one JSON line per shape: milliseconds per call (wall clock around
 `reps` synchronised calls, and the CUDA-event time of the sliced kernel),
 algorithmic FP64 TFLOP/s (2 N m^2 per call) and the error of the sliced
-result against the DGEMM result relative to max |X|^T |Y|.
+result against the DGEMM result (Gram: relative to ||x_i|| ||y_j||; rotation:
+relative to max_i |X_ki| sum_i |T_ij|).
 """
 from __future__ import annotations
 
@@ -65,8 +66,9 @@ def main() -> None:
             ctx.check_status()
             res[mode] = (ms, st, r if what == "gram" else Z.numpy())
         ctx.set_fp64_apply(0)
-        if what == "gram":
-            err = float(np.abs(res[1][2] - res[0][2]).max() / (np.abs(X0).T @ np.abs(Y0)).max())
+        if what == "gram":  # relative to ||x_i|| ||y_j|| (Cauchy-Schwarz bound of each entry)
+            scale = np.sqrt((X0 * X0).sum(axis=0))[:, None] * np.sqrt((Y0 * Y0).sum(axis=0))[None, :]
+            err = float((np.abs(res[1][2] - res[0][2]) / scale).max())
         else:
             scale = np.abs(X0).max(axis=1, keepdims=True) * np.abs(T).sum(axis=0, keepdims=True)
             err = float((np.abs(res[1][2] - res[0][2]) / scale).max())
