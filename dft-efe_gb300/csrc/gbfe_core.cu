@@ -139,6 +139,14 @@ __global__ void k_assemble(const TC *__restrict__ Yc, uint32_t m, uint64_t n_dof
   }
 }
 
+// gather scale of the fused filter: (float)d[i] (the factor k_diag_apply<float>
+// applies), 0 on homogeneous Dirichlet rows
+__global__ void k_diag_gather(const double *__restrict__ d, const uint8_t *__restrict__ is_row, uint64_t n,
+                              float *__restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = (is_row && is_row[i]) ? 0.f : (float)d[i];
+}
+
 // Assembly of a FP32 cell-wise result with one Chebyshev recurrence step fused
 // in (homogeneous Dirichlet rows only): with S the assembled A B^-1 RN,
 //   R = alpha1 S + (-c alpha1) RN + alpha2 R + (alpha1 eF2[j]) Y
@@ -405,9 +413,15 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
       (c && !c->pure_dirichlet) || RN->m == 0)
     return false;
   const uint32_t m = RN->m;
+  if (!BInv->diag_gather.p) {
+    BInv->diag_gather.alloc(me->n_dofs);
+    k_diag_gather<<<grid_for(me->n_dofs, 256), 256, 0, ctx->stream>>>(BInv->diag.p, c ? c->is_row.p : nullptr,
+                                                                      me->n_dofs, BInv->diag_gather.p);
+    check_launch(ctx, "diag_gather");
+  }
   constraints_p2c(ctx, c, RN);  // BInv's parent-to-child on its input, as apply_op does
   A->cellbuf_f32.ensure((size_t)me->total_cell_dofs * m);
-  cell_apply_tc(A, RN, A->cellbuf_f32.p, BInv->diag.p, c ? c->is_row.p : nullptr);
+  cell_apply_tc(A, RN, A->cellbuf_f32.p, BInv->diag_gather.p);
   const uint64_t n = (uint64_t)me->n_dofs * m;
   k_assemble_cheb<<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p,
                                                                me->slot.p, c ? c->is_row.p : nullptr, coef, RN->f.p,

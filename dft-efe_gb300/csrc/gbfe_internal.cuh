@@ -238,6 +238,7 @@ struct gbfe_op {
   mutable gbfe::DBuf<int> oz_xexp;    // per-vector exponent of the current X
   gbfe::DBuf<float> mats_f32;         // FP32 copy for the SIMT mixed apply
   gbfe::DBuf<double> diag;
+  mutable gbfe::DBuf<float> diag_gather;  // (float)diag, 0 on homogeneous Dirichlet rows (fused filter)
   uint64_t blk_begin = 0, blk_n = 0;  // OP_DIAG_BLOCK: dense block rows
   gbfe::DBuf<double> blk;             // column-major blk_n x blk_n
   gbfe::DBuf<float> blk_f32;
@@ -316,8 +317,7 @@ void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
 void build_mixed_mats(gbfe_op *op);
 void build_tc_mats(gbfe_op *op);
 bool tc_supported(const gbfe_mesh *me);
-void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const double *xscale = nullptr,
-                   const uint8_t *xzero = nullptr);
+void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *xscale = nullptr);
 // one step of the mixed Chebyshev recurrence in two launches:
 //   R = alpha1 (A B^-1 RN - c RN) + alpha2 R + alpha1 eF2[j] Y
 // (B^-1 applied in the tensor-core gather, the step fused into the assembly);

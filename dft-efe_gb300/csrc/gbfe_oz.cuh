@@ -62,6 +62,16 @@ __device__ __forceinline__ void digits(double v, int e, int *d) {
   d[0] = (int)X;  // |X| <= 64 after the seven low digits
 }
 
+// v * 2^k by adding k to the exponent field (integer pipe), exact; zero
+// stays zero and results outside the normal range go through ldexp.
+__device__ __forceinline__ double scale2(double v, int k) {
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0) return v;                                   // zero
+  if (e + k <= 0 || e + k >= 0x7ff) return ldexp(v, k);  // leaves the normal range
+  return __longlong_as_double(b + ((long long)k << 52));
+}
+
 // 2^k as a double (k within the normal range)
 __device__ __forceinline__ double pow2(int k) { return __longlong_as_double((long long)(uint64_t)(k + 1023) << 52); }
 

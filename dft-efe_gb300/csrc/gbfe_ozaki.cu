@@ -315,9 +315,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
           for (int q2 = 0; q2 < 16; ++q2) {
             const uint32_t v = v0 + col + q2;
             if (v < m) {
-              const int sc = er + a.x_exp[v] + 2;
-              const double scale = __longlong_as_double((long long)(uint64_t)(sc + 1023) << 52);
-              dst[q2] = ((double)hi[q2] + (double)lo[q2]) * scale;
+              dst[q2] = oz::scale2((double)hi[q2] + (double)lo[q2], er + a.x_exp[v] + 2);
             }
           }
         }

@@ -308,7 +308,8 @@ __global__ void k_oz_gram_final(const double *__restrict__ part, uint32_t na, ui
     const uint32_t rt = R / 128, r = R % 128, ct = j / OG_N, cj = j % OG_N;
     const double *p = part + ((uint64_t)(rt * col_tiles + ct) * splits) * TILE + (uint64_t)cj * 128 + r;
     double s = 0.0;
-    for (uint32_t sp = 0; sp < splits; ++sp) s += p[(uint64_t)sp * TILE];
+#pragma unroll 8
+    for (uint32_t sp = 0; sp < splits; ++sp) s += __ldg(p + (uint64_t)sp * TILE);
     const double v = s * oz::pow2(aexp[R] + bexp[j] + 2);
     const uint32_t i = R % ma;
     (R < ma ? S0 : S1)[i + (uint64_t)ma * j] = v;
@@ -462,7 +463,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
           double *dst = a.out[op] + orow * a.mo + j0;
 #pragma unroll
           for (int i = 0; i < 16; ++i)
-            if (j0 + i < a.mo) dst[i] = ((double)hi[i] + (double)lo[i]) * oz::pow2(oe + a.texp[j0 + i] + 2);
+            if (j0 + i < a.mo) dst[i] = oz::scale2((double)hi[i] + (double)lo[i], oe + a.texp[j0 + i] + 2);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -572,7 +573,8 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
   const uint32_t row_tiles = (rows + 127) / 128, col_tiles = (mb + OG_N - 1) / OG_N;
   const uint32_t chunks = (uint32_t)std::max<uint64_t>(1, (N + CHUNK - 1) / CHUNK);
   const uint32_t tiles = row_tiles * col_tiles;
-  const uint32_t want = std::max<uint32_t>(1, (2 * (uint32_t)ctx->sm_count + tiles - 1) / tiles);
+  // about one item per SM: every item is a few 512-row chunks, partials stay few
+  const uint32_t want = std::max<uint32_t>(1, ((uint32_t)ctx->sm_count + tiles - 1) / tiles);
   const uint32_t splits_req = std::min(chunks, want);
   const uint32_t cps = (chunks + splits_req - 1) / splits_req;
   const uint32_t splits = (chunks + cps - 1) / cps;
@@ -596,7 +598,7 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
     check_launch(ctx, "oz_gram");
   }
   const uint64_t total = (uint64_t)rows * mb;
-  k_oz_gram_final<<<grid_for(total, 256), 256, 0, ctx->stream>>>(ctx->oz_part.p, na, ma, mb, col_tiles, splits,
+  k_oz_gram_final<<<grid_for(total, 64), 64, 0, ctx->stream>>>(ctx->oz_part.p, na, ma, mb, col_tiles, splits,
                                                                ctx->oz_exp.p, ctx->oz_exp.p + rows, S[0],
                                                                na > 1 ? S[1] : S[0]);
   check_launch(ctx, "oz_gram_final");

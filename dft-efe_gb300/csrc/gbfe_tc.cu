@@ -253,10 +253,9 @@ struct Tc2Args {
   float *Yc;
   uint32_t N, mtiles, tmem_cols, nbuf, stages;
   int *status;
-  // optional gather scale: X[i] -> is_zero[i] ? 0 : (float)scale[i] * X[i], the
-  // diagonal operator B^-1 (with homogeneous Dirichlet rows) applied on the fly
-  const double *xscale;
-  const uint8_t *xzero;
+  // optional gather scale X[i] -> xscale[i] * X[i]: the diagonal operator B^-1
+  // applied on the fly (xscale = 0 on homogeneous Dirichlet rows)
+  const float *xscale;
 };
 
 __global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a) {
@@ -437,13 +436,19 @@ __global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a)
 #pragma unroll
             for (int kk = 0; kk < 8; ++kk) {
               const uint32_t k = kc * KC + kb * 8 + kk;
-              float x = 0.f;
-              if (vin && k < nd) {
-                const uint32_t id = a.ids[off + k];
-                x = __ldg(a.X + (uint64_t)id * m + v0 + vv[u]);
-                if (a.xscale) x = (a.xzero && a.xzero[id]) ? 0.f : (float)a.xscale[id] * x;
+              xv[u][kk] = (vin && k < nd) ? __ldg(a.X + (uint64_t)a.ids[off + k] * m + v0 + vv[u]) : 0.f;
+            }
+          }
+          if (a.xscale) {  // separate pass: keeps the 16 row loads above independent
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+              const uint32_t itm = item + u * GATHER_WARPS;
+              const uint32_t kb = itm % (KC / 8);
+#pragma unroll
+              for (int kk = 0; kk < 8; ++kk) {
+                const uint32_t k = kc * KC + kb * 8 + kk;
+                xv[u][kk] *= (has[u] && k < nd) ? __ldg(a.xscale + a.ids[off + k]) : 0.f;
               }
-              xv[u][kk] = x;
             }
           }
 #pragma unroll
@@ -505,7 +510,7 @@ bool tc_supported(const gbfe_mesh *me) { return me->nd_max <= 256; }
 // N_req / stages_req = 0: the tuned shape if one exists, else the heuristic.
 static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg, uint32_t ncell,
                        uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0, uint32_t stages_req = 0,
-                       const double *xscale = nullptr, const uint8_t *xzero = nullptr) {
+                       const float *xscale = nullptr) {
   gbfe_mesh *me = op->mesh;
   const uint32_t m = X->m;
   if (!N_req) {
@@ -538,7 +543,7 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
     attr_set = true;
   }
   Tc2Args args{X->f.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, vt, op->tc_aoff.p,
-               op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xscale, xzero};
+               op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xscale};
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
   k_cell_apply_tc2<<<grid, THREADS2, smem, ctx->stream>>>(args);
@@ -547,7 +552,7 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
 
 // Yc (FP32 cell-wise buffer) = split-BF16 tensor-core products, size-binned by
 // the number of 128-row M tiles a cell needs.
-void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const double *xscale, const uint8_t *xzero) {
+void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *xscale) {
   gbfe_mesh *me = op->mesh;
   gbfe_ctx *ctx = me->ctx;
   const uint32_t m = X->m;
@@ -567,8 +572,7 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const double 
     const uint32_t cbeg = me->bin_begin[b0], cend = me->bin_begin[b1];
     const uint32_t ncell = cend - cbeg;
     if (ctx->tc_version == 2) {
-      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1], 0, 0, xscale,
-                 xzero);
+      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1], 0, 0, xscale);
       continue;
     }
     uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
