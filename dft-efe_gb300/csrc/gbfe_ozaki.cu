@@ -199,7 +199,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
   } else if (warp == 5) {
     // ---------------- MMA issuer: 36 products per K step into 8 level accumulators
     if (lane == 0) {
-      const uint32_t idesc = instr_desc(128, OZ_N);
       uint32_t q = 0, li = 0;
       for (uint32_t it = blockIdx.x; it < n_items && !*abort_flag; it += gridDim.x, ++li) {
         uint32_t c, mt, v0;
@@ -219,17 +218,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
           const uint32_t abase = smem_u32(smem + s * OZ_STAGE);
           const uint32_t bbase = abase + OZ_S * OZ_A_PART;
           for (uint32_t ks = 0; ks < KC / 16; ++ks) {
+            // slice sl of A against the stacked B slices t0..t1 (one descriptor,
+            // N = 64 (t1 - t0 + 1)) into the contiguous levels sl+t0 .. sl+t1:
+            // 12 MMAs per K step; the two sl = 1 MMAs start every level
 #pragma unroll
-            for (int g = 2; g <= OZ_S + 1; ++g) {
-              const uint32_t d = tmem + (g - 2) * OZ_N;
-              const int s_lo = g - OZ_S > 1 ? g - OZ_S : 1;
-              const int s_hi = g - 1 < OZ_S ? g - 1 : OZ_S;
+            for (int sl = 1; sl <= OZ_S; ++sl) {
 #pragma unroll
-              for (int sl = s_lo; sl <= s_hi; ++sl) {
-                const int tl = g - sl;
+              for (int t0 = 1; t0 <= OZ_S + 1 - sl; t0 += 4) {
+                const int t1 = t0 + 3 < OZ_S + 1 - sl ? t0 + 3 : OZ_S + 1 - sl;
                 const uint64_t ad = smem_desc(abase + (sl - 1) * OZ_A_PART + ks * 2 * LBO);
-                const uint64_t bd = smem_desc(bbase + (tl - 1) * OZ_B_PART + ks * 2 * LBO);
-                umma(d, ad, bd, idesc, ((kc | ks) != 0 || sl != s_lo) ? 1u : 0u);
+                const uint64_t bd = smem_desc(bbase + (t0 - 1) * OZ_B_PART + ks * 2 * LBO);
+                umma(tmem + (sl + t0 - 2) * OZ_N, ad, bd, instr_desc(128, OZ_N * (t1 - t0 + 1)),
+                     ((kc | ks) == 0 && sl == 1) ? 0u : 1u);
               }
             }
           }

@@ -63,21 +63,22 @@ __device__ __forceinline__ void store_core_rows(uint8_t *tile, uint32_t part, ui
     *(uint4 *)(tile + s * part + pos) = make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
 }
 
-// 36 digit-pair MMAs of one 16-row K step into the 8 level accumulators
+// The 36 digit-pair products of one 16-row K step as 12 MMAs: slice s of A
+// against the stacked B slices t0..t1 (contiguous in shared memory, so one
+// descriptor with N = 64 (t1 - t0 + 1) <= 256 covers them) lands in the
+// contiguous level accumulators s+t0 .. s+t1.  The two s = 1 MMAs cover every
+// level (2..9) and start them at the first K step.
 __device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t abase, uint32_t bbase, uint32_t ks,
                                              bool first) {
-  const uint32_t idesc = instr_desc(128, OG_N);
 #pragma unroll
-  for (int g = 2; g <= oz::S + 1; ++g) {
-    const uint32_t d = tmem + (g - 2) * OG_N;
-    const int s_lo = g - oz::S > 1 ? g - oz::S : 1;
-    const int s_hi = g - 1 < oz::S ? g - 1 : oz::S;
+  for (int sl = 1; sl <= oz::S; ++sl) {
 #pragma unroll
-    for (int sl = s_lo; sl <= s_hi; ++sl) {
-      const int tl = g - sl;
+    for (int t0 = 1; t0 <= oz::S + 1 - sl; t0 += 4) {
+      const int t1 = min(t0 + 3, oz::S + 1 - sl);
+      const uint32_t idesc = instr_desc(128, OG_N * (t1 - t0 + 1));
       const uint64_t ad = smem_desc(abase + (sl - 1) * A_PART + ks * 2 * LBO);
-      const uint64_t bd = smem_desc(bbase + (tl - 1) * B_PART + ks * 2 * LBO);
-      umma(d, ad, bd, idesc, (!first || sl != s_lo) ? 1u : 0u);
+      const uint64_t bd = smem_desc(bbase + (t0 - 1) * B_PART + ks * 2 * LBO);
+      umma(tmem + (sl + t0 - 2) * OG_N, ad, bd, idesc, (first && sl == 1) ? 0u : 1u);
     }
   }
 }
