@@ -163,6 +163,8 @@ struct gbfe_ctx {
   int fuse_filter = 1;       // mixed filter: B^-1 in the tensor-core gather, step fused into the assembly
   gbfe::DBuf<int> oz_exp, oz_rexp;  // sliced products: column / row exponents
   gbfe::DBuf<int> oz_ipart;         // partial exponent maxima
+  std::vector<std::unique_ptr<gbfe::DBuf<double>>> vec_pool;  // scoped m-vectors of a pass (LIFO)
+  size_t vec_top = 0;
   gbfe::DBuf<double> oz_part;       // per-item Gram partials
   gbfe::DBuf<__nv_bfloat16> oz_tdig;  // slices of the rotation factor
 };

@@ -189,21 +189,33 @@ void d_coldots(gbfe_ctx *ctx, const gbfe_mv *x, const gbfe_mv *y, double *out_d,
   check_launch(ctx, "coldot_final");
 }
 
+// Short-lived device vector of doubles (length m scalars of a pass), taken
+// from a per-context stack of buffers: no cudaMalloc / cudaFree (and their
+// implicit device synchronisation) in the pass loop.  Scoped use only (LIFO).
 struct DevVec {
-  DBuf<double> b;
-  explicit DevVec(size_t n) { b.alloc(std::max<size_t>(n, 1)); }
-  void set(gbfe_ctx *ctx, const double *h, size_t n) {
-    GBFE_CUDA(cudaMemcpyAsync(b.p, h, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  gbfe_ctx *ctx;
+  double *p;
+  DevVec(gbfe_ctx *c, size_t n) : ctx(c) {
+    const size_t idx = ctx->vec_top++;
+    if (ctx->vec_pool.size() <= idx) ctx->vec_pool.emplace_back(new DBuf<double>());
+    ctx->vec_pool[idx]->ensure(std::max<size_t>(n, 1));
+    p = ctx->vec_pool[idx]->p;
   }
-  void get(gbfe_ctx *ctx, double *h, size_t n) const {
-    GBFE_CUDA(cudaMemcpyAsync(h, b.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  ~DevVec() { --ctx->vec_top; }
+  DevVec(const DevVec &) = delete;
+  DevVec &operator=(const DevVec &) = delete;
+  void set(gbfe_ctx *, const double *h, size_t n) {
+    GBFE_CUDA(cudaMemcpyAsync(p, h, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  void get(gbfe_ctx *, double *h, size_t n) const {
+    GBFE_CUDA(cudaMemcpyAsync(h, p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
     GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
   }
 };
 
 void host_coldots(gbfe_ctx *ctx, const gbfe_mv *x, const gbfe_mv *y, double *h, bool take_sqrt) {
-  DevVec o(x->m);
-  d_coldots(ctx, x, y, o.b.p, take_sqrt);
+  DevVec o(ctx, x->m);
+  d_coldots(ctx, x, y, o.p, take_sqrt);
   o.get(ctx, h, x->m);
 }
 
@@ -282,13 +294,13 @@ int small_syevd(gbfe_ctx *ctx, int m, double *dA, double *eig_h, std::string &ms
     GBFE_CUDA(cudaMemcpyAsync(dA, h.data(), h.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
     return GBFE_OK;
   }
-  DevVec W(m);
+  DevVec W(ctx, m);
   int lwork = 0;
   GBFE_CUSOLVER(cusolverDnDsyevd_bufferSize(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, dA, m,
-                                            W.b.p, &lwork));
+                                            W.p, &lwork));
   ctx->lwork.ensure(std::max(lwork, 1));
   ctx->info.ensure(1);
-  GBFE_CUSOLVER(cusolverDnDsyevd(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, dA, m, W.b.p,
+  GBFE_CUSOLVER(cusolverDnDsyevd(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, dA, m, W.p,
                                  ctx->lwork.p, lwork, ctx->info.p));
   count_launch(ctx);
   int info = 0;
@@ -441,7 +453,7 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
     coef[3 * k + 1] = s.c;
     coef[3 * k + 2] = s.alpha2[k];
   }
-  DevVec d_ones(m), d_eig(m);
+  DevVec d_ones(ctx, m), d_eig(ctx, m);
   std::vector<double> ones(m, 1.0);
   d_ones.set(ctx, ones.data(), m);
   d_eig.set(ctx, eig_h, m);
@@ -457,7 +469,7 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
     auto s3 = make_like(X, GBFE_F64);
     apply_op(B, X, Y);
     apply_op(A, X, s3.get());
-    d_axpby_blocked(ctx, 1.0, d_ones.b.p, s3.get(), -1.0, d_eig.b.p, Y, Y);  // Y = AX - lambda BX
+    d_axpby_blocked(ctx, 1.0, d_ones.p, s3.get(), -1.0, d_eig.p, Y, Y);  // Y = AX - lambda BX
   }
   const gbfe_mv *Yr = Y;
   if (mixed) {
@@ -551,9 +563,9 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
     k_cheb_final_mixed<<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, Rfin->f.p, eF2_final, X->d.p, Y->d.p);
     check_launch(ctx, "cheb_final_mixed");
   } else {
-    d_axpby_blocked(ctx, 1.0, d_ones.b.p, Rfin, 1.0, eF2_final, X, Y);
+    d_axpby_blocked(ctx, 1.0, d_ones.p, Rfin, 1.0, eF2_final, X, Y);
   }
-  GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+  // no host sync: the callers' next operations are ordered on the stream
 }
 
 // ------------------------------------------------------------ small host eigensolver
@@ -640,10 +652,10 @@ int residual_norms_impl(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X, const do
   apply_op(A, X, HX.get());
   apply_op(B, X, MX.get());
   std::vector<double> nOnes(m, -1.0);
-  DevVec d_no(m), d_e(m);
+  DevVec d_no(ctx, m), d_e(ctx, m);
   d_no.set(ctx, nOnes.data(), m);
   d_e.set(ctx, eig_h, m);
-  d_axpby_blocked(ctx, 1.0, d_no.b.p, HX.get(), 1.0, d_e.b.p, MX.get(), Rr.get());
+  d_axpby_blocked(ctx, 1.0, d_no.p, HX.get(), 1.0, d_e.p, MX.get(), Rr.get());
   host_coldots(ctx, Rr.get(), Rr.get(), norms_h, true);
   return GBFE_OK;
 }
@@ -754,11 +766,11 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
     count_launch(ctx, 3);
   }
   std::vector<double> nOnes(m, -1.0);
-  DevVec d_no(m), d_e(m);
+  DevVec d_no(ctx, m), d_e(ctx, m);
   d_no.set(ctx, nOnes.data(), m);
   d_e.set(ctx, eig_h, m);
   // R = HX - MX diag(eps)   (getLinearEigenSolveResidual's axpbyBlocked with the sign flipped)
-  d_axpby_blocked(ctx, -1.0, d_no.b.p, st.HX.get(), -1.0, d_e.b.p, st.MX.get(), st.R.get());
+  d_axpby_blocked(ctx, -1.0, d_no.p, st.HX.get(), -1.0, d_e.p, st.MX.get(), st.R.get());
   host_coldots(ctx, st.R.get(), st.R.get(), res_h, true);
   return GBFE_OK;
 }
@@ -782,10 +794,10 @@ int ks_solve_fused(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe
   apply_op(B, X, st.MX.get());
   {
     std::vector<double> ones(m, 1.0);
-    DevVec d_o(m), d_e(m);
+    DevVec d_o(ctx, m), d_e(ctx, m);
     d_o.set(ctx, ones.data(), m);
     d_e.set(ctx, eig_h, m);
-    d_axpby_blocked(ctx, 1.0, d_o.b.p, st.HX.get(), -1.0, d_e.b.p, st.MX.get(), st.R.get());
+    d_axpby_blocked(ctx, 1.0, d_o.p, st.HX.get(), -1.0, d_e.p, st.MX.get(), st.R.get());
     GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
   }
   int status = GBFE_ERR_NOT_CONVERGED;
@@ -855,6 +867,7 @@ int gbfe_residual_chebyshev_filter(const gbfe_op *A, const gbfe_op *B, const gbf
     GBFE_REQUIRE(X->m == Y->m && X->mesh == Y->mesh, "filter: shape mismatch");
     GBFE_REQUIRE(degree >= 1, "filter: degree must be >= 1");
     residual_filter(A, B, BInv, eigenvalues, X, degree, wl, wu, uu, Y, precision);
+    GBFE_CUDA(cudaStreamSynchronize(CTX_OF(X)->stream));
   });
 }
 
@@ -1080,7 +1093,7 @@ int gbfe_cg_solve(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b, gbfe_mv
     std::vector<double> bn(k), rn(k), zr(k), pw(k), zrn(k), ones(k, 1.0), nones(k, -1.0), coef(k);
     std::vector<char> conv(k, 0);
     host_coldots(ctx, b, b, bn.data(), true);
-    DevVec d_ones(k), d_nones(k), d_coef(k);
+    DevVec d_ones(ctx, k), d_nones(ctx, k), d_coef(ctx, k);
     d_ones.set(ctx, ones.data(), k);
     d_nones.set(ctx, nones.data(), k);
     bool diverge = false, all = false;
@@ -1093,7 +1106,7 @@ int gbfe_cg_solve(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b, gbfe_mv
       }
       if (iter == 0) {
         apply_op(A, xw.get(), w.get());
-        d_axpby_blocked(ctx, 1.0, d_ones.b.p, b, 1.0, d_nones.b.p, w.get(), r.get());
+        d_axpby_blocked(ctx, 1.0, d_ones.p, b, 1.0, d_nones.p, w.get(), r.get());
         apply_op(PC, r.get(), z.get());
         GBFE_CUDA(cudaMemcpyAsync(p->d.p, z->d.p, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
       } else {
@@ -1102,16 +1115,16 @@ int gbfe_cg_solve(const gbfe_op *A, const gbfe_op *PC, const gbfe_mv *b, gbfe_mv
         host_coldots(ctx, p.get(), w.get(), pw.data(), false);
         for (uint32_t j = 0; j < k; ++j) coef[j] = zr[j] / pw[j];
         d_coef.set(ctx, coef.data(), k);
-        d_axpby_blocked(ctx, 1.0, d_ones.b.p, xw.get(), 1.0, d_coef.b.p, p.get(), xw.get());
+        d_axpby_blocked(ctx, 1.0, d_ones.p, xw.get(), 1.0, d_coef.p, p.get(), xw.get());
         GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
         for (uint32_t j = 0; j < k; ++j) coef[j] = -zr[j] / pw[j];
         d_coef.set(ctx, coef.data(), k);
-        d_axpby_blocked(ctx, 1.0, d_ones.b.p, r.get(), 1.0, d_coef.b.p, w.get(), r.get());
+        d_axpby_blocked(ctx, 1.0, d_ones.p, r.get(), 1.0, d_coef.p, w.get(), r.get());
         apply_op(PC, r.get(), z.get());
         host_coldots(ctx, z.get(), r.get(), zrn.data(), false);
         for (uint32_t j = 0; j < k; ++j) coef[j] = zrn[j] / zr[j];
         d_coef.set(ctx, coef.data(), k);
-        d_axpby_blocked(ctx, 1.0, d_ones.b.p, z.get(), 1.0, d_coef.b.p, p.get(), p.get());
+        d_axpby_blocked(ctx, 1.0, d_ones.p, z.get(), 1.0, d_coef.p, p.get(), p.get());
       }
       host_coldots(ctx, r.get(), r.get(), rn.data(), true);
       for (uint32_t j = 0; j < k; ++j) {
