@@ -413,12 +413,7 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
       (c && !c->pure_dirichlet) || RN->m == 0)
     return false;
   const uint32_t m = RN->m;
-  if (!BInv->diag_gather.p) {
-    BInv->diag_gather.alloc(me->n_dofs);
-    k_diag_gather<<<grid_for(me->n_dofs, 256), 256, 0, ctx->stream>>>(BInv->diag.p, c ? c->is_row.p : nullptr,
-                                                                      me->n_dofs, BInv->diag_gather.p);
-    check_launch(ctx, "diag_gather");
-  }
+  if (!BInv->diag_gather.p) return false;  // built at upload for diagonal operators
   constraints_p2c(ctx, c, RN);  // BInv's parent-to-child on its input, as apply_op does
   A->cellbuf_f32.ensure((size_t)me->total_cell_dofs * m);
   cell_apply_tc(A, RN, A->cellbuf_f32.p, BInv->diag_gather.p);
@@ -958,6 +953,13 @@ static int diag_upload_impl(gbfe_mesh *mesh, const gbfe_cons *cons, const double
       GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
     } else {
       op->diag.upload(diag, mesh->n_dofs, mesh->ctx->stream);
+      if (kind == OP_DIAG && (!cons || cons->pure_dirichlet)) {
+        // gather factor of the fused mixed filter step
+        op->diag_gather.alloc(mesh->n_dofs);
+        k_diag_gather<<<grid_for(mesh->n_dofs, 256), 256, 0, mesh->ctx->stream>>>(
+            op->diag.p, cons ? cons->is_row.p : nullptr, mesh->n_dofs, op->diag_gather.p);
+        check_launch(mesh->ctx, "diag_gather");
+      }
       GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
     }
   });

@@ -240,7 +240,7 @@ struct gbfe_op {
   mutable gbfe::DBuf<int> oz_xexp;    // per-vector exponent of the current X
   gbfe::DBuf<float> mats_f32;         // FP32 copy for the SIMT mixed apply
   gbfe::DBuf<double> diag;
-  mutable gbfe::DBuf<float> diag_gather;  // (float)diag, 0 on homogeneous Dirichlet rows (fused filter)
+  gbfe::DBuf<float> diag_gather;  // (float)diag, 0 on homogeneous Dirichlet rows (fused filter)
   uint64_t blk_begin = 0, blk_n = 0;  // OP_DIAG_BLOCK: dense block rows
   gbfe::DBuf<double> blk;             // column-major blk_n x blk_n
   gbfe::DBuf<float> blk_f32;
