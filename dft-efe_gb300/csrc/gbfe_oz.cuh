@@ -10,6 +10,7 @@
 // L_g = sum_{s+t=g} sum_k a_s x_t (at most 8 digit pairs) over K <= 512 terms
 // stays within 2^24 and FP32 tensor-core accumulation of it is exact.
 #pragma once
+#include <cuda_bf16.h>
 #include <cstdint>
 
 namespace gbfe {
@@ -38,28 +39,51 @@ __device__ __forceinline__ int exp_bits(double v) {
 }
 __device__ __forceinline__ int exp_or_zero(int e) { return e == EXP_NONE ? 0 : e; }
 
-// balanced digits of v (|v| < 2^e): d[0] most significant
-__device__ __forceinline__ void digits(double v, int e, int *d) {
+// trunc(v 2^(55-e)) as a signed integer, |.| < 2^55 for |v| < 2^e
+__device__ __forceinline__ int64_t fixed55(double v, int e) {
   const uint64_t bits = (uint64_t)__double_as_longlong(v);
   const int ex = (int)((bits >> 52) & 0x7ff);
-  int64_t X = 0;
-  if (ex != 0) {
-    const uint64_t mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-    const int sh = ex - 1075 + 55 - e;  // v 2^(55-e) = mant 2^sh and |v| < 2^e: sh <= 2
-    uint64_t fx = 0;
-    if (sh >= 0)
-      fx = mant << sh;
-    else if (sh > -64)
-      fx = mant >> (-sh);
-    X = (bits >> 63) ? -(int64_t)fx : (int64_t)fx;
-  }
+  if (ex == 0) return 0;
+  const uint64_t mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+  const int sh = ex - 1075 + 55 - e;  // v 2^(55-e) = mant 2^sh and |v| < 2^e: sh <= 2
+  uint64_t fx = 0;
+  if (sh >= 0)
+    fx = mant << sh;
+  else if (sh > -64)
+    fx = mant >> (-sh);
+  return (bits >> 63) ? -(int64_t)fx : (int64_t)fx;
+}
+
+// Balanced base-128 digits of v (|v| < 2^e), d[0] most significant.  Adding 64
+// at each of the seven low digit positions turns the balanced digits b_j in
+// [-64, 63] into the plain base-128 digits b_j + 64 of the sum, so every digit
+// is one shift-and-mask; the top digit is the arithmetic shift of the rest
+// (|d[0]| <= 64).
+constexpr int64_t DIGIT_BIAS = 64LL * (((1LL << 49) - 1) / 127);
+__device__ __forceinline__ void digits(double v, int e, int *d) {
+  const int64_t Y = fixed55(v, e) + DIGIT_BIAS;
+  const uint64_t u = (uint64_t)Y;
 #pragma unroll
-  for (int s = S - 1; s >= 1; --s) {
-    const int r = (int)((X + 64) & 127) - 64;  // balanced remainder in [-64, 63]
-    d[s] = r;
-    X = (X - r) >> 7;  // exact division
+  for (int s = 1; s < S; ++s) d[s] = (int)((u >> (7 * (S - 1 - s))) & 127u) - 64;
+  d[0] = (int)(Y >> 49);
+}
+
+// small integer -> float without the conversion unit (exact for |d| < 2^22)
+__device__ __forceinline__ float int_to_float_small(int d) {
+  return __int_as_float(0x4B400000 + d) - 12582912.0f;
+}
+
+// the 8 slices of two consecutive K values, packed as BF16 pairs (low half =
+// first value): packed[s] for slice s
+__device__ __forceinline__ void digits_pair_bf16(double v0, double v1, int e, uint32_t *packed) {
+  int d0[S], d1[S];
+  digits(v0, e, d0);
+  digits(v1, e, d1);
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const __nv_bfloat162 pr = __floats2bfloat162_rn(int_to_float_small(d0[s]), int_to_float_small(d1[s]));
+    packed[s] = *reinterpret_cast<const uint32_t *>(&pr);
   }
-  d[0] = (int)X;  // |X| <= 64 after the seven low digits
 }
 
 // v * 2^k by adding k to the exponent field (integer pipe), exact; zero

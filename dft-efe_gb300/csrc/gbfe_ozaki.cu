@@ -17,14 +17,15 @@
 // exact.  The epilogue forms sum_g L_g 2^-7g as an FP32 double-float
 // (error-free TwoSum), converts once to FP64 and applies 2^(ea_j + ex_v + 2).
 // Products with s + t > 9 are below 2^-63 and are dropped.  Result: the FP64
-// product to ~2^-48 relative per entry (normwise), with 36 tensor-core MMAs
-// per K step.
+// product to ~2^-48 relative per entry (normwise); the 36 digit-pair
+// products of a K step are issued as 12 MMAs (N up to 256) over stacked slices.
 //
 // Data movement follows the persistent split-BF16 kernel: A slices are
 // pre-laid-out in HBM (per cell, per K chunk of 32, 8 slices in the canonical
 // K-major core-matrix layout) and land by bulk TMA copies; X rows are gathered
-// by four warps that cut each FP64 value into digits with integer
-// instructions; one thread issues tcgen05.mma; warps 0-3 run the epilogue.
+// by eight warps that cut each FP64 value into digits with integer
+// instructions and also run the epilogue; one thread issues tcgen05.mma, one
+// thread the bulk copies.
 // Cells with more than 128 dofs are processed as two 128-row work items.
 #include "gbfe_internal.cuh"
 #include "gbfe_oz.cuh"
@@ -41,7 +42,9 @@ constexpr int OZ_S = 8;        // slices per operand
 constexpr int OZ_LEVELS = 8;   // g = 2..9
 constexpr int OZ_N = 64;       // vectors per work item (8 levels x 64 = 512 TMEM columns)
 constexpr int OZ_STAGES = 2;
-constexpr int OZ_THREADS = 192;
+constexpr int OZ_GW = 8;                       // gather / epilogue warps
+constexpr int OZ_TMA_WARP = OZ_GW, OZ_MMA_WARP = OZ_GW + 1;
+constexpr int OZ_THREADS = (OZ_GW + 2) * 32;
 constexpr uint32_t OZ_A_PART = 128 * KC * 2;  // one slice of a 128-row A chunk (bytes)
 constexpr uint32_t OZ_B_PART = OZ_N * KC * 2;  // one slice of a B chunk
 constexpr uint32_t OZ_STAGE = OZ_S * (OZ_A_PART + OZ_B_PART);
@@ -139,15 +142,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
   if (tid == 0) {
     for (int s = 0; s < OZ_STAGES; ++s) {
       mbar_init(&full_a[s], 1);
-      mbar_init(&full_b[s], 4);
+      mbar_init(&full_b[s], OZ_GW);
       mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
-    mbar_init(tempty, 4);
+    mbar_init(tempty, OZ_GW);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 5) {
+  if (warp == OZ_MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(a.tmem_cols)
                  : "memory");
@@ -171,7 +174,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
     v0 = (rem % a.vt) * OZ_N;
   };
 
-  if (warp == 4) {
+  if (warp == OZ_TMA_WARP) {
     // ---------------- TMA producer: 8 slice tiles per chunk
     if (lane == 0) {
       uint32_t q = 0;
@@ -196,7 +199,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
       }
     }
     __syncwarp();
-  } else if (warp == 5) {
+  } else if (warp == OZ_MMA_WARP) {
     // ---------------- MMA issuer: 36 products per K step into 8 level accumulators
     if (lane == 0) {
       uint32_t q = 0, li = 0;
@@ -241,7 +244,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
     }
     __syncwarp();
   } else {
-    // ---------------- gather warps 0-3: X rows -> 8 digit slices; epilogue
+    // ---------------- gather warps 0-7: X rows -> 8 digit slices; epilogue
     uint32_t q = 0, li = 0;
     bool ok = true;
     for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
@@ -256,8 +259,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
           if (!ok) break;
         }
         uint8_t *Bst = smem + s * OZ_STAGE + OZ_S * OZ_A_PART;
-        // (KC/8) K blocks x (OZ_N/32) vector groups = 8 items, two per warp
-        for (uint32_t item = warp; item < (KC / 8) * (OZ_N / 32); item += 4) {
+        // (KC/8) K blocks x (OZ_N/32) vector groups = 8 items, one per warp
+        for (uint32_t item = warp; item < (KC / 8) * (OZ_N / 32); item += OZ_GW) {
           const uint32_t kb = item % (KC / 8), vg = item / (KC / 8);
           const uint32_t v = vg * 32 + lane;
           const bool vin = (v0 + v) < m;
@@ -265,17 +268,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
           uint32_t packed[OZ_S][4];
 #pragma unroll
           for (int kk = 0; kk < 8; kk += 2) {
-            int d0[OZ_S], d1[OZ_S];
             const uint32_t k0 = kc * KC + kb * 8 + kk;
             const double x0 = (vin && k0 < nd) ? __ldg(a.X + (uint64_t)a.ids[off + k0] * m + v0 + v) : 0.0;
             const double x1 = (vin && k0 + 1 < nd) ? __ldg(a.X + (uint64_t)a.ids[off + k0 + 1] * m + v0 + v) : 0.0;
-            oz_digits(x0, ex, d0);
-            oz_digits(x1, ex, d1);
+            uint32_t pp[OZ_S];
+            oz::digits_pair_bf16(x0, x1, ex, pp);
 #pragma unroll
-            for (int sl = 0; sl < OZ_S; ++sl) {
-              const __nv_bfloat162 pr = __halves2bfloat162(__int2bfloat16_rn(d0[sl]), __int2bfloat16_rn(d1[sl]));
-              packed[sl][kk / 2] = *reinterpret_cast<const uint32_t *>(&pr);
-            }
+            for (int sl = 0; sl < OZ_S; ++sl) packed[sl][kk / 2] = pp[sl];
           }
           const uint32_t pos = (v / 8) * SBO + kb * LBO + (v % 8) * 16;
 #pragma unroll
@@ -291,15 +290,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
       ok = __all_sync(0xffffffffu, wait(tfull, li & 1, 26));
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t row = mt * 128 + warp * 32 + lane;
+      // warp w reads TMEM lanes of quadrant w % 4, columns [32 (w / 4), +32)
+      const uint32_t quad = warp % 4, colh = warp / 4;
+      const uint32_t row = mt * 128 + quad * 32 + lane;
       const int er = row < nd ? a.row_exp[off + row] : 0;
-      for (uint32_t col = 0; col < OZ_N; col += 16) {
+      for (uint32_t col = colh * 32; col < colh * 32 + 32; col += 16) {
         float hi[16], lo[16];
 #pragma unroll
         for (int q2 = 0; q2 < 16; ++q2) hi[q2] = lo[q2] = 0.f;
         for (int g = OZ_S + 1; g >= 2; --g) {  // smallest level first
           float L[16];
-          tmem_ld16(tmem + ((warp * 32) << 16) + (g - 2) * OZ_N + col, L);
+          tmem_ld16(tmem + ((quad * 32) << 16) + (g - 2) * OZ_N + col, L);
           const float w = __int_as_float((127 - 7 * g) << 23);  // 2^-7g, exact
 #pragma unroll
           for (int q2 = 0; q2 < 16; ++q2) {
@@ -327,7 +328,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 5) {
+  if (warp == OZ_MMA_WARP) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
   }

@@ -49,14 +49,10 @@ __device__ __forceinline__ void store_core_rows(uint8_t *tile, uint32_t part, ui
   uint32_t packed[oz::S][4];
 #pragma unroll
   for (int kk = 0; kk < 8; kk += 2) {
-    int d0[oz::S], d1[oz::S];
-    oz::digits(v[kk], e, d0);
-    oz::digits(v[kk + 1], e, d1);
+    uint32_t pp[oz::S];
+    oz::digits_pair_bf16(v[kk], v[kk + 1], e, pp);
 #pragma unroll
-    for (int s = 0; s < oz::S; ++s) {
-      const __nv_bfloat162 pr = __halves2bfloat162(__int2bfloat16_rn(d0[s]), __int2bfloat16_rn(d1[s]));
-      packed[s][kk / 2] = *reinterpret_cast<const uint32_t *>(&pr);
-    }
+    for (int s = 0; s < oz::S; ++s) packed[s][kk / 2] = pp[s];
   }
 #pragma unroll
   for (int s = 0; s < oz::S; ++s)
