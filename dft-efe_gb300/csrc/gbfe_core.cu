@@ -378,6 +378,21 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
   assemble_cells(me, c, GBFE_F64, op->cellbuf.p, Y);
 }
 
+void h2d_staged(gbfe_ctx *ctx, PinnedSlot &slot, void *dst, const void *src, size_t n) {
+  if (!n) return;
+  if (slot.done) GBFE_CUDA(cudaEventSynchronize(slot.done));  // the previous staged copy has left
+  if (slot.cap < n) {
+    if (slot.h) GBFE_CUDA(cudaFreeHost(slot.h));
+    slot.h = nullptr;
+    GBFE_CUDA(cudaMallocHost(&slot.h, n));
+    slot.cap = n;
+  }
+  if (!slot.done) GBFE_CUDA(cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming));
+  std::memcpy(slot.h, src, n);
+  GBFE_CUDA(cudaMemcpyAsync(dst, slot.h, n, cudaMemcpyHostToDevice, ctx->stream));
+  GBFE_CUDA(cudaEventRecord(slot.done, ctx->stream));
+}
+
 void assemble_cells(gbfe_mesh *me, const gbfe_cons *c, int dtype, const void *Yc, gbfe_mv *Y) {
   gbfe_ctx *ctx = me->ctx;
   const bool has_par = c && !c->pure_dirichlet;

@@ -132,6 +132,22 @@ struct TcTune {
   float ms = 0.f;
 };
 
+// Pinned host staging for small host-to-device copies issued inside a solve:
+// a copy from pageable memory synchronises the stream first, one from pinned
+// memory does not.  `done` marks when the staged bytes may be overwritten.
+struct PinnedSlot {
+  void *h = nullptr;
+  size_t cap = 0;
+  cudaEvent_t done = nullptr;
+  PinnedSlot() = default;
+  PinnedSlot(const PinnedSlot &) = delete;
+  PinnedSlot &operator=(const PinnedSlot &) = delete;
+  ~PinnedSlot() {
+    if (done) cudaEventDestroy(done);
+    if (h) cudaFreeHost(h);
+  }
+};
+
 struct gbfe_ctx {
   int device = 0;
   std::map<std::tuple<uint32_t, uint32_t, uint32_t>, TcTune> tc_tune;
@@ -164,6 +180,8 @@ struct gbfe_ctx {
   gbfe::DBuf<int> oz_exp, oz_rexp;  // sliced products: column / row exponents
   gbfe::DBuf<int> oz_ipart;         // partial exponent maxima
   std::vector<std::unique_ptr<gbfe::DBuf<double>>> vec_pool;  // scoped m-vectors of a pass (LIFO)
+  std::vector<std::unique_ptr<PinnedSlot>> vec_pin;            // their host staging
+  PinnedSlot pin_small;                                        // m x m eigenvectors
   size_t vec_top = 0;
   gbfe::DBuf<double> oz_part;       // per-item Gram partials
   gbfe::DBuf<__nv_bfloat16> oz_tdig;  // slices of the rotation factor
@@ -327,6 +345,8 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *
 bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_mv *R, const double *coef,
                        const double *eF2, const gbfe_mv *Y);
 // nonlocal part: W = V * (sum over slots of C_c X_c) and Yc += C_c^T W
+// host -> device copy of n bytes through a pinned staging slot (no stream sync)
+void h2d_staged(gbfe_ctx *ctx, PinnedSlot &slot, void *dst, const void *src, size_t n);
 // Y = assembled cell-wise buffer Yc with the constraint epilogue of `cons`
 void assemble_cells(gbfe_mesh *me, const gbfe_cons *cons, int dtype, const void *Yc, gbfe_mv *Y);
 void nonlocal_project(const gbfe_nl *nl, const gbfe_mv *X);

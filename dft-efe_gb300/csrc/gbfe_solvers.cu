@@ -195,18 +195,20 @@ void d_coldots(gbfe_ctx *ctx, const gbfe_mv *x, const gbfe_mv *y, double *out_d,
 struct DevVec {
   gbfe_ctx *ctx;
   double *p;
+  size_t idx;
   DevVec(gbfe_ctx *c, size_t n) : ctx(c) {
-    const size_t idx = ctx->vec_top++;
-    if (ctx->vec_pool.size() <= idx) ctx->vec_pool.emplace_back(new DBuf<double>());
+    idx = ctx->vec_top++;
+    if (ctx->vec_pool.size() <= idx) {
+      ctx->vec_pool.emplace_back(new DBuf<double>());
+      ctx->vec_pin.emplace_back(new PinnedSlot());
+    }
     ctx->vec_pool[idx]->ensure(std::max<size_t>(n, 1));
     p = ctx->vec_pool[idx]->p;
   }
   ~DevVec() { --ctx->vec_top; }
   DevVec(const DevVec &) = delete;
   DevVec &operator=(const DevVec &) = delete;
-  void set(gbfe_ctx *, const double *h, size_t n) {
-    GBFE_CUDA(cudaMemcpyAsync(p, h, n * 8, cudaMemcpyHostToDevice, ctx->stream));
-  }
+  void set(gbfe_ctx *, const double *h, size_t n) { h2d_staged(ctx, *ctx->vec_pin[idx], p, h, n * 8); }
   void get(gbfe_ctx *, double *h, size_t n) const {
     GBFE_CUDA(cudaMemcpyAsync(h, p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
     GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -290,8 +292,7 @@ int small_syevd(gbfe_ctx *ctx, int m, double *dA, double *eig_h, std::string &ms
       msg = "LAPACK_ERROR: FAILED_STANDARD_EIGENPROBLEM (QR iteration did not converge)";
       return GBFE_ERR_LAPACK;
     }
-    // pageable source: the call returns once the data is staged
-    GBFE_CUDA(cudaMemcpyAsync(dA, h.data(), h.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    h2d_staged(ctx, ctx->pin_small, dA, h.data(), h.size() * 8);
     return GBFE_OK;
   }
   DevVec W(ctx, m);
@@ -398,6 +399,7 @@ void launch_cheb_step<float>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha
 struct FilterWork {
   std::unique_ptr<gbfe_mv> s1, s2, R, RN, Yf;
   DBuf<double> tab, coef;
+  PinnedSlot pin_tab, pin_coef;
   cudaGraphExec_t exec = nullptr;
   std::vector<GraphProf> prof;
   uint64_t per_replay = 0;
@@ -457,8 +459,8 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
   std::vector<double> ones(m, 1.0);
   d_ones.set(ctx, ones.data(), m);
   d_eig.set(ctx, eig_h, m);
-  GBFE_CUDA(cudaMemcpyAsync(w.tab.p, s.eF2.data(), s.eF2.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
-  GBFE_CUDA(cudaMemcpyAsync(w.coef.p, coef.data(), coef.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  h2d_staged(ctx, w.pin_tab, w.tab.p, s.eF2.data(), s.eF2.size() * 8);
+  h2d_staged(ctx, w.pin_coef, w.coef.p, coef.data(), coef.size() * 8);
   gbfe_mv *s1 = w.s1.get(), *s2 = w.s2.get();
   std::unique_ptr<gbfe_mv> &R = w.R, &RN = w.RN;
   if (R0) {
