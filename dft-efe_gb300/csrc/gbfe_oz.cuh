@@ -96,6 +96,20 @@ __device__ __forceinline__ double scale2(double v, int k) {
   return __longlong_as_double(b + ((long long)k << 52));
 }
 
+// float -> double by moving the bit fields (integer pipe; the FP64 pipe is the
+// scarce one).  Exact for zero and normal floats, which is all the level
+// sums and their TwoSum errors can be (integer multiples of 2^-63 or zero).
+__device__ __forceinline__ double f2d(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double((long long)sign);
+  return __longlong_as_double((long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(u & 0x7fffffu) << 29)));
+}
+
+// hi + lo of a double-float as one FP64 add
+__device__ __forceinline__ double df_to_double(float hi, float lo) { return f2d(hi) + f2d(lo); }
+
 // 2^k as a double (k within the normal range)
 __device__ __forceinline__ double pow2(int k) { return __longlong_as_double((long long)(uint64_t)(k + 1023) << 52); }
 

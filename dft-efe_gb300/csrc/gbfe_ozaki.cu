@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
           for (int q2 = 0; q2 < 16; ++q2) {
             const uint32_t v = v0 + col + q2;
             if (v < m) {
-              dst[q2] = oz::scale2((double)hi[q2] + (double)lo[q2], er + a.x_exp[v] + 2);
+              dst[q2] = oz::scale2(oz::df_to_double(hi[q2], lo[q2]), er + a.x_exp[v] + 2);
             }
           }
         }

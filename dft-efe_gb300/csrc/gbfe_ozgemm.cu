@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
           float hi[16], lo[16];
           combine16(tmem + ((quad * 32) << 16) + colh * 32 + cg * 16, hi, lo);
 #pragma unroll
-          for (int i = 0; i < 16; ++i) acc[cg * 16 + i] += (double)hi[i] + (double)lo[i];
+          for (int i = 0; i < 16; ++i) acc[cg * 16 + i] += oz::df_to_double(hi[i], lo[i]);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncwarp();
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
           double *dst = a.out[op] + orow * a.mo + j0;
 #pragma unroll
           for (int i = 0; i < 16; ++i)
-            if (j0 + i < a.mo) dst[i] = oz::scale2((double)hi[i] + (double)lo[i], oe + a.texp[j0 + i] + 2);
+            if (j0 + i < a.mo) dst[i] = oz::scale2(oz::df_to_double(hi[i], lo[i]), oe + a.texp[j0 + i] + 2);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
