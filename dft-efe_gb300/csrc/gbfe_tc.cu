@@ -229,16 +229,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_cell_apply_tc(
 
 // ---------------------------------------------------------------------------
 // v2: persistent, warp-specialised, continuous chunk stream across cells.
-//   warps 0-3  gather X chunks into the B ring (one mbarrier arrive per warp per
-//              chunk) and run the epilogue of the previous cell (TMEM -> Yc)
-//   warp 4     lane 0 issues the bulk TMA copies of A up to `stages` chunks ahead
-//   warp 5     allocates TMEM; lane 0 issues tcgen05.mma and the commits
+//   warps 0-7  gather X chunks into the B ring (one mbarrier arrive per warp per
+//              chunk) and run the epilogue of the previous cell (TMEM -> Yc;
+//              warp w reads the lanes of quadrant w % 4, every other 16 columns)
+//   warp 8     lane 0 issues the bulk TMA copies of A up to `stages` chunks ahead
+//   warp 9     allocates TMEM; lane 0 issues tcgen05.mma and the commits
+// Two CTAs per SM (registers capped by the launch bounds) keep 16 gather warps
+// in flight per SM: the gather's indirect row loads are the latency to hide.
 // TMEM holds `nbuf` accumulator buffers so one cell's epilogue overlaps the
 // next cell's MMAs.  The main loop synchronises through mbarriers only.
 // ---------------------------------------------------------------------------
 constexpr int MAX_STAGES = 4;
-constexpr int GATHER_WARPS = 4;
-constexpr int THREADS2 = 192;
+constexpr int GATHER_WARPS = 8;
+constexpr int TMA_WARP2 = GATHER_WARPS, MMA_WARP2 = GATHER_WARPS + 1;
+constexpr int THREADS2 = (GATHER_WARPS + 2) * 32;
 
 struct Tc2Args {
   const float *X;
@@ -258,7 +262,7 @@ struct Tc2Args {
   const float *xscale;
 };
 
-__global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a) {
+__global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t N = a.N, mtiles = a.mtiles, S = a.stages, nbuf = a.nbuf, m = a.m;
@@ -289,7 +293,7 @@ __global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a)
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 5) {
+  if (warp == MMA_WARP2) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(a.tmem_cols)
                  : "memory");
@@ -307,7 +311,7 @@ __global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a)
     return false;
   };
 
-  if (warp == 4) {
+  if (warp == TMA_WARP2) {
     // ---------------- TMA producer for A
     if (lane == 0) {
       uint32_t q = 0;
@@ -329,7 +333,7 @@ __global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a)
       }
     }
     __syncwarp();  // lanes 1-31 wait for lane 0 before the CTA barrier
-  } else if (warp == 5) {
+  } else if (warp == MMA_WARP2) {
     // ---------------- MMA issuer
     if (lane == 0) {
       const uint32_t idesc = instr_desc(128, (int)N);
@@ -383,11 +387,12 @@ __global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a)
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) return false;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t quad = warp % 4;
       for (uint32_t t = 0; t < mtiles; ++t) {
-        const uint32_t row = t * 128 + warp * 32 + lane;
-        for (uint32_t col = 0; col < N; col += 16) {
+        const uint32_t row = t * 128 + quad * 32 + lane;
+        for (uint32_t col = (warp / 4) * 16; col < N; col += 32) {
           float v[16];
-          tmem_ld16(tmem + ((warp * 32) << 16) + (b * mtiles + t) * N + col, v);
+          tmem_ld16(tmem + ((quad * 32) << 16) + (b * mtiles + t) * N + col, v);
           if (row < nd) {
             float *dst = a.Yc + (uint64_t)(off + row) * m + v0 + col;
             const uint32_t nvalid = min(16u, m - min(m, v0 + col));
@@ -477,7 +482,7 @@ __global__ void __launch_bounds__(THREADS2, 1) k_cell_apply_tc2(const Tc2Args a)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 5) {
+  if (warp == MMA_WARP2) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
   }
@@ -534,7 +539,7 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
   const uint32_t nbuf = (2 * mtiles * N <= 512) ? 2 : 1;
   uint32_t cols = 32;
   while (cols < nbuf * mtiles * N) cols *= 2;
-  const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>((227 * 1024) / smem, 512 / cols));
+  const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(std::min<uint32_t>((227 * 1024) / smem, 512 / cols), 2));
   const uint32_t items = ncell * vt;
   const uint32_t grid = std::min<uint32_t>(items, per_sm * (uint32_t)ctx->sm_count);
   static bool attr_set = false;
