@@ -357,6 +357,7 @@ def run_gpu(args, cfg_name, rank, world):
     st_dense = {k: ctx.kernel_stats(k) for k in ("gram_f64_oz", "rotate_f64_oz", "gram_f64_dgemm",
                                                   "rotate_f64_dgemm")}
     st_eig = ctx.kernel_stats("eig_small_f64")
+    st_pass = {k: ctx.kernel_stats(k) for k in ("pass_total", "pass_filter", "pass_fp64_applies")}
     ctx.set_profiling(False)
 
     # e2e: the same solve through the C ABI with host buffers each step
@@ -376,7 +377,7 @@ def run_gpu(args, cfg_name, rank, world):
     fp64_peak = ctx.probe_fp64_peak()
     return dict(cfg=cfg, prob=prob, deg=deg, bounds=(wl, wu, uu), fp64_times=fp64_times, passes64=passes64,
                 rc64=rc64, lat=lat, errs=errs, passes=passes, ok=ok, t_total=t_total, launches=launches,
-                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, st_dense=st_dense, st_eig=st_eig, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
+                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, st_dense=st_dense, st_eig=st_eig, st_pass=st_pass, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
                 h2d=prob.n_dofs * m * 8, d2h=prob.n_dofs * m * 8 + 2 * m * 8)
 
 
@@ -694,6 +695,8 @@ def main():
     roof = roofline(dom, cand[dom], r["fp64_peak"])
     others = {k: v for k, v in cand.items() if k != dom and v["launches"]}
     others["eig_small_f64 (potrf, trsm, syevd block; includes its host sync)"] = r["st_eig"]
+    # device-timeline spans of the fused pass (CUDA events; idle gaps included)
+    others.update({f"{k} (span)": v for k, v in r["st_pass"].items()})
     e2e_sps = world / float(np.mean(r["e2e_lat"]))
     line = {
         "metric": "ChFSI solves/s at |d_eps|<=1e-6 Ha (mixed precision), FP64 beside it",

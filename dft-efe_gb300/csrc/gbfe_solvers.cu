@@ -696,9 +696,16 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   gbfe_ctx *ctx = X->mesh->ctx;
   const int m = (int)X->m;
   const int N = (int)X->mesh->n_dofs;
-  residual_filter(A, B, BInv, eig_h, X, degree, wl, wu, uu, st.Y.get(), prec, st.R.get(), &st.fw);
-  apply_op(B, st.Y.get(), st.MY.get());
-  apply_op(A, st.Y.get(), st.HY.get());
+  ProfScope prof_pass(ctx, "pass_total", 0.0, 0.0);
+  {
+    ProfScope prof(ctx, "pass_filter", 0.0, 0.0);
+    residual_filter(A, B, BInv, eig_h, X, degree, wl, wu, uu, st.Y.get(), prec, st.R.get(), &st.fw);
+  }
+  {
+    ProfScope prof(ctx, "pass_fp64_applies", 0.0, 0.0);
+    apply_op(B, st.Y.get(), st.MY.get());
+    apply_op(A, st.Y.get(), st.HY.get());
+  }
   // FP64 Gram matrices and rotations: the sliced tensor-core products when
   // the FP64 applies use them, else DGEMM
   const bool oz_dense = ctx->fp64_tc && ctx->fp64_tc_dense && oz_gemm_supported(ctx, (uint32_t)m);
