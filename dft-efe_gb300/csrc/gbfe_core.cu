@@ -534,6 +534,12 @@ int gbfe_ctx_destroy(gbfe_ctx *ctx) {
   ctx->small.reset();
   ctx->info.reset();
   ctx->lwork.reset();
+  for (auto &kv : ctx->kstats)
+    for (auto &pr : kv.second.pending) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  for (cudaEvent_t e : ctx->event_free) cudaEventDestroy(e);
   if (ctx->cusolver) cusolverDnDestroy(ctx->cusolver);
   if (ctx->cublas) cublasDestroy(ctx->cublas);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -651,8 +657,8 @@ int gbfe_ctx_kernel_stats(gbfe_ctx *ctx, const char *name, uint64_t *launches, d
       float ms = 0.f;
       GBFE_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
       st.ms += ms;
-      cudaEventDestroy(pr.first);
-      cudaEventDestroy(pr.second);
+      ctx->event_free.push_back(pr.first);
+      ctx->event_free.push_back(pr.second);
     }
     st.pending.clear();
     if (launches) *launches = st.launches;
@@ -668,8 +674,8 @@ int gbfe_ctx_reset_kernel_stats(gbfe_ctx *ctx) {
     GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
     for (auto &kv : ctx->kstats)
       for (auto &pr : kv.second.pending) {
-        cudaEventDestroy(pr.first);
-        cudaEventDestroy(pr.second);
+        ctx->event_free.push_back(pr.first);
+        ctx->event_free.push_back(pr.second);
       }
     ctx->kstats.clear();
   });

@@ -156,6 +156,7 @@ struct gbfe_ctx {
   std::vector<GraphProf> *capture_prof = nullptr;  // set while a graph is captured with profiling on
   int use_graphs = 1;        // capture the Chebyshev recurrence into a CUDA graph
   std::map<std::string, KernelStat> kstats;
+  std::vector<cudaEvent_t> event_free;  // recycled timing events of ProfScope
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   cublasHandle_t cublas = nullptr;
@@ -298,10 +299,20 @@ struct ProfScope {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   const char *nm = nullptr;
   double fl = 0, by = 0;
+  static cudaEvent_t get(gbfe_ctx *c) {
+    cudaEvent_t e = nullptr;
+    if (!c->event_free.empty()) {
+      e = c->event_free.back();
+      c->event_free.pop_back();
+    } else {
+      cudaEventCreate(&e);
+    }
+    return e;
+  }
   ProfScope(gbfe_ctx *c, const char *name, double flops, double bytes) : ctx(c), nm(name), fl(flops), by(bytes) {
     if (!ctx->profiling) return;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    e0 = get(ctx);
+    e1 = get(ctx);
     if (ctx->capture_prof) {  // inside a graph: an event-record node, read after each replay
       cudaEventRecordWithFlags(e0, ctx->stream, cudaEventRecordExternal);
       return;
