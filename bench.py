@@ -361,6 +361,9 @@ def run_gpu(args, cfg_name, rank, world):
                                                   "rotate_f64_dgemm")}
     st_eig = ctx.kernel_stats("eig_small_f64")
     st_pass = {k: ctx.kernel_stats(k) for k in ("pass_total", "pass_filter", "pass_fp64_applies")}
+    st_small = {k: ctx.kernel_stats(k) for k in ("k:p2c", "k:diag_apply", "k:assemble_f64", "k:assemble_f32",
+                                                  "k:assemble_cheb", "k:cheb_final_mixed", "k:axpby",
+                                                  "k:axpby_blocked", "k:coldot_partial", "k:convert", "k:fill")}
     ctx.set_profiling(False)
 
     # e2e: the same solve through the C ABI with host buffers each step
@@ -380,7 +383,7 @@ def run_gpu(args, cfg_name, rank, world):
     fp64_peak = ctx.probe_fp64_peak()
     return dict(cfg=cfg, prob=prob, deg=deg, bounds=(wl, wu, uu), tuned=tuned, fp64_times=fp64_times, passes64=passes64,
                 rc64=rc64, lat=lat, errs=errs, passes=passes, ok=ok, t_total=t_total, launches=launches,
-                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, st_dense=st_dense, st_eig=st_eig, st_pass=st_pass, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
+                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, st_dense=st_dense, st_eig=st_eig, st_pass=st_pass, st_small=st_small, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
                 h2d=prob.n_dofs * m * 8, d2h=prob.n_dofs * m * 8 + 2 * m * 8)
 
 
@@ -700,6 +703,7 @@ def main():
     others["eig_small_f64 (potrf, trsm, syevd block; includes its host sync)"] = r["st_eig"]
     # device-timeline spans of the fused pass (CUDA events; idle gaps included)
     others.update({f"{k} (span)": v for k, v in r["st_pass"].items()})
+    others.update({k: v for k, v in r["st_small"].items() if v["launches"]})
     e2e_sps = world / float(np.mean(r["e2e_lat"]))
     line = {
         "metric": "ChFSI solves/s at |d_eps|<=1e-6 Ha (mixed precision), FP64 beside it",

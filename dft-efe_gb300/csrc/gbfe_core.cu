@@ -235,6 +235,7 @@ namespace gbfe {
 
 void constraints_p2c(gbfe_ctx *ctx, const gbfe_cons *c, gbfe_mv *x) {
   if (!c || c->n_rows == 0 || x->m == 0) return;
+  ProfScope prof_k(ctx, "k:p2c", 0.0, 0.0);
   const uint64_t n = (uint64_t)c->n_rows * x->m;
   if (c->pure_dirichlet) {
     if (x->dtype == GBFE_F64)
@@ -350,6 +351,7 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
     return;
   }
   if (op->kind == OP_DIAG) {
+    ProfScope prof_k(ctx, "k:diag_apply", 0.0, 0.0);
     const uint8_t *isr = c ? c->is_row.p : nullptr;
     if (X->dtype == GBFE_F64)
       k_diag_apply<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
@@ -399,15 +401,21 @@ void assemble_cells(gbfe_mesh *me, const gbfe_cons *c, int dtype, const void *Yc
   const uint64_t n = (uint64_t)me->n_dofs * Y->m;
   const uint8_t *isr = c ? c->is_row.p : nullptr;
   if (dtype == GBFE_F64) {
-    k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
-        static_cast<const double *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
-        has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->d.p);
-    check_launch(ctx, "assemble_f64");
+    {
+      ProfScope prof_k(ctx, "k:assemble_f64", 0.0, 0.0);
+      k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+          static_cast<const double *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
+          has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->d.p);
+      check_launch(ctx, "assemble_f64");
+    }
   } else {
-    k_assemble<float, float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
-        static_cast<const float *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
-        has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->f.p);
-    check_launch(ctx, "assemble_f32");
+    {
+      ProfScope prof_k(ctx, "k:assemble_f32", 0.0, 0.0);
+      k_assemble<float, float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+          static_cast<const float *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
+          has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->f.p);
+      check_launch(ctx, "assemble_f32");
+    }
   }
 }
 
@@ -433,10 +441,13 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
   A->cellbuf_f32.ensure((size_t)me->total_cell_dofs * m);
   cell_apply_tc(A, RN, A->cellbuf_f32.p, BInv->diag_gather.p);
   const uint64_t n = (uint64_t)me->n_dofs * m;
-  k_assemble_cheb<<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p,
-                                                               me->slot.p, c ? c->is_row.p : nullptr, coef, RN->f.p,
-                                                               R->f.p, eF2, Y->f.p);
-  check_launch(ctx, "assemble_cheb");
+  {
+    ProfScope prof_k(ctx, "k:assemble_cheb", 0.0, 0.0);
+    k_assemble_cheb<<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p,
+                                                                 me->slot.p, c ? c->is_row.p : nullptr, coef, RN->f.p,
+                                                                 R->f.p, eF2, Y->f.p);
+    check_launch(ctx, "assemble_cheb");
+  }
   return true;
 }
 

@@ -402,11 +402,31 @@ struct FilterWork {
   PinnedSlot pin_tab, pin_coef;
   cudaGraphExec_t exec = nullptr;
   std::vector<GraphProf> prof;
+  gbfe_ctx *prof_ctx = nullptr;  // replay whose event timings are not read yet
   uint64_t per_replay = 0;
   const gbfe_op *A = nullptr, *BInv = nullptr;
   uint32_t degree = 0, m = 0;
   int prec = -1, uses = 0, graph_failed = 0;
+  // kernel timings of the last replay (event-record nodes inside the graph);
+  // read lazily, before the next replay or when the graph goes away, so the
+  // profiled run does not wait for each replay
+  void flush_prof() {
+    if (!prof_ctx) return;
+    gbfe_ctx *ctx = prof_ctx;
+    prof_ctx = nullptr;
+    if (prof.empty() || cudaEventSynchronize(prof.back().e1) != cudaSuccess) return;
+    for (auto &g : prof) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, g.e0, g.e1) != cudaSuccess) continue;
+      KernelStat &st = ctx->kstats[g.name];
+      st.ms += ms;
+      st.launches++;
+      st.flops += g.flops;
+      st.bytes += g.bytes;
+    }
+  }
   void drop_graph() {
+    flush_prof();
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
     for (auto &g : prof) {
@@ -537,21 +557,10 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
     }
   }
   if (can_graph && w.exec) {
+    w.flush_prof();  // the previous replay's events, before this replay re-records them
     GBFE_CUDA(cudaGraphLaunch(w.exec, ctx->stream));
     ctx->launches += w.per_replay;
-    if (!w.prof.empty()) {
-      // kernel timings of this replay (event-record nodes inside the graph)
-      GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
-      for (auto &g : w.prof) {
-        float ms = 0.f;
-        GBFE_CUDA(cudaEventElapsedTime(&ms, g.e0, g.e1));
-        KernelStat &st = ctx->kstats[g.name];
-        st.ms += ms;
-        st.launches++;
-        st.flops += g.flops;
-        st.bytes += g.bytes;
-      }
-    }
+    if (!w.prof.empty() && ctx->profiling) w.prof_ctx = ctx;
   } else {
     recurrence();
   }
@@ -562,8 +571,11 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
   gbfe_mv *Rfin = other;
   const double *eF2_final = w.tab.p + (size_t)(degree - 1) * m;
   if (mixed) {
-    k_cheb_final_mixed<<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, Rfin->f.p, eF2_final, X->d.p, Y->d.p);
-    check_launch(ctx, "cheb_final_mixed");
+    {
+      ProfScope prof_k(ctx, "k:cheb_final_mixed", 0.0, 0.0);
+      k_cheb_final_mixed<<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, Rfin->f.p, eF2_final, X->d.p, Y->d.p);
+      check_launch(ctx, "cheb_final_mixed");
+    }
   } else {
     d_axpby_blocked(ctx, 1.0, d_ones.p, Rfin, 1.0, eF2_final, X, Y);
   }
