@@ -230,6 +230,12 @@ class CpuBaseline:
         self.tmp.cleanup()
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# dominant kernel, from one ncu capture of the same workload's apply
+# (profiles/k_cell_apply_tc2_cfg2.md: the two launches of one apply moved
+# 116.7 + 45.6 MB; averaged per launch like the algorithmic bytes)
+NCU_TRAFFIC_PER_LAUNCH = {("cfg2", "cell_apply_mixed"): (116.7e6 + 45.6e6) / 2}
+
 # BF16 tensor-core products per FP64-accurate sliced product (8 x 8 digit
 # pairs with s + t <= 9)
 SLICED_PRODUCTS = 36
@@ -699,6 +705,7 @@ def main():
             **r["st_dense"]}
     dom = max(cand, key=lambda k: cand[k]["ms"])
     roof = roofline(dom, cand[dom], r["fp64_peak"])
+    roof["traffic"] = NCU_TRAFFIC_PER_LAUNCH.get((args.config, dom))
     others = {k: v for k, v in cand.items() if k != dom and v["launches"]}
     others["eig_small_f64 (potrf, trsm, syevd block; includes its host sync)"] = r["st_eig"]
     # device-timeline spans of the fused pass (CUDA events; idle gaps included)
