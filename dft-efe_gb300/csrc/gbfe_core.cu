@@ -115,12 +115,13 @@ __global__ void k_assemble(const TC *__restrict__ Yc, uint32_t m, uint64_t n_dof
                            const uint32_t *__restrict__ slot_ptr, const uint32_t *__restrict__ slot,
                            const uint8_t *__restrict__ is_row, const uint32_t *__restrict__ par_ptr,
                            const uint32_t *__restrict__ par_row, const double *__restrict__ par_w,
-                           TY *__restrict__ Y) {
+                           TY *__restrict__ Y, const FastDiv fm) {
   const uint64_t total = n_dofs * m;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
        t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t i = t / m;
-    const uint32_t v = (uint32_t)(t - i * m);
+    uint64_t i;
+    uint32_t v;
+    fm.divmod(t, i, v);
     if (is_row && is_row[i]) {
       Y[t] = (TY)0;
       continue;
@@ -155,13 +156,14 @@ __global__ void k_assemble_cheb(const float *__restrict__ Yc, uint32_t m, uint64
                                 const uint32_t *__restrict__ slot_ptr, const uint32_t *__restrict__ slot,
                                 const uint8_t *__restrict__ is_row, const double *__restrict__ coef,
                                 const float *__restrict__ RN, float *__restrict__ R, const double *__restrict__ eF2,
-                                const float *__restrict__ Y) {
+                                const float *__restrict__ Y, const FastDiv fm) {
   const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
   const uint64_t total = n_dofs * m;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
        t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t i = t / m;
-    const uint32_t v = (uint32_t)(t - i * m);
+    uint64_t i;
+    uint32_t v;
+    fm.divmod(t, i, v);
     float acc = 0.f;
     if (!(is_row && is_row[i]))
       for (uint32_t p = slot_ptr[i], e = slot_ptr[i + 1]; p < e; ++p) acc = acc + Yc[(uint64_t)slot[p] * m + v];
@@ -176,12 +178,13 @@ template <class T>
 __global__ void k_diag_apply(const T *__restrict__ X, uint32_t m, uint64_t n_dofs, const double *__restrict__ d,
                              const uint8_t *__restrict__ is_row, const uint32_t *__restrict__ par_ptr,
                              const uint32_t *__restrict__ par_row, const double *__restrict__ par_w,
-                             T *__restrict__ Y) {
+                             T *__restrict__ Y, const FastDiv fm) {
   const uint64_t total = n_dofs * m;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
        t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t i = t / m;
-    const uint32_t v = (uint32_t)(t - i * m);
+    uint64_t i;
+    uint32_t v;
+    fm.divmod(t, i, v);
     if (is_row && is_row[i]) {
       Y[t] = (T)0;
       continue;
@@ -318,10 +321,10 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
   if (op->kind == OP_JACOBI) {
     if (X->dtype == GBFE_F64)
       k_diag_apply<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->d.p, m, me->n_dofs, op->diag.p, nullptr,
-                                                                         nullptr, nullptr, nullptr, Y->d.p);
+                                                                         nullptr, nullptr, nullptr, Y->d.p, FastDiv(m));
     else
       k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->f.p, m, me->n_dofs, op->diag.p, nullptr,
-                                                                        nullptr, nullptr, nullptr, Y->f.p);
+                                                                        nullptr, nullptr, nullptr, Y->f.p, FastDiv(m));
     check_launch(ctx, "jacobi_apply");
     return;
   }
@@ -331,10 +334,10 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
     // dof, the enrichment rows replaced by block * X_enr, then child-to-parent
     if (X->dtype == GBFE_F64)
       k_diag_apply<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->d.p, m, me->n_dofs, op->diag.p, nullptr,
-                                                                         nullptr, nullptr, nullptr, Y->d.p);
+                                                                         nullptr, nullptr, nullptr, Y->d.p, FastDiv(m));
     else
       k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->f.p, m, me->n_dofs, op->diag.p, nullptr,
-                                                                        nullptr, nullptr, nullptr, Y->f.p);
+                                                                        nullptr, nullptr, nullptr, Y->f.p, FastDiv(m));
     check_launch(ctx, "diag_apply");
     const int nb = (int)op->blk_n, mm = (int)m;
     if (X->dtype == GBFE_F64) {
@@ -356,11 +359,11 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
     if (X->dtype == GBFE_F64)
       k_diag_apply<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
           X->d.p, m, me->n_dofs, op->diag.p, isr, has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr,
-          has_par ? c->par_w.p : nullptr, Y->d.p);
+          has_par ? c->par_w.p : nullptr, Y->d.p, FastDiv(m));
     else
       k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
           X->f.p, m, me->n_dofs, op->diag.p, isr, has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr,
-          has_par ? c->par_w.p : nullptr, Y->f.p);
+          has_par ? c->par_w.p : nullptr, Y->f.p, FastDiv(m));
     check_launch(ctx, "diag_apply");
     return;
   }
@@ -405,7 +408,8 @@ void assemble_cells(gbfe_mesh *me, const gbfe_cons *c, int dtype, const void *Yc
       ProfScope prof_k(ctx, "k:assemble_f64", 0.0, 0.0);
       k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
           static_cast<const double *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
-          has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->d.p);
+          has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->d.p,
+          FastDiv(Y->m));
       check_launch(ctx, "assemble_f64");
     }
   } else {
@@ -413,7 +417,8 @@ void assemble_cells(gbfe_mesh *me, const gbfe_cons *c, int dtype, const void *Yc
       ProfScope prof_k(ctx, "k:assemble_f32", 0.0, 0.0);
       k_assemble<float, float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
           static_cast<const float *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
-          has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->f.p);
+          has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->f.p,
+          FastDiv(Y->m));
       check_launch(ctx, "assemble_f32");
     }
   }
@@ -432,20 +437,33 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
   gbfe_ctx *ctx = me->ctx;
   const gbfe_cons *c = BInv->cons;
   if (RN->dtype != GBFE_F32 || A->kind != OP_CELL || !(A->prec & GBFE_PREC_MIXED) || A->nl || !ctx->use_tc ||
-      ctx->tc_version != 2 || !A->tc_aoff.p || BInv->kind != OP_DIAG || BInv->mesh != me || A->cons != c ||
-      (c && !c->pure_dirichlet) || RN->m == 0)
+      ctx->tc_version != 2 || !A->tc_aoff.p || (BInv->kind != OP_DIAG && BInv->kind != OP_DIAG_BLOCK) ||
+      BInv->mesh != me || A->cons != c || (c && !c->pure_dirichlet) || RN->m == 0)
     return false;
   const uint32_t m = RN->m;
   if (!BInv->diag_gather.p) return false;  // built at upload for diagonal operators
   constraints_p2c(ctx, c, RN);  // BInv's parent-to-child on its input, as apply_op does
+  const float *xsub = nullptr;
+  if (BInv->kind == OP_DIAG_BLOCK) {
+    // the enrichment rows of B^-1 RN: the dense block times those rows of RN,
+    // the same cuBLAS call as the separate B^-1 apply
+    const int nb = (int)BInv->blk_n, mm = (int)m;
+    BInv->blk_out_f32.ensure((size_t)BInv->blk_n * m);
+    const float one = 1.f, zero = 0.f;
+    GBFE_CUBLAS(cublasSgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, mm, nb, nb, &one, RN->f.p + BInv->blk_begin * m,
+                            mm, BInv->blk_f32.p, nb, &zero, BInv->blk_out_f32.p, mm));
+    count_launch(ctx);
+    xsub = BInv->blk_out_f32.p;
+  }
   A->cellbuf_f32.ensure((size_t)me->total_cell_dofs * m);
-  cell_apply_tc(A, RN, A->cellbuf_f32.p, BInv->diag_gather.p);
+  cell_apply_tc(A, RN, A->cellbuf_f32.p, BInv->diag_gather.p, xsub, (uint32_t)BInv->blk_begin,
+                xsub ? (uint32_t)BInv->blk_n : 0u);
   const uint64_t n = (uint64_t)me->n_dofs * m;
   {
     ProfScope prof_k(ctx, "k:assemble_cheb", 0.0, 0.0);
     k_assemble_cheb<<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p,
                                                                  me->slot.p, c ? c->is_row.p : nullptr, coef, RN->f.p,
-                                                                 R->f.p, eF2, Y->f.p);
+                                                                 R->f.p, eF2, Y->f.p, FastDiv(m));
     check_launch(ctx, "assemble_cheb");
   }
   return true;
@@ -985,7 +1003,7 @@ static int diag_upload_impl(gbfe_mesh *mesh, const gbfe_cons *cons, const double
       GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
     } else {
       op->diag.upload(diag, mesh->n_dofs, mesh->ctx->stream);
-      if (kind == OP_DIAG && (!cons || cons->pure_dirichlet)) {
+      if ((kind == OP_DIAG || kind == OP_DIAG_BLOCK) && (!cons || cons->pure_dirichlet)) {
         // gather factor of the fused mixed filter step
         op->diag_gather.alloc(mesh->n_dofs);
         k_diag_gather<<<grid_for(mesh->n_dofs, 256), 256, 0, mesh->ctx->stream>>>(
@@ -1226,7 +1244,7 @@ extern "C" int gbfe_apply_f64_noalloc(const gbfe_op *op, double *X_dev, double *
     const uint64_t n = me->n_dofs * (uint64_t)m;
     k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
         Yc, m, me->n_dofs, me->slot_ptr.p, me->slot.p, c ? c->is_row.p : nullptr, has_par ? c->par_ptr.p : nullptr,
-        has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y_dev);
+        has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y_dev, FastDiv(m));
     check_launch(ctx, "assemble_f64_noalloc");
   });
 }

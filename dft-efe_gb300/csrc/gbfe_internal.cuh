@@ -263,6 +263,7 @@ struct gbfe_op {
   uint64_t blk_begin = 0, blk_n = 0;  // OP_DIAG_BLOCK: dense block rows
   gbfe::DBuf<double> blk;             // column-major blk_n x blk_n
   gbfe::DBuf<float> blk_f32;
+  mutable gbfe::DBuf<float> blk_out_f32;  // block rows of B^-1 X for the fused filter
   mutable gbfe::DBuf<double> cellbuf;  // per-apply cell-wise result scratch (f64)
   mutable gbfe::DBuf<float> cellbuf_f32;
 };
@@ -278,6 +279,31 @@ struct gbfe_mv {
 };
 
 namespace gbfe {
+
+// Division of an element index by the block width m without the
+// multi-instruction integer division: q = (umulhi(n, mul) + n) >> shift
+// (round-up multiplier), exact for n < 2^31; larger n fall back to '/'.
+struct FastDiv {
+  uint32_t d = 1, mul = 1, shift = 0;
+  FastDiv() = default;
+  explicit FastDiv(uint32_t div) : d(div ? div : 1) {
+    shift = 0;
+    while ((1ull << shift) < d) ++shift;
+    mul = (uint32_t)(((1ull << 32) * ((1ull << shift) - d)) / d + 1);
+  }
+  // t -> (row, column)
+  __device__ __forceinline__ void divmod(uint64_t t, uint64_t &q, uint32_t &r) const {
+    if (t < (1ull << 31)) {
+      const uint32_t n = (uint32_t)t;
+      const uint32_t qq = (uint32_t)(((uint64_t)__umulhi(n, mul) + n) >> shift);
+      q = qq;
+      r = n - qq * d;
+    } else {
+      q = t / d;
+      r = (uint32_t)(t - q * d);
+    }
+  }
+};
 
 inline unsigned grid_for(uint64_t n, unsigned block) {
   uint64_t g = (n + block - 1) / block;
@@ -348,7 +374,8 @@ void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
 void build_mixed_mats(gbfe_op *op);
 void build_tc_mats(gbfe_op *op);
 bool tc_supported(const gbfe_mesh *me);
-void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *xscale = nullptr);
+void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *xscale = nullptr,
+                   const float *xsub = nullptr, uint32_t sub_begin = 0, uint32_t sub_n = 0);
 // one step of the mixed Chebyshev recurrence in two launches:
 //   R = alpha1 (A B^-1 RN - c RN) + alpha2 R + alpha1 eF2[j] Y
 // (B^-1 applied in the tensor-core gather, the step fused into the assembly);

@@ -35,10 +35,12 @@ __global__ void k_axpby(uint64_t n, double a, const T *__restrict__ x, double b,
 template <class T>
 __global__ void k_axpby_blocked(uint64_t rows, uint32_t m, double a1, const double *__restrict__ alpha,
                                 const T *__restrict__ x, double b1, const double *__restrict__ beta,
-                                const T *__restrict__ y, T *__restrict__ z) {
+                                const T *__restrict__ y, T *__restrict__ z, const FastDiv fm) {
   const uint64_t n = rows * m;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t j = (uint32_t)(t % m);
+    uint64_t i;
+    uint32_t j;
+    fm.divmod(t, i, j);
     z[t] = (T)(a1 * alpha[j]) * x[t] + (T)(b1 * beta[j]) * y[t];
   }
 }
@@ -48,9 +50,11 @@ __global__ void k_axpby_blocked(uint64_t rows, uint32_t m, double a1, const doub
 template <class T>
 __global__ void k_cheb_step(uint64_t n, uint32_t m, double alpha1, double c, double alpha2,
                             const T *__restrict__ AS, const T *__restrict__ RN, T *__restrict__ R,
-                            const double *__restrict__ eF2, const T *__restrict__ Y) {
+                            const double *__restrict__ eF2, const T *__restrict__ Y, const FastDiv fm) {
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t j = (uint32_t)(t % m);
+    uint64_t i;
+    uint32_t j;
+    fm.divmod(t, i, j);
     T s1 = (T)alpha1 * AS[t] + (T)(-c * alpha1) * RN[t];
     T r = s1 + (T)alpha2 * R[t];
     R[t] = r + (T)(alpha1 * eF2[j]) * Y[t];
@@ -62,10 +66,12 @@ __global__ void k_cheb_step(uint64_t n, uint32_t m, double alpha1, double c, dou
 template <class T>
 __global__ void k_cheb_step_dev(uint64_t n, uint32_t m, const double *__restrict__ coef, const T *__restrict__ AS,
                                 const T *__restrict__ RN, T *__restrict__ R, const double *__restrict__ eF2,
-                                const T *__restrict__ Y) {
+                                const T *__restrict__ Y, const FastDiv fm) {
   const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t j = (uint32_t)(t % m);
+    uint64_t i;
+    uint32_t j;
+    fm.divmod(t, i, j);
     T s1 = (T)alpha1 * AS[t] + (T)(-c * alpha1) * RN[t];
     T r = s1 + (T)alpha2 * R[t];
     R[t] = r + (T)(alpha1 * eF2[j]) * Y[t];
@@ -74,9 +80,11 @@ __global__ void k_cheb_step_dev(uint64_t n, uint32_t m, const double *__restrict
 
 // Y = R + eF2[j] * X, with R in FP32 and X, Y in FP64 (mixed filter epilogue)
 __global__ void k_cheb_final_mixed(uint64_t n, uint32_t m, const float *__restrict__ R, const double *__restrict__ eF2,
-                                   const double *__restrict__ X, double *__restrict__ Y) {
+                                   const double *__restrict__ X, double *__restrict__ Y, const FastDiv fm) {
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t j = (uint32_t)(t % m);
+    uint64_t i;
+    uint32_t j;
+    fm.divmod(t, i, j);
     Y[t] = (double)R[t] + eF2[j] * X[t];
   }
 }
@@ -167,10 +175,10 @@ void d_axpby_blocked(gbfe_ctx *ctx, double a1, const double *alpha_d, const gbfe
   const uint64_t n = z->count();
   if (z->dtype == GBFE_F64)
     k_axpby_blocked<double><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(z->mesh->n_dofs, z->m, a1, alpha_d, x->d.p, b1,
-                                                                     beta_d, y->d.p, z->d.p);
+                                                                     beta_d, y->d.p, z->d.p, FastDiv(z->m));
   else
     k_axpby_blocked<float><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(z->mesh->n_dofs, z->m, a1, alpha_d, x->f.p, b1,
-                                                                    beta_d, y->f.p, z->f.p);
+                                                                    beta_d, y->f.p, z->f.p, FastDiv(z->m));
   check_launch(ctx, "axpby_blocked");
 }
 
@@ -383,14 +391,14 @@ template <>
 void launch_cheb_step<double>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha1, double c, double alpha2,
                               const gbfe_mv *AS, const gbfe_mv *RN, gbfe_mv *R, const double *eF2, const gbfe_mv *Y) {
   k_cheb_step<double><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, alpha1, c, alpha2, AS->d.p, RN->d.p, R->d.p, eF2,
-                                                              Y->d.p);
+                                                              Y->d.p, FastDiv(m));
   check_launch(ctx, "cheb_step");
 }
 template <>
 void launch_cheb_step<float>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha1, double c, double alpha2,
                              const gbfe_mv *AS, const gbfe_mv *RN, gbfe_mv *R, const double *eF2, const gbfe_mv *Y) {
   k_cheb_step<float><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, alpha1, c, alpha2, AS->f.p, RN->f.p, R->f.p, eF2,
-                                                             Y->f.p);
+                                                             Y->f.p, FastDiv(m));
   check_launch(ctx, "cheb_step_f32");
 }
 
@@ -515,10 +523,10 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
       apply_op(A, s1, s2);
       if (mixed)
         k_cheb_step_dev<float><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, w.coef.p + 3 * k, s2->f.p, rn->f.p,
-                                                                        r->f.p, w.tab.p + (size_t)k * m, Yr->f.p);
+                                                                        r->f.p, w.tab.p + (size_t)k * m, Yr->f.p, FastDiv(m));
       else
         k_cheb_step_dev<double><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, w.coef.p + 3 * k, s2->d.p, rn->d.p,
-                                                                         r->d.p, w.tab.p + (size_t)k * m, Yr->d.p);
+                                                                         r->d.p, w.tab.p + (size_t)k * m, Yr->d.p, FastDiv(m));
       check_launch(ctx, "cheb_step");
     }
   };
@@ -573,7 +581,8 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
   if (mixed) {
     {
       ProfScope prof_k(ctx, "k:cheb_final_mixed", 0.0, 0.0);
-      k_cheb_final_mixed<<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, Rfin->f.p, eF2_final, X->d.p, Y->d.p);
+      k_cheb_final_mixed<<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, Rfin->f.p, eF2_final, X->d.p, Y->d.p,
+                                                                 FastDiv(m));
       check_launch(ctx, "cheb_final_mixed");
     }
   } else {

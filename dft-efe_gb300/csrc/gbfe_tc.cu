@@ -258,8 +258,12 @@ struct Tc2Args {
   uint32_t N, mtiles, tmem_cols, nbuf, stages;
   int *status;
   // optional gather scale X[i] -> xscale[i] * X[i]: the diagonal operator B^-1
-  // applied on the fly (xscale = 0 on homogeneous Dirichlet rows)
+  // applied on the fly (xscale = 0 on homogeneous Dirichlet rows); rows
+  // [sub_begin, sub_begin + sub_n) are taken from xsub instead (the dense
+  // enrichment block of the inverse overlap, applied beforehand)
   const float *xscale;
+  const float *xsub;
+  uint32_t sub_begin, sub_n;
 };
 
 __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a) {
@@ -452,7 +456,12 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
 #pragma unroll
               for (int kk = 0; kk < 8; ++kk) {
                 const uint32_t k = kc * KC + kb * 8 + kk;
-                xv[u][kk] *= (has[u] && k < nd) ? __ldg(a.xscale + a.ids[off + k]) : 0.f;
+                const uint32_t id = (has[u] && k < nd) ? a.ids[off + k] : 0u;
+                const uint32_t e = id - a.sub_begin;
+                if (has[u] && k < nd && e < a.sub_n)
+                  xv[u][kk] = (vv[u] < N && (v0 + vv[u]) < m) ? __ldg(a.xsub + (uint64_t)e * m + v0 + vv[u]) : 0.f;
+                else
+                  xv[u][kk] *= (has[u] && k < nd) ? __ldg(a.xscale + id) : 0.f;
               }
             }
           }
@@ -515,7 +524,8 @@ bool tc_supported(const gbfe_mesh *me) { return me->nd_max <= 256; }
 // N_req / stages_req = 0: the tuned shape if one exists, else the heuristic.
 static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg, uint32_t ncell,
                        uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0, uint32_t stages_req = 0,
-                       const float *xscale = nullptr) {
+                       const float *xscale = nullptr, const float *xsub = nullptr, uint32_t sub_begin = 0,
+                       uint32_t sub_n = 0) {
   gbfe_mesh *me = op->mesh;
   const uint32_t m = X->m;
   if (!N_req) {
@@ -548,7 +558,7 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
     attr_set = true;
   }
   Tc2Args args{X->f.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, vt, op->tc_aoff.p,
-               op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xscale};
+               op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xscale, xsub, sub_begin, sub_n};
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
   k_cell_apply_tc2<<<grid, THREADS2, smem, ctx->stream>>>(args);
@@ -557,7 +567,8 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
 
 // Yc (FP32 cell-wise buffer) = split-BF16 tensor-core products, size-binned by
 // the number of 128-row M tiles a cell needs.
-void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *xscale) {
+void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *xscale, const float *xsub,
+                   uint32_t sub_begin, uint32_t sub_n) {
   gbfe_mesh *me = op->mesh;
   gbfe_ctx *ctx = me->ctx;
   const uint32_t m = X->m;
@@ -577,7 +588,8 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *
     const uint32_t cbeg = me->bin_begin[b0], cend = me->bin_begin[b1];
     const uint32_t ncell = cend - cbeg;
     if (ctx->tc_version == 2) {
-      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1], 0, 0, xscale);
+      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1], 0, 0, xscale,
+                 xsub, sub_begin, sub_n);
       continue;
     }
     uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
