@@ -449,21 +449,29 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
             }
           }
           if (a.xscale) {  // separate pass: keeps the 16 row loads above independent
+            // all loads first (predicated, no branches), then the selects
+            float sc[2][8], sb[2][8];
+            bool sub[2][8];
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
               const uint32_t itm = item + u * GATHER_WARPS;
               const uint32_t kb = itm % (KC / 8);
+              const bool vin = has[u] && vv[u] < N && (v0 + vv[u]) < m;
 #pragma unroll
               for (int kk = 0; kk < 8; ++kk) {
                 const uint32_t k = kc * KC + kb * 8 + kk;
-                const uint32_t id = (has[u] && k < nd) ? a.ids[off + k] : 0u;
+                const bool kin = has[u] && k < nd;
+                const uint32_t id = kin ? a.ids[off + k] : 0u;
                 const uint32_t e = id - a.sub_begin;
-                if (has[u] && k < nd && e < a.sub_n)
-                  xv[u][kk] = (vv[u] < N && (v0 + vv[u]) < m) ? __ldg(a.xsub + (uint64_t)e * m + v0 + vv[u]) : 0.f;
-                else
-                  xv[u][kk] *= (has[u] && k < nd) ? __ldg(a.xscale + id) : 0.f;
+                sub[u][kk] = kin && e < a.sub_n;
+                sc[u][kk] = kin ? __ldg(a.xscale + id) : 0.f;
+                sb[u][kk] = (sub[u][kk] && vin) ? __ldg(a.xsub + (uint64_t)e * m + v0 + vv[u]) : 0.f;
               }
             }
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+              for (int kk = 0; kk < 8; ++kk) xv[u][kk] = sub[u][kk] ? sb[u][kk] : xv[u][kk] * sc[u][kk];
           }
 #pragma unroll
           for (int u = 0; u < 2; ++u) {
