@@ -102,6 +102,7 @@ int gbfe_op_assemble_local(gbfe_op *op, uint32_t nq, const double *basis_values,
       check_launch(ctx, "f64_to_f32");
     }
     if (op->tc_aoff.p) build_tc_mats(op);
+    op->folded_for = 0;  // folded tiles follow the new matrices on their next use
     if (op->oz_aoff.p) build_oz_mats(op);
     GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
   });

@@ -140,12 +140,13 @@ __global__ void k_assemble(const TC *__restrict__ Yc, uint32_t m, uint64_t n_dof
   }
 }
 
-// gather scale of the fused filter: (float)d[i] (the factor k_diag_apply<float>
-// applies), 0 on homogeneous Dirichlet rows
-__global__ void k_diag_gather(const double *__restrict__ d, const uint8_t *__restrict__ is_row, uint64_t n,
-                              float *__restrict__ out) {
+// per-dof factor of B^-1 for folding into A (fused filter): d[i], 0 on
+// homogeneous Dirichlet rows, 1 on the rows of the dense block (those rows
+// are computed separately and substituted in the gather)
+__global__ void k_fold_scale(const double *__restrict__ d, const uint8_t *__restrict__ is_row, uint64_t n,
+                             uint64_t blk_begin, uint64_t blk_n, double *__restrict__ out) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-    out[i] = (is_row && is_row[i]) ? 0.f : (float)d[i];
+    out[i] = (is_row && is_row[i]) ? 0.0 : ((i - blk_begin) < blk_n ? 1.0 : d[i]);
 }
 
 // Assembly of a FP32 cell-wise result with one Chebyshev recurrence step fused
@@ -524,7 +525,7 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
       BInv->mesh != me || A->cons != c || (c && !c->pure_dirichlet) || RN->m == 0)
     return false;
   const uint32_t m = RN->m;
-  if (!BInv->diag_gather.p) return false;  // built at upload for diagonal operators
+  if (!BInv->fold_scale.p) return false;  // built at upload for diagonal operators
   constraints_p2c(ctx, c, RN);  // BInv's parent-to-child on its input, as apply_op does
   const float *xsub = nullptr;
   if (BInv->kind == OP_DIAG_BLOCK) {
@@ -538,8 +539,13 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
     count_launch(ctx);
     xsub = BInv->blk_out_f32.p;
   }
+  if (A->folded_for != BInv->serial) {
+    // A diag(B^-1 factor) in split tiles, built on the first fused step
+    build_tc_mats_folded(A, BInv->fold_scale.p, A->mats_hi_folded);
+    A->folded_for = BInv->serial;
+  }
   A->cellbuf_f32.ensure((size_t)me->total_cell_dofs * m);
-  cell_apply_tc(A, RN, A->cellbuf_f32.p, BInv->diag_gather.p, xsub, (uint32_t)BInv->blk_begin,
+  cell_apply_tc(A, RN, A->cellbuf_f32.p, A->mats_hi_folded.p, xsub, (uint32_t)BInv->blk_begin,
                 xsub ? (uint32_t)BInv->blk_n : 0u);
   const uint64_t n = (uint64_t)me->n_dofs * m;
   {
@@ -1093,10 +1099,12 @@ static int diag_upload_impl(gbfe_mesh *mesh, const gbfe_cons *cons, const double
       op->diag.upload(diag, mesh->n_dofs, mesh->ctx->stream);
       if ((kind == OP_DIAG || kind == OP_DIAG_BLOCK) && (!cons || cons->pure_dirichlet)) {
         // gather factor of the fused mixed filter step
-        op->diag_gather.alloc(mesh->n_dofs);
-        k_diag_gather<<<grid_for(mesh->n_dofs, 256), 256, 0, mesh->ctx->stream>>>(
-            op->diag.p, cons ? cons->is_row.p : nullptr, mesh->n_dofs, op->diag_gather.p);
-        check_launch(mesh->ctx, "diag_gather");
+        // the B^-1 factor folded into a Hamiltonian's tiles by the fused filter
+        // (block rows, if any, are set by gbfe_diag_block_upload)
+        op->fold_scale.alloc(mesh->n_dofs);
+        k_fold_scale<<<grid_for(mesh->n_dofs, 256), 256, 0, mesh->ctx->stream>>>(
+            op->diag.p, cons ? cons->is_row.p : nullptr, mesh->n_dofs, 0, 0, op->fold_scale.p);
+        check_launch(mesh->ctx, "fold_scale");
       }
       GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
     }
@@ -1124,6 +1132,11 @@ int gbfe_diag_block_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double 
     op->blk_begin = blk_begin;
     op->blk_n = blk_n;
     op->blk.upload(blk, blk_n * blk_n, mesh->ctx->stream);
+    if (op->fold_scale.p) {
+      k_fold_scale<<<grid_for(mesh->n_dofs, 256), 256, 0, mesh->ctx->stream>>>(
+          op->diag.p, cons ? cons->is_row.p : nullptr, mesh->n_dofs, blk_begin, blk_n, op->fold_scale.p);
+      check_launch(mesh->ctx, "fold_scale");
+    }
     std::vector<float> f(blk, blk + blk_n * blk_n);
     op->blk_f32.upload(f.data(), f.size(), mesh->ctx->stream);
     GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));

@@ -242,6 +242,11 @@ struct gbfe_nl {
   mutable gbfe::DBuf<float> ycell_f32;
 };
 
+inline uint64_t gbfe_next_serial() {
+  static std::atomic<uint64_t> n{0};
+  return ++n;
+}
+
 struct gbfe_op {
   gbfe_mesh *mesh = nullptr;
   const gbfe_cons *cons = nullptr;
@@ -259,7 +264,10 @@ struct gbfe_op {
   mutable gbfe::DBuf<int> oz_xexp;    // per-vector exponent of the current X
   gbfe::DBuf<float> mats_f32;         // FP32 copy for the SIMT mixed apply
   gbfe::DBuf<double> diag;
-  gbfe::DBuf<float> diag_gather;  // (float)diag, 0 on homogeneous Dirichlet rows (fused filter)
+  gbfe::DBuf<double> fold_scale;  // per-dof factor of this B^-1 folded into A (0 on Dirichlet rows)
+  uint64_t serial = gbfe_next_serial();  // identity (folded tiles name their B^-1 by it)
+  mutable gbfe::DBuf<__nv_bfloat16> mats_hi_folded;  // split tiles of A diag(fold_scale of folded_for)
+  mutable uint64_t folded_for = 0;
   uint64_t blk_begin = 0, blk_n = 0;  // OP_DIAG_BLOCK: dense block rows
   gbfe::DBuf<double> blk;             // column-major blk_n x blk_n
   gbfe::DBuf<float> blk_f32;
@@ -374,8 +382,9 @@ void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
 void build_mixed_mats(gbfe_op *op);
 void build_tc_mats(gbfe_op *op);
 bool tc_supported(const gbfe_mesh *me);
-void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *xscale = nullptr,
+void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const __nv_bfloat16 *tiles = nullptr,
                    const float *xsub = nullptr, uint32_t sub_begin = 0, uint32_t sub_n = 0);
+void build_tc_mats_folded(const gbfe_op *op, const double *kscale, gbfe::DBuf<__nv_bfloat16> &out);
 // one step of the mixed Chebyshev recurrence in two launches:
 //   R = alpha1 (A B^-1 RN - c RN) + alpha2 R + alpha1 eF2[j] Y
 // (B^-1 applied in the tensor-core gather, the step fused into the assembly);

@@ -42,9 +42,12 @@ using namespace gbfe::tc;
 // Pre-split A_op = A_c^T into the per-(cell, K chunk) tile layout:
 // [hi: MT8 rows x KC][lo: MT8 rows x KC], element (r, kk) at
 // (r/8)*(KC/8)*64 + (kk/8)*64 + (r%8)*8 + kk%8.
+// kscale (optional): A_c(k, j) *= kscale[ids_c[k]] in FP64 before the split,
+// i.e. A diag(kscale): a diagonal operator applied to X folded into A
 __global__ void k_build_tc_mats(const double *__restrict__ mats, const uint64_t *__restrict__ mat_off,
                                 const uint32_t *__restrict__ cell_off, const uint64_t *__restrict__ a_off,
-                                uint32_t n_cells, __nv_bfloat16 *__restrict__ out) {
+                                uint32_t n_cells, __nv_bfloat16 *__restrict__ out,
+                                const uint32_t *__restrict__ ids = nullptr, const double *__restrict__ kscale = nullptr) {
   const uint32_t c = blockIdx.x;
   if (c >= n_cells) return;
   const uint32_t nd = cell_off[c + 1] - cell_off[c];
@@ -57,7 +60,8 @@ __global__ void k_build_tc_mats(const double *__restrict__ mats, const uint64_t 
     const uint32_t kc = idx / per_chunk, rem = idx - kc * per_chunk;
     const uint32_t r = rem / KC, kk = rem - r * KC;
     const uint32_t k = kc * KC + kk;
-    const double val = (r < nd && k < nd) ? A[k + (uint64_t)nd * r] : 0.0;
+    double val = (r < nd && k < nd) ? A[k + (uint64_t)nd * r] : 0.0;
+    if (kscale && r < nd && k < nd) val *= kscale[ids[cell_off[c] + k]];
     const __nv_bfloat16 hi = __double2bfloat16(val);
     const __nv_bfloat16 lo = __double2bfloat16(val - (double)__bfloat162float(hi));
     const uint32_t pos = (r / 8) * (KC / 8) * 64 + (kk / 8) * 64 + (r % 8) * 8 + (kk % 8);
@@ -257,11 +261,9 @@ struct Tc2Args {
   float *Yc;
   uint32_t N, mtiles, tmem_cols, nbuf, stages;
   int *status;
-  // optional gather scale X[i] -> xscale[i] * X[i]: the diagonal operator B^-1
-  // applied on the fly (xscale = 0 on homogeneous Dirichlet rows); rows
-  // [sub_begin, sub_begin + sub_n) are taken from xsub instead (the dense
-  // enrichment block of the inverse overlap, applied beforehand)
-  const float *xscale;
+  // optional: X rows [sub_begin, sub_begin + sub_n) are taken from xsub (rows
+  // of B^-1 X computed beforehand: the dense enrichment block of the inverse
+  // overlap; the diagonal part of B^-1 is folded into the tiles)
   const float *xsub;
   uint32_t sub_begin, sub_n;
 };
@@ -448,10 +450,7 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
               xv[u][kk] = (vin && k < nd) ? __ldg(a.X + (uint64_t)a.ids[off + k] * m + v0 + vv[u]) : 0.f;
             }
           }
-          if (a.xscale) {  // separate pass: keeps the 16 row loads above independent
-            // all loads first (predicated, no branches), then the selects
-            float sc[2][8], sb[2][8];
-            bool sub[2][8];
+          if (a.xsub) {  // separate pass: keeps the 16 row loads above independent
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
               const uint32_t itm = item + u * GATHER_WARPS;
@@ -460,18 +459,10 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
 #pragma unroll
               for (int kk = 0; kk < 8; ++kk) {
                 const uint32_t k = kc * KC + kb * 8 + kk;
-                const bool kin = has[u] && k < nd;
-                const uint32_t id = kin ? a.ids[off + k] : 0u;
-                const uint32_t e = id - a.sub_begin;
-                sub[u][kk] = kin && e < a.sub_n;
-                sc[u][kk] = kin ? __ldg(a.xscale + id) : 0.f;
-                sb[u][kk] = (sub[u][kk] && vin) ? __ldg(a.xsub + (uint64_t)e * m + v0 + vv[u]) : 0.f;
+                const uint32_t e = ((has[u] && k < nd) ? a.ids[off + k] : a.sub_begin + a.sub_n) - a.sub_begin;
+                if (e < a.sub_n) xv[u][kk] = vin ? __ldg(a.xsub + (uint64_t)e * m + v0 + vv[u]) : 0.f;
               }
             }
-#pragma unroll
-            for (int u = 0; u < 2; ++u)
-#pragma unroll
-              for (int kk = 0; kk < 8; ++kk) xv[u][kk] = sub[u][kk] ? sb[u][kk] : xv[u][kk] * sc[u][kk];
           }
 #pragma unroll
           for (int u = 0; u < 2; ++u) {
@@ -526,13 +517,23 @@ void build_tc_mats(gbfe_op *op) {
   check_launch(ctx, "build_tc_mats");
 }
 
+// split-BF16 tiles of A diag(kscale) (same layout and offsets as the plain tiles)
+void build_tc_mats_folded(const gbfe_op *op, const double *kscale, DBuf<__nv_bfloat16> &out) {
+  gbfe_mesh *me = op->mesh;
+  gbfe_ctx *ctx = me->ctx;
+  out.alloc(op->mats_hi.n);
+  k_build_tc_mats<<<me->n_cells, 256, 0, ctx->stream>>>(op->mats.p, op_mat_off(op), me->cell_off.p, op->tc_aoff.p,
+                                                        me->n_cells, out.p, me->ids.p, kscale);
+  check_launch(ctx, "build_tc_mats_folded");
+}
+
 bool tc_supported(const gbfe_mesh *me) { return me->nd_max <= 256; }
 
 // v2 launch: persistent grid over (cell, vector tile) items of one M-tile group.
 // N_req / stages_req = 0: the tuned shape if one exists, else the heuristic.
 static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg, uint32_t ncell,
                        uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0, uint32_t stages_req = 0,
-                       const float *xscale = nullptr, const float *xsub = nullptr, uint32_t sub_begin = 0,
+                       const __nv_bfloat16 *tiles = nullptr, const float *xsub = nullptr, uint32_t sub_begin = 0,
                        uint32_t sub_n = 0) {
   gbfe_mesh *me = op->mesh;
   const uint32_t m = X->m;
@@ -566,7 +567,8 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
     attr_set = true;
   }
   Tc2Args args{X->f.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, vt, op->tc_aoff.p,
-               op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xscale, xsub, sub_begin, sub_n};
+               tiles ? tiles : op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xsub, sub_begin,
+               sub_n};
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
   k_cell_apply_tc2<<<grid, THREADS2, smem, ctx->stream>>>(args);
@@ -575,12 +577,12 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
 
 // Yc (FP32 cell-wise buffer) = split-BF16 tensor-core products, size-binned by
 // the number of 128-row M tiles a cell needs.
-void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *xscale, const float *xsub,
+void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const __nv_bfloat16 *tiles, const float *xsub,
                    uint32_t sub_begin, uint32_t sub_n) {
   gbfe_mesh *me = op->mesh;
   gbfe_ctx *ctx = me->ctx;
   const uint32_t m = X->m;
-  GBFE_REQUIRE(!xscale || ctx->tc_version == 2, "scaled gather needs the persistent tensor-core kernel");
+  GBFE_REQUIRE((!tiles && !xsub) || ctx->tc_version == 2, "folded tiles need the persistent tensor-core kernel");
   // group bins (distinct nd) into launches by M-tile count
   for (uint32_t mtiles = 1; mtiles <= 2; ++mtiles) {
     uint32_t b0 = UINT32_MAX, b1 = 0;
@@ -596,7 +598,7 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const float *
     const uint32_t cbeg = me->bin_begin[b0], cend = me->bin_begin[b1];
     const uint32_t ncell = cend - cbeg;
     if (ctx->tc_version == 2) {
-      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1], 0, 0, xscale,
+      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1], 0, 0, tiles,
                  xsub, sub_begin, sub_n);
       continue;
     }

@@ -115,10 +115,13 @@ int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len
  * on every later pass; 0: launched one by one. */
 int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on);
 /* 1 (default): each step of the mixed-precision Chebyshev recurrence runs as
- * two launches -- the tensor-core cell product gathers B^-1 R directly (GLL
- * diagonal inverse, homogeneous Dirichlet rows) and the assembly computes the
- * recurrence update -- where the operators allow it; 0: B^-1 apply, A apply
- * and the update as separate launches. */
+ * two launches -- the split-BF16 cell product with the diagonal of B^-1 folded
+ * into A's tiles (A diag(B^-1), built on first use; rows of a dense
+ * enrichment block of B^-1 are computed beforehand and substituted in the
+ * gather) and the assembly that also computes the recurrence update -- where
+ * the operators allow it (homogeneous Dirichlet rows); 0: B^-1 apply, A apply
+ * and the update as separate launches.  The two agree to the split-BF16
+ * rounding. */
 int gbfe_ctx_set_fused_filter(gbfe_ctx *ctx, int on);
 /* The m x m symmetric eigenproblems of Rayleigh-Ritz (syevd('V','L') in
  * RayleighRitzEigenSolver.t.cpp:233-301): 1 (default) on the host for

@@ -91,9 +91,10 @@ def test_gpu_enriched_ks_solve(gpu_ctx, enriched, mixed):
 
 @pytest.mark.gpu
 def test_gpu_enriched_fused_filter_matches_separate(gpu_ctx, enriched):
-    """The fused mixed filter step with the OrthoEFE inverse (diagonal on the
-    classical rows in the tensor-core gather, the enrichment block applied
-    beforehand) computes what the separate launches compute."""
+    """The fused mixed filter step with the OrthoEFE inverse (diagonal folded
+    into the split-BF16 tiles, the enrichment block applied beforehand and
+    substituted in the gather) against the separate launches: within 1e-3
+    relative (split-BF16 rounding of A diag(B^-1) versus A)."""
     from gbfe import api
 
     p = enriched
@@ -120,4 +121,4 @@ def test_gpu_enriched_fused_filter_matches_separate(gpu_ctx, enriched):
             gpu_ctx.set_fused_filter(True)
     err = rel_maxnorm(outs[True], outs[False])
     print(f"enriched fused filter vs separate: {err:.2e}, bitwise {np.array_equal(outs[True], outs[False])}")
-    assert err <= 1e-6
+    assert err <= 1e-3

@@ -464,10 +464,11 @@ def test_small_eigenproblem_host_and_cusolver_agree(gpu_ctx, small_problem):
 
 
 def test_fused_mixed_filter_step_matches_separate_launches(gpu_ctx, small_problem):
-    """The two-launch mixed filter step (B^-1 in the tensor-core gather, the
-    recurrence in the assembly) computes the same FP32 operations as the
-    separate launches: filtered blocks within 1e-6 relative, KS eigenvalues
-    within 1e-9 Ha."""
+    """The two-launch mixed filter step (B^-1 folded into the split-BF16
+    tiles, the recurrence in the assembly) against the separate launches:
+    the same filter up to the split-BF16 rounding of A diag(B^-1) versus A
+    (filtered blocks within 1e-3 relative), KS eigenvalues within 1e-6 Ha of
+    each other (both within 1e-6 Ha of FP64)."""
     from gbfe import api
 
     p = small_problem
@@ -494,5 +495,5 @@ def test_fused_mixed_filter_step_matches_separate_launches(gpu_ctx, small_proble
             gpu_ctx.set_fused_filter(True)
     err = rel_maxnorm(outs[True], outs[False])
     print(f"fused filter vs separate: rel max-norm {err:.2e}, bitwise {np.array_equal(outs[True], outs[False])}")
-    assert err <= 1e-6
-    assert np.abs(eigs[True][:10] - eigs[False][:10]).max() <= 1e-9
+    assert err <= 1e-3
+    assert np.abs(eigs[True][:10] - eigs[False][:10]).max() <= 1e-6
