@@ -230,6 +230,11 @@ class CpuBaseline:
         self.tmp.cleanup()
 
 
+# scopes timed with CUDA events inside the timed region (the rest of the
+# breakdown comes from one untimed solve after it)
+ROOFLINE_CANDIDATES = ("cell_apply_mixed", "cell_apply_f64", "cell_apply_f64_oz", "gram_f64_oz", "rotate_f64_oz",
+                       "gram_f64_dgemm", "rotate_f64_dgemm", "eig_small_f64")
+
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # dominant kernel, from one ncu capture of the same workload's apply
 # (profiles/k_cell_apply_tc2_cfg2.md: the two launches of one apply moved
@@ -334,7 +339,9 @@ def run_gpu(args, cfg_name, rank, world):
     for _ in range(args.warmup):
         solve(True)
     ctx.synchronize()
+    # inside the timed region only the roofline candidates carry CUDA events
     ctx.set_profiling(True)
+    ctx.set_profile_filter(ROOFLINE_CANDIDATES)
     ctx.reset_kernel_stats()
     launches0 = ctx.kernel_launches()
     lat, errs, passes, ok, eigs, rcs = [], [], [], 0, [], []
@@ -366,10 +373,18 @@ def run_gpu(args, cfg_name, rank, world):
     st_dense = {k: ctx.kernel_stats(k) for k in ("gram_f64_oz", "rotate_f64_oz", "gram_f64_dgemm",
                                                   "rotate_f64_dgemm")}
     st_eig = ctx.kernel_stats("eig_small_f64")
-    st_pass = {k: ctx.kernel_stats(k) for k in ("pass_total", "pass_filter", "pass_fp64_applies")}
-    st_small = {k: ctx.kernel_stats(k) for k in ("k:p2c", "k:diag_apply", "k:assemble_f64", "k:assemble_f32",
-                                                  "k:assemble_cheb", "k:cheb_final_mixed", "k:axpby",
-                                                  "k:axpby_blocked", "k:coldot_partial", "k:convert", "k:fill")}
+    # breakdown of one more solve, outside the timed region, with every scope
+    # timed (kernels, the fused pass's spans, the small sweeps)
+    ctx.set_profile_filter(())
+    ctx.reset_kernel_stats()
+    solve(True)
+    ctx.synchronize()
+    breakdown = {k: ctx.kernel_stats(k) for k in (
+        "cell_apply_mixed", "cell_apply_f64_oz", "gram_f64_oz", "rotate_f64_oz", "eig_small_f64",
+        "pass_total", "pass_filter", "pass_fp64_applies", "k:p2c", "k:diag_apply", "k:assemble_f64",
+        "k:assemble_f32", "k:assemble_cheb", "k:cheb_final_mixed", "k:axpby", "k:axpby_blocked",
+        "k:coldot_partial", "k:convert", "k:fill")}
+    breakdown = {k: {"launches": v["launches"], "ms": v["ms"]} for k, v in breakdown.items() if v["launches"]}
     ctx.set_profiling(False)
 
     # e2e: the same solve through the C ABI with host buffers each step
@@ -389,7 +404,7 @@ def run_gpu(args, cfg_name, rank, world):
     fp64_peak = ctx.probe_fp64_peak()
     return dict(cfg=cfg, prob=prob, deg=deg, bounds=(wl, wu, uu), tuned=tuned, fp64_times=fp64_times, passes64=passes64,
                 rc64=rc64, lat=lat, errs=errs, passes=passes, ok=ok, t_total=t_total, launches=launches,
-                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, st_dense=st_dense, st_eig=st_eig, st_pass=st_pass, st_small=st_small, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
+                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, st_dense=st_dense, st_eig=st_eig, breakdown=breakdown, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
                 h2d=prob.n_dofs * m * 8, d2h=prob.n_dofs * m * 8 + 2 * m * 8)
 
 
@@ -708,9 +723,6 @@ def main():
     roof["traffic"] = NCU_TRAFFIC_PER_LAUNCH.get((args.config, dom))
     others = {k: v for k, v in cand.items() if k != dom and v["launches"]}
     others["eig_small_f64 (potrf, trsm, syevd block; includes its host sync)"] = r["st_eig"]
-    # device-timeline spans of the fused pass (CUDA events; idle gaps included)
-    others.update({f"{k} (span)": v for k, v in r["st_pass"].items()})
-    others.update({k: v for k, v in r["st_small"].items() if v["launches"]})
     e2e_sps = world / float(np.mean(r["e2e_lat"]))
     line = {
         "metric": "ChFSI solves/s at |d_eps|<=1e-6 Ha (mixed precision), FP64 beside it",
@@ -732,6 +744,7 @@ def main():
         "e2e": {"value": e2e_sps, "unit": "solves/s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
         "gpu_launches": r["launches"],
         "tuned_launch_shapes": r["tuned"],
+        "breakdown_one_solve_untimed": r["breakdown"],
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = CpuBaseline(prob, r["cfg"], r["bounds"], r["deg"], procs)

@@ -737,6 +737,24 @@ int gbfe_ctx_set_graphs(gbfe_ctx *ctx, int on) {
   return GBFE_OK;
 }
 
+int gbfe_ctx_set_profile_filter(gbfe_ctx *ctx, const char *names) {
+  if (!ctx) return GBFE_ERR_ARG;
+  ctx->prof_only.clear();
+  if (names) {
+    std::string all(names), cur;
+    for (char ch : all) {
+      if (ch == ',') {
+        if (!cur.empty()) ctx->prof_only.push_back(cur);
+        cur.clear();
+      } else {
+        cur += ch;
+      }
+    }
+    if (!cur.empty()) ctx->prof_only.push_back(cur);
+  }
+  return GBFE_OK;
+}
+
 int gbfe_ctx_set_fused_filter(gbfe_ctx *ctx, int on) {
   if (!ctx || on < 0 || on > 1) return GBFE_ERR_ARG;
   ctx->fuse_filter = on;

@@ -157,6 +157,7 @@ struct gbfe_ctx {
   int use_graphs = 1;        // capture the Chebyshev recurrence into a CUDA graph
   std::map<std::string, KernelStat> kstats;
   std::vector<cudaEvent_t> event_free;  // recycled timing events of ProfScope
+  std::vector<std::string> prof_only;   // profiling restricted to these scope names (empty: all)
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   cublasHandle_t cublas = nullptr;
@@ -343,8 +344,14 @@ struct ProfScope {
     }
     return e;
   }
+  static bool wanted(const gbfe_ctx *c, const char *name) {
+    if (c->prof_only.empty()) return true;
+    for (const auto &s : c->prof_only)
+      if (s == name) return true;
+    return false;
+  }
   ProfScope(gbfe_ctx *c, const char *name, double flops, double bytes) : ctx(c), nm(name), fl(flops), by(bytes) {
-    if (!ctx->profiling) return;
+    if (!ctx->profiling || !wanted(ctx, name)) return;
     e0 = get(ctx);
     e1 = get(ctx);
     if (ctx->capture_prof) {  // inside a graph: an event-record node, read after each replay
@@ -357,7 +364,7 @@ struct ProfScope {
     cudaEventRecord(e0, ctx->stream);
   }
   ~ProfScope() {
-    if (!ctx->profiling || !e0) return;
+    if (!e0) return;
     if (ctx->capture_prof && !st) {
       cudaEventRecordWithFlags(e1, ctx->stream, cudaEventRecordExternal);
       ctx->capture_prof->push_back(GraphProf{nm, e0, e1, fl, by});

@@ -58,6 +58,7 @@ SIGNATURES = {
     "gbfe_ctx_set_graphs": (i32, [p, i32]),
     "gbfe_autotune": (i32, [p, u32, C.c_char_p, C.c_size_t]),
     "gbfe_ctx_set_small_eig": (i32, [p, i32]),
+    "gbfe_ctx_set_profile_filter": (i32, [p, C.c_char_p]),
     "gbfe_ctx_set_fused_filter": (i32, [p, i32]),
     "gbfe_nonlocal_upload": (i32, [p, u32, p, p, p, p, C.POINTER(p)]),
     "gbfe_mv_gram": (i32, [p, p, p]),

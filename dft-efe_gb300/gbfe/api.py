@@ -79,6 +79,11 @@ class LinAlgOpContext:
         """Mixed filter steps as two fused launches (default) or as separate applies."""
         check(self.lib.gbfe_ctx_set_fused_filter(self.h, 1 if on else 0), self.h, "set_fused_filter")
 
+    def set_profile_filter(self, names: Sequence[str] = ()) -> None:
+        """Profile only these scopes (empty: all)."""
+        check(self.lib.gbfe_ctx_set_profile_filter(self.h, ",".join(names).encode() if names else None), self.h,
+              "set_profile_filter")
+
     def set_small_eig(self, on_host: bool) -> None:
         """Rayleigh-Ritz m x m eigenproblems on the host (m <= 128, default) or in cuSOLVER."""
         check(self.lib.gbfe_ctx_set_small_eig(self.h, 1 if on_host else 0), self.h, "set_small_eig")

@@ -144,6 +144,9 @@ int gbfe_ctx_kernel_launches(const gbfe_ctx *ctx, uint64_t *count);
  * by CUDA events on the launching stream; stats report launches, total device
  * milliseconds and the algorithmic flops / bytes of those launches. */
 int gbfe_ctx_set_profiling(gbfe_ctx *ctx, int on);
+/* Restrict profiling to the comma-separated scope names (NULL or "": every
+ * scope), so a timed run pays for the events of the kernels it reports only. */
+int gbfe_ctx_set_profile_filter(gbfe_ctx *ctx, const char *names);
 int gbfe_ctx_kernel_stats(gbfe_ctx *ctx, const char *name, uint64_t *launches, double *total_ms,
                           double *flops, double *bytes);
 int gbfe_ctx_reset_kernel_stats(gbfe_ctx *ctx);
