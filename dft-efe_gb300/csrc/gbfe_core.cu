@@ -899,8 +899,13 @@ int gbfe_mesh_upload(gbfe_ctx *ctx, uint32_t n_cells, const uint32_t *nd_per_cel
     bcells.reserve(n_cells);
     for (uint32_t b = 0; b < nds.size(); ++b) {
       me->bin_begin.push_back((uint32_t)bcells.size());
+      uint32_t mx = 0;
       for (uint32_t c = 0; c < n_cells; ++c)
-        if (me->h_nd[c] == nds[b]) bcells.push_back(c);
+        if (me->h_nd[c] == nds[b]) {
+          bcells.push_back(c);
+          for (uint32_t a = me->h_cell_off[c]; a < me->h_cell_off[c + 1]; ++a) mx = std::max(mx, cell_dof_ids[a]);
+        }
+      me->bin_max_id.push_back(mx);
     }
     me->bin_begin.push_back((uint32_t)bcells.size());
     cudaStream_t s = ctx->stream;

@@ -205,6 +205,7 @@ struct gbfe_mesh {
   // size bins for variable-nd meshes: cells sorted by nd, grouped
   std::vector<uint32_t> bin_nd;       // nd of each bin
   std::vector<uint32_t> bin_begin;    // offset into bin_cells
+  std::vector<uint32_t> bin_max_id;   // largest dof id in the cells of each bin
   gbfe::DBuf<uint32_t> bin_cells;     // cell ids grouped by bin
 };
 

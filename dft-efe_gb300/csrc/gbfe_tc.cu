@@ -598,8 +598,12 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const __nv_bf
     const uint32_t cbeg = me->bin_begin[b0], cend = me->bin_begin[b1];
     const uint32_t ncell = cend - cbeg;
     if (ctx->tc_version == 2) {
+      // substitution only where the group's cells hold substituted rows
+      uint32_t max_id = 0;
+      for (uint32_t b = b0; b < b1; ++b) max_id = std::max(max_id, me->bin_max_id[b]);
+      const bool sub = xsub && max_id >= sub_begin;
       launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1], 0, 0, tiles,
-                 xsub, sub_begin, sub_n);
+                 sub ? xsub : nullptr, sub_begin, sub ? sub_n : 0u);
       continue;
     }
     uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
