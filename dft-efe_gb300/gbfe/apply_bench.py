@@ -33,6 +33,8 @@ def main() -> None:
     ap.add_argument("--precision", default="mixed", choices=["f64", "f64_tensor", "mixed", "mixed_v1", "simt"])
     ap.add_argument("--m", type=int, default=0, help="vectors (0: the workload's)")
     ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--filter", type=int, default=0,
+                    help="time the mixed residual Chebyshev filter of this degree instead of one apply")
     args = ap.parse_args()
     w = WORKLOADS[args.config]
     m = args.m or w["m"]
@@ -45,6 +47,8 @@ def main() -> None:
                         nq=w["nq"], matrices=("H",))
     ctx = api.LinAlgOpContext(0)
     basis = api.FEBasisManager.from_problem(ctx, prob)
+    if args.filter:
+        return filter_bench(args, prob, ctx, basis, m)
     mixed = args.precision not in ("f64", "f64_tensor")
     H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=mixed, fp64_tensor=args.precision == "f64_tensor")
     if args.precision == "f64_tensor":
@@ -79,6 +83,33 @@ def main() -> None:
         "cell_kernel_tflops": flops / (k_ms * 1e-3) / 1e12, "cell_kernel_gbs": bytes_ / (k_ms * 1e-3) / 1e9,
         "algorithmic_gflop": flops / 1e9, "algorithmic_mb": bytes_ / 1e6,
     }))
+
+
+def filter_bench(args, prob, ctx, basis, m) -> None:
+    """Mixed residual Chebyshev filter (FP32 recurrence, split-BF16 products)
+    of the workload's Hamiltonian, overlap and inverse overlap."""
+    H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=True)
+    Mo = api.CFEOverlapOperatorContext(basis, prob.M, mixed=True)
+    if "enr_block_inv" in prob.extra:
+        Mi = api.OrthoEFEOverlapInverseOpContextGLL(basis, prob.m_gll_diag, prob.extra["enr_begin"],
+                                                    prob.extra["enr_block_inv"])
+    else:
+        Mi = api.CFEOverlapInverseOpContextGLL(basis, prob.m_gll_diag)
+    b = api.lanczos_bounds(H, Mo, Mi, 20, 7)
+    wl, wu, uu = b[0], b[0] + 0.1 * (b[1] - b[0]), b[1] + b[2] / 10
+    eig = np.linspace(wl, wu, m)
+    X = api.MultiVector(basis, m, init=M.random_block(prob.n_dofs, m, 1))
+    Y = api.MultiVector(basis, m)
+    for _ in range(3):
+        api.ResidualChebyshevFilterGEP(H, Mo, Mi, eig, X, args.filter, wl, wu, uu, Y, mixed=True)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.reps):
+        api.ResidualChebyshevFilterGEP(H, Mo, Mi, eig, X, args.filter, wl, wu, uu, Y, mixed=True)
+    ctx.synchronize()
+    ctx.check_status()
+    print(json.dumps({"config": args.config, "filter_degree": args.filter, "m": m, "n_dofs": prob.n_dofs,
+                      "filter_ms": (time.perf_counter() - t0) / args.reps * 1e3}))
 
 
 if __name__ == "__main__":
