@@ -152,13 +152,23 @@ __global__ void k_fold_scale(const double *__restrict__ d, const uint8_t *__rest
 // Assembly of a FP32 cell-wise result with one Chebyshev recurrence step fused
 // in (homogeneous Dirichlet rows only): with S the assembled A B^-1 RN,
 //   R = alpha1 S + (-c alpha1) RN + alpha2 R + (alpha1 eF2[j]) Y
-// in the operation order of the separate step kernel.
+// in the operation order of the separate step kernel.  The constrained rows of
+// RN read as zero and are zeroed in place: the parent-to-child step that the
+// separate B^-1 apply runs on its input (the cell product never sees those
+// rows: their factor in the folded tiles is zero).
 __global__ void k_assemble_cheb(const float *__restrict__ Yc, uint32_t m, uint64_t n_dofs,
                                 const uint32_t *__restrict__ slot_ptr, const uint32_t *__restrict__ slot,
                                 const uint8_t *__restrict__ is_row, const double *__restrict__ coef,
-                                const float *__restrict__ RN, float *__restrict__ R, const double *__restrict__ eF2,
-                                const float *__restrict__ Y, const FastDiv fm) {
+                                float *__restrict__ RN, float *__restrict__ R, const double *__restrict__ eF2,
+                                const float *__restrict__ Y, const FastDiv fm, bool sh) {
+  extern __shared__ __align__(16) unsigned char col_sh[];
+  float *g = reinterpret_cast<float *>(col_sh);
   const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
+  if (sh) {
+    load_col_factors(g, m, alpha1, eF2);
+    __syncthreads();
+  }
+  const float a1 = (float)alpha1, b1 = (float)(-c * alpha1), a2 = (float)alpha2;
   const uint64_t total = n_dofs * m;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
        t += (uint64_t)gridDim.x * blockDim.x) {
@@ -166,11 +176,13 @@ __global__ void k_assemble_cheb(const float *__restrict__ Yc, uint32_t m, uint64
     uint32_t v;
     fm.divmod(t, i, v);
     float acc = 0.f;
-    if (!(is_row && is_row[i]))
+    const bool crow = is_row && is_row[i];
+    if (!crow)
       for (uint32_t p = slot_ptr[i], e = slot_ptr[i + 1]; p < e; ++p) acc = acc + Yc[(uint64_t)slot[p] * m + v];
-    const float s1 = (float)alpha1 * acc + (float)(-c * alpha1) * RN[t];
-    const float r = s1 + (float)alpha2 * R[t];
-    R[t] = r + (float)(alpha1 * eF2[v]) * Y[t];
+    const float s1 = a1 * acc + b1 * (crow ? 0.f : RN[t]);
+    const float r = s1 + a2 * R[t];
+    R[t] = r + (sh ? g[v] : (float)(alpha1 * eF2[v])) * Y[t];
+    if (crow) RN[t] = 0.f;
   }
 }
 
@@ -194,12 +206,17 @@ __global__ void k_assemble_vec(const T *__restrict__ Yc, uint32_t m, uint64_t n_
     V acc;
 #pragma unroll
     for (int w = 0; w < W; ++w) acc.x[w] = (T)0;
-    if (!(is_row && is_row[i]))
-      for (uint32_t p = slot_ptr[i], e = slot_ptr[i + 1]; p < e; ++p) {
+    const uint32_t p0 = slot_ptr[i], e = slot_ptr[i + 1];
+    if (!(is_row && is_row[i]) && p0 < e) {
+      // the first slot starts the sum (no add to zero: for FP64 blocks the
+      // adds run on GB300's narrow FP64 pipe)
+      acc = *reinterpret_cast<const V *>(Yc + (uint64_t)slot[p0] * m + v);
+      for (uint32_t p = p0 + 1; p < e; ++p) {
         const V y = *reinterpret_cast<const V *>(Yc + (uint64_t)slot[p] * m + v);
 #pragma unroll
         for (int w = 0; w < W; ++w) acc.x[w] = acc.x[w] + y.x[w];
       }
+    }
     *reinterpret_cast<V *>(Y + i * m + v) = acc;
   }
 }
@@ -210,9 +227,16 @@ __global__ void k_assemble_vec(const T *__restrict__ Yc, uint32_t m, uint64_t n_
 __global__ void k_assemble_cheb4(const float *__restrict__ Yc, uint32_t m, uint64_t n_dofs,
                                  const uint32_t *__restrict__ slot_ptr, const uint32_t *__restrict__ slot,
                                  const uint8_t *__restrict__ is_row, const double *__restrict__ coef,
-                                 const float *__restrict__ RN, float *__restrict__ R, const double *__restrict__ eF2,
-                                 const float *__restrict__ Y, const FastDiv fq) {
+                                 float *__restrict__ RN, float *__restrict__ R, const double *__restrict__ eF2,
+                                 const float *__restrict__ Y, const FastDiv fq, bool sh) {
+  extern __shared__ __align__(16) unsigned char col_sh[];
+  float *g = reinterpret_cast<float *>(col_sh);
   const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
+  if (sh) {
+    load_col_factors(g, m, alpha1, eF2);
+    __syncthreads();
+  }
+  const float a1 = (float)alpha1, b1 = (float)(-c * alpha1), a2 = (float)alpha2;
   const uint32_t m4 = m / 4;
   const uint64_t total = n_dofs * m4;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
@@ -223,7 +247,8 @@ __global__ void k_assemble_cheb4(const float *__restrict__ Yc, uint32_t m, uint6
     const uint32_t v = 4 * q;
     const uint64_t o = i * m + v;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!(is_row && is_row[i]))
+    const bool crow = is_row && is_row[i];
+    if (!crow)
       for (uint32_t p = slot_ptr[i], e = slot_ptr[i + 1]; p < e; ++p) {
         const float4 y = __ldg(reinterpret_cast<const float4 *>(Yc + (uint64_t)slot[p] * m + v));
         acc.x = acc.x + y.x;
@@ -231,16 +256,19 @@ __global__ void k_assemble_cheb4(const float *__restrict__ Yc, uint32_t m, uint6
         acc.z = acc.z + y.z;
         acc.w = acc.w + y.w;
       }
-    const float4 rn = *reinterpret_cast<const float4 *>(RN + o);
+    const float4 rn = crow ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(RN + o);
     const float4 r0 = *reinterpret_cast<const float4 *>(R + o);
     const float4 yy = *reinterpret_cast<const float4 *>(Y + o);
-    const float a1 = (float)alpha1, b1 = (float)(-c * alpha1), a2 = (float)alpha2;
+    const float4 gg = sh ? *reinterpret_cast<const float4 *>(g + v)
+                         : make_float4((float)(alpha1 * eF2[v]), (float)(alpha1 * eF2[v + 1]),
+                                       (float)(alpha1 * eF2[v + 2]), (float)(alpha1 * eF2[v + 3]));
     float4 out;
-    out.x = (a1 * acc.x + b1 * rn.x + a2 * r0.x) + (float)(alpha1 * eF2[v]) * yy.x;
-    out.y = (a1 * acc.y + b1 * rn.y + a2 * r0.y) + (float)(alpha1 * eF2[v + 1]) * yy.y;
-    out.z = (a1 * acc.z + b1 * rn.z + a2 * r0.z) + (float)(alpha1 * eF2[v + 2]) * yy.z;
-    out.w = (a1 * acc.w + b1 * rn.w + a2 * r0.w) + (float)(alpha1 * eF2[v + 3]) * yy.w;
+    out.x = (a1 * acc.x + b1 * rn.x + a2 * r0.x) + gg.x * yy.x;
+    out.y = (a1 * acc.y + b1 * rn.y + a2 * r0.y) + gg.y * yy.y;
+    out.z = (a1 * acc.z + b1 * rn.z + a2 * r0.z) + gg.z * yy.z;
+    out.w = (a1 * acc.w + b1 * rn.w + a2 * r0.w) + gg.w * yy.w;
     *reinterpret_cast<float4 *>(R + o) = out;
+    if (crow) *reinterpret_cast<float4 *>(RN + o) = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
@@ -526,7 +554,10 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
     return false;
   const uint32_t m = RN->m;
   if (!BInv->fold_scale.p) return false;  // built at upload for diagonal operators
-  constraints_p2c(ctx, c, RN);  // BInv's parent-to-child on its input, as apply_op does
+  // BInv's parent-to-child on RN (zero rows) happens in the assembly kernel
+  // below; before it only the dense block reads rows of RN, so it runs here
+  // only when a constrained row lies inside the block
+  if (BInv->blk_cons) constraints_p2c(ctx, c, RN);
   const float *xsub = nullptr;
   if (BInv->kind == OP_DIAG_BLOCK) {
     // the enrichment rows of B^-1 RN: the dense block times those rows of RN,
@@ -550,14 +581,15 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
   const uint64_t n = (uint64_t)me->n_dofs * m;
   {
     ProfScope prof_k(ctx, "k:assemble_cheb", 0.0, 0.0);
+    const size_t sh = col_factor_smem<float>(m);
     if (m % 4 == 0)
-      k_assemble_cheb4<<<stride_grid(ctx, n / 4), 256, 0, ctx->stream>>>(
+      k_assemble_cheb4<<<stride_grid(ctx, n / 4), 256, sh, ctx->stream>>>(
           A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p, me->slot.p, c ? c->is_row.p : nullptr, coef, RN->f.p,
-          R->f.p, eF2, Y->f.p, FastDiv(m / 4));
+          R->f.p, eF2, Y->f.p, FastDiv(m / 4), sh > 0);
     else
-      k_assemble_cheb<<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p,
-                                                                   me->slot.p, c ? c->is_row.p : nullptr, coef,
-                                                                   RN->f.p, R->f.p, eF2, Y->f.p, FastDiv(m));
+      k_assemble_cheb<<<stride_grid(ctx, n), 256, sh, ctx->stream>>>(A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p,
+                                                                    me->slot.p, c ? c->is_row.p : nullptr, coef,
+                                                                    RN->f.p, R->f.p, eF2, Y->f.p, FastDiv(m), sh > 0);
     check_launch(ctx, "assemble_cheb");
   }
   return true;
@@ -706,9 +738,10 @@ int gbfe_ctx_check_status(gbfe_ctx *ctx) {
 }
 
 int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode) {
-  if (!ctx || mode < 0 || mode > 2) return GBFE_ERR_ARG;
+  if (!ctx || mode < 0 || mode > 3) return GBFE_ERR_ARG;
   ctx->use_tc = mode ? 1 : 0;
-  if (mode) ctx->tc_version = mode;
+  if (mode) ctx->tc_version = mode == 3 ? 2 : mode;
+  ctx->tc_gather4 = mode == 3 ? 0 : 1;
   return GBFE_OK;
 }
 
@@ -1155,6 +1188,13 @@ int gbfe_diag_block_upload(gbfe_mesh *mesh, const gbfe_cons *cons, const double 
     op->blk_begin = blk_begin;
     op->blk_n = blk_n;
     op->blk.upload(blk, blk_n * blk_n, mesh->ctx->stream);
+    if (cons && cons->n_rows) {
+      std::vector<uint32_t> rows(cons->n_rows);
+      GBFE_CUDA(cudaMemcpyAsync(rows.data(), cons->row_ids.p, rows.size() * 4, cudaMemcpyDeviceToHost,
+                                mesh->ctx->stream));
+      GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
+      for (uint32_t r : rows) op->blk_cons = op->blk_cons || (r >= blk_begin && r - blk_begin < blk_n);
+    }
     if (op->fold_scale.p) {
       k_fold_scale<<<grid_for(mesh->n_dofs, 256), 256, 0, mesh->ctx->stream>>>(
           op->diag.p, cons ? cons->is_row.p : nullptr, mesh->n_dofs, blk_begin, blk_n, op->fold_scale.p);

@@ -173,6 +173,7 @@ struct gbfe_ctx {
   gbfe::DBuf<int> status;    // device status word written by bounded waits (0 = ok)
   int use_tc = 1;            // split-BF16 tcgen05 cell product for the mixed path
   int tc_version = 2;        // 2: persistent warp-specialised kernel; 1: one CTA per cell
+  int tc_gather4 = 1;        // persistent kernel: 16-byte row gathers when the rows are aligned
   std::atomic<int> *cancel = nullptr;  // polled between passes / iterations when set
   int fp64_tc = 0;           // 1: FP64 applies use the sliced tensor-core product when built
   int fp64_tc_dense = 1;     // with fp64_tc: the Gram / rotation stages use the sliced products too
@@ -271,6 +272,7 @@ struct gbfe_op {
   mutable gbfe::DBuf<__nv_bfloat16> mats_hi_folded;  // split tiles of A diag(fold_scale of folded_for)
   mutable uint64_t folded_for = 0;
   uint64_t blk_begin = 0, blk_n = 0;  // OP_DIAG_BLOCK: dense block rows
+  bool blk_cons = false;              // a constrained row lies inside the block
   gbfe::DBuf<double> blk;             // column-major blk_n x blk_n
   gbfe::DBuf<float> blk_f32;
   mutable gbfe::DBuf<float> blk_out_f32;  // block rows of B^-1 X for the fused filter
@@ -314,6 +316,22 @@ struct FastDiv {
     }
   }
 };
+
+// Per-column factors f[j] = (T)(s * w[j]) of one sweep over an N x m block,
+// computed once per thread block into dynamic shared memory instead of once
+// per element: GB300's FP64 pipe retires about two operations per SM clock,
+// too few for a DMUL and a conversion per element of an FP32 sweep.
+// col_factor_smem = the dynamic shared bytes of k factor arrays (0: the block
+// width is too large, the kernel computes the factors per element).
+template <class T>
+inline size_t col_factor_smem(uint32_t m, int k = 1) {
+  const size_t b = (size_t)k * m * sizeof(T);
+  return b <= 32 * 1024 ? b : 0;
+}
+template <class T>
+__device__ __forceinline__ void load_col_factors(T *f, uint32_t m, double s, const double *__restrict__ w) {
+  for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) f[j] = (T)(s * w[j]);
+}
 
 inline unsigned grid_for(uint64_t n, unsigned block) {
   uint64_t g = (n + block - 1) / block;

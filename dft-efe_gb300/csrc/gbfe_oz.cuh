@@ -13,6 +13,8 @@
 #include <cuda_bf16.h>
 #include <cstdint>
 
+#include "gbfe_tc_ptx.cuh"
+
 namespace gbfe {
 namespace oz {
 
@@ -74,25 +76,30 @@ __device__ __forceinline__ float int_to_float_small(int d) {
 }
 
 // the 8 slices of two consecutive K values, packed as BF16 pairs (low half =
-// first value): packed[s] for slice s
+// first value): packed[s] for slice s.  A digit (|d| <= 64) is a float with
+// at most 7 significant bits, so its BF16 form is the upper half of the float
+// bits: one byte permute per pair, no conversion instruction.
 __device__ __forceinline__ void digits_pair_bf16(double v0, double v1, int e, uint32_t *packed) {
   int d0[S], d1[S];
   digits(v0, e, d0);
   digits(v1, e, d1);
 #pragma unroll
-  for (int s = 0; s < S; ++s) {
-    const __nv_bfloat162 pr = __floats2bfloat162_rn(int_to_float_small(d0[s]), int_to_float_small(d1[s]));
-    packed[s] = *reinterpret_cast<const uint32_t *>(&pr);
-  }
+  for (int s = 0; s < S; ++s)
+    packed[s] = __byte_perm(__float_as_uint(int_to_float_small(d0[s])), __float_as_uint(int_to_float_small(d1[s])),
+                            0x7632);
 }
+
+// out-of-line, so that the rare call is a branch and not FP64 work that the
+// compiler predicates into every lane
+static __device__ __noinline__ double ldexp_outlined(double v, int k) { return ldexp(v, k); }
 
 // v * 2^k by adding k to the exponent field (integer pipe), exact; zero
 // stays zero and results outside the normal range go through ldexp.
 __device__ __forceinline__ double scale2(double v, int k) {
   const long long b = __double_as_longlong(v);
   const int e = (int)((b >> 52) & 0x7ff);
-  if (e == 0) return v;                                   // zero
-  if (e + k <= 0 || e + k >= 0x7ff) return ldexp(v, k);  // leaves the normal range
+  if (e == 0) return v;                                            // zero
+  if (e + k <= 0 || e + k >= 0x7ff) return ldexp_outlined(v, k);  // leaves the normal range
   return __longlong_as_double(b + ((long long)k << 52));
 }
 
@@ -122,6 +129,59 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 // sum_g L_g 2^-7g of one accumulator column, smallest level first, as an
 // FP32 double-float (every term L_g 2^-7g is exact in FP32)
 __device__ __forceinline__ float level_weight(int g) { return __int_as_float((127 - 7 * g) << 23); }
+
+// sum_g L_g 2^-7g (g = 9 .. 2, smallest level first) for 16 columns of this
+// thread's TMEM lane; level g's accumulator at taddr + (g - 2) * stride.  The
+// load of the next level is in flight while the current one is added.
+__device__ __forceinline__ void combine16(uint32_t taddr, uint32_t stride, float *hi, float *lo) {
+#pragma unroll
+  for (int q = 0; q < 16; ++q) hi[q] = lo[q] = 0.f;
+  uint32_t La[16], Lb[16];
+  auto step = [&](uint32_t(&cur)[16], uint32_t(&nxt)[16], int g) {
+    if (g > 2) tc::tmem_ld16_issue(taddr + (uint32_t)(g - 3) * stride, nxt);
+    const float w = level_weight(g);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      float s2, e2;
+      two_sum(hi[q], __uint_as_float(cur[q]) * w, s2, e2);
+      hi[q] = s2;
+      lo[q] += e2;
+    }
+    if (g > 2) tc::tmem_wait_ld16(nxt);
+  };
+  tc::tmem_ld16_issue(taddr + (uint32_t)(S - 1) * stride, La);
+  tc::tmem_wait_ld16(La);
+  step(La, Lb, 9);
+  step(Lb, La, 8);
+  step(La, Lb, 7);
+  step(Lb, La, 6);
+  step(La, Lb, 5);
+  step(Lb, La, 4);
+  step(La, Lb, 3);
+  step(Lb, La, 2);
+}
+static_assert(S + 1 == 9, "combine16 is written out for levels 9 .. 2");
+
+// Epilogue staging of one warp (its 32 TMEM lanes = 32 output rows): 16
+// columns are combined, scaled by 2^(row_e + col_e[j] + 2) and written into the
+// warp's 32 x 16 FP64 scratch, entry (r, j) at r * 16 + (j ^ (r % 16)); the
+// row-wise reads that follow (scratch_at) hand each half-warp 16 consecutive
+// columns of one row, so the global stores are whole 128-byte row segments.
+// Both the per-lane writes and the per-row reads touch every bank pair twice
+// per warp access: no conflicts beyond the two wavefronts of 256 bytes.
+constexpr uint32_t EPI_SCRATCH_DOUBLES = 32 * 16;  // per warp
+__device__ __forceinline__ void combine16_to_scratch(uint32_t taddr, uint32_t stride, double *scratch, uint32_t lane,
+                                                     int row_e, const int (&col_e)[16]) {
+  float hi[16], lo[16];
+  combine16(taddr, stride, hi, lo);
+#pragma unroll
+  for (int j = 0; j < 16; ++j)
+    scratch[lane * 16 + (j ^ (lane & 15))] = scale2(df_to_double(hi[j], lo[j]), row_e + col_e[j] + 2);
+  __syncwarp();
+}
+__device__ __forceinline__ double scratch_at(const double *scratch, uint32_t r, uint32_t j) {
+  return scratch[r * 16 + (j ^ (r & 15))];
+}
 
 }  // namespace oz
 }  // namespace gbfe

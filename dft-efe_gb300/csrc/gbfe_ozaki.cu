@@ -39,7 +39,6 @@ using namespace gbfe::tc;
 namespace {
 
 constexpr int OZ_S = 8;        // slices per operand
-constexpr int OZ_LEVELS = 8;   // g = 2..9
 constexpr int OZ_N = 64;       // vectors per work item (8 levels x 64 = 512 TMEM columns)
 constexpr int OZ_STAGES = 2;
 constexpr int OZ_GW = 8;                       // gather / epilogue warps
@@ -48,6 +47,9 @@ constexpr int OZ_THREADS = (OZ_GW + 2) * 32;
 constexpr uint32_t OZ_A_PART = 128 * KC * 2;  // one slice of a 128-row A chunk (bytes)
 constexpr uint32_t OZ_B_PART = OZ_N * KC * 2;  // one slice of a B chunk
 constexpr uint32_t OZ_STAGE = OZ_S * (OZ_A_PART + OZ_B_PART);
+constexpr uint32_t OZ_EPI = OZ_GW * oz::EPI_SCRATCH_DOUBLES * 8;  // epilogue staging, one 4 KB tile per warp
+constexpr uint32_t OZ_SMEM = OZ_STAGES * OZ_STAGE + OZ_EPI + 1024 + 512;
+static_assert(OZ_SMEM <= 227 * 1024, "sliced cell product: shared memory");
 
 __device__ __forceinline__ void oz_digits(double v, int e, int *d) { oz::digits(v, e, d); }
 __device__ __forceinline__ int oz_exponent(double vmax) { return oz::exponent_of(vmax); }
@@ -121,18 +123,18 @@ struct OzArgs {
   int *status;
 };
 
-using oz::two_sum;
-
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t *bars = (uint64_t *)(smem + OZ_STAGES * OZ_STAGE);
+  double *epi_scratch = (double *)(smem + OZ_STAGES * OZ_STAGE);
+  uint64_t *bars = (uint64_t *)(smem + OZ_STAGES * OZ_STAGE + OZ_EPI);
   uint64_t *full_a = bars;
   uint64_t *full_b = bars + OZ_STAGES;
   uint64_t *empty = bars + 2 * OZ_STAGES;
   uint64_t *tfull = bars + 3 * OZ_STAGES;
   uint64_t *tempty = tfull + 1;
-  uint32_t *tmem_slot = (uint32_t *)(tempty + 1);
+  uint64_t *spare = tempty + 1;  // drain_mmas before TMEM is freed
+  uint32_t *tmem_slot = (uint32_t *)(spare + 1);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   const uint32_t tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
   const uint32_t m = a.m;
@@ -147,6 +149,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
     }
     mbar_init(tfull, 1);
     mbar_init(tempty, OZ_GW);
+    mbar_init(spare, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -197,6 +200,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
           }
         }
       }
+      drain_copies(full_a, q, OZ_STAGES);
     }
     __syncwarp();
   } else if (warp == OZ_MMA_WARP) {
@@ -241,85 +245,92 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
         if (!ok) break;
         umma_commit(tfull);
       }
+      drain_mmas(spare);
     }
     __syncwarp();
   } else {
     // ---------------- gather warps 0-7: X rows -> 8 digit slices; epilogue
+    // (KC/8) K blocks x (OZ_N/32) vector groups = 8 items per chunk, one per
+    // warp: warp w always gathers K block w % 4 of vector group w / 4.  The
+    // row loads of the next chunk (of this item, or the first chunk of the
+    // next item, across the epilogue) are issued before the current chunk's
+    // digits are cut, so their latency overlaps that work.
+    static_assert((KC / 8) * (OZ_N / 32) == OZ_GW, "one gather item per warp");
+    const uint32_t kb = warp % (KC / 8), vg = warp / (KC / 8);
+    const uint32_t v = vg * 32 + lane;
+    auto load_chunk = [&](uint32_t it, uint32_t kc, double (&x)[8]) {
+      uint32_t c, mt, v0;
+      decode(it, c, mt, v0);
+      const uint32_t off = a.cell_off[c], nd = a.cell_off[c + 1] - off;
+      const bool vin = (v0 + v) < m;
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        const uint32_t k = kc * KC + kb * 8 + kk;
+        x[kk] = (vin && k < nd) ? __ldg(a.X + (uint64_t)a.ids[off + k] * m + v0 + v) : 0.0;
+      }
+    };
     uint32_t q = 0, li = 0;
     bool ok = true;
+    double xcur[8], xnxt[8];
+    if (blockIdx.x < n_items) load_chunk(blockIdx.x, 0, xcur);
     for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
       uint32_t c, mt, v0;
       decode(it, c, mt, v0);
       const uint32_t off = a.cell_off[c], nd = a.cell_off[c + 1] - off;
       const uint32_t nk = (nd + KC - 1) / KC;
+      const bool vin = (v0 + v) < m;
+      const int ex = vin ? a.x_exp[v0 + v] : 0;
       for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
         const uint32_t s = q % OZ_STAGES;
+        // prefetch: the next chunk of this item, else the first of the next item
+        const bool more = kc + 1 < nk || it + gridDim.x < n_items;
+        if (more) load_chunk(kc + 1 < nk ? it : it + gridDim.x, kc + 1 < nk ? kc + 1 : 0, xnxt);
         if (q >= OZ_STAGES) {
           ok = __all_sync(0xffffffffu, wait(&empty[s], ((q / OZ_STAGES) - 1) & 1, 25));
           if (!ok) break;
         }
         uint8_t *Bst = smem + s * OZ_STAGE + OZ_S * OZ_A_PART;
-        // (KC/8) K blocks x (OZ_N/32) vector groups = 8 items, one per warp
-        for (uint32_t item = warp; item < (KC / 8) * (OZ_N / 32); item += OZ_GW) {
-          const uint32_t kb = item % (KC / 8), vg = item / (KC / 8);
-          const uint32_t v = vg * 32 + lane;
-          const bool vin = (v0 + v) < m;
-          const int ex = vin ? a.x_exp[v0 + v] : 0;
-          uint32_t packed[OZ_S][4];
+        uint32_t packed[OZ_S][4];
 #pragma unroll
-          for (int kk = 0; kk < 8; kk += 2) {
-            const uint32_t k0 = kc * KC + kb * 8 + kk;
-            const double x0 = (vin && k0 < nd) ? __ldg(a.X + (uint64_t)a.ids[off + k0] * m + v0 + v) : 0.0;
-            const double x1 = (vin && k0 + 1 < nd) ? __ldg(a.X + (uint64_t)a.ids[off + k0 + 1] * m + v0 + v) : 0.0;
-            uint32_t pp[OZ_S];
-            oz::digits_pair_bf16(x0, x1, ex, pp);
+        for (int kk = 0; kk < 8; kk += 2) {
+          uint32_t pp[OZ_S];
+          oz::digits_pair_bf16(xcur[kk], xcur[kk + 1], ex, pp);
 #pragma unroll
-            for (int sl = 0; sl < OZ_S; ++sl) packed[sl][kk / 2] = pp[sl];
-          }
-          const uint32_t pos = (v / 8) * SBO + kb * LBO + (v % 8) * 16;
-#pragma unroll
-          for (int sl = 0; sl < OZ_S; ++sl)
-            *(uint4 *)(Bst + sl * OZ_B_PART + pos) = make_uint4(packed[sl][0], packed[sl][1], packed[sl][2], packed[sl][3]);
+          for (int sl = 0; sl < OZ_S; ++sl) packed[sl][kk / 2] = pp[sl];
         }
+        const uint32_t pos = (v / 8) * SBO + kb * LBO + (v % 8) * 16;
+#pragma unroll
+        for (int sl = 0; sl < OZ_S; ++sl)
+          *(uint4 *)(Bst + sl * OZ_B_PART + pos) = make_uint4(packed[sl][0], packed[sl][1], packed[sl][2], packed[sl][3]);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
         if (lane == 0) mbar_arrive(&full_b[s]);
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) xcur[kk] = xnxt[kk];
       }
       if (!ok) break;
       // epilogue of this item (single TMEM buffer)
       ok = __all_sync(0xffffffffu, wait(tfull, li & 1, 26));
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // warp w reads TMEM lanes of quadrant w % 4, columns [32 (w / 4), +32)
+      // warp w reads TMEM lanes of quadrant w % 4, columns [32 (w / 4), +32),
+      // 16 at a time, staged through its scratch tile into whole-row stores
       const uint32_t quad = warp % 4, colh = warp / 4;
       const uint32_t row = mt * 128 + quad * 32 + lane;
       const int er = row < nd ? a.row_exp[off + row] : 0;
+      double *scr = epi_scratch + warp * oz::EPI_SCRATCH_DOUBLES;
       for (uint32_t col = colh * 32; col < colh * 32 + 32; col += 16) {
-        float hi[16], lo[16];
+        int xe[16];
 #pragma unroll
-        for (int q2 = 0; q2 < 16; ++q2) hi[q2] = lo[q2] = 0.f;
-        for (int g = OZ_S + 1; g >= 2; --g) {  // smallest level first
-          float L[16];
-          tmem_ld16(tmem + ((quad * 32) << 16) + (g - 2) * OZ_N + col, L);
-          const float w = __int_as_float((127 - 7 * g) << 23);  // 2^-7g, exact
-#pragma unroll
-          for (int q2 = 0; q2 < 16; ++q2) {
-            float s2, e2;
-            two_sum(hi[q2], L[q2] * w, s2, e2);
-            hi[q2] = s2;
-            lo[q2] += e2;
-          }
+        for (int j = 0; j < 16; ++j) xe[j] = (v0 + col + j < m) ? a.x_exp[v0 + col + j] : 0;
+        oz::combine16_to_scratch(tmem + ((quad * 32) << 16) + col, OZ_N, scr, lane, er, xe);
+        const uint32_t j = lane % 16, v = v0 + col + j;
+#pragma unroll 4
+        for (uint32_t i = 0; i < 16; ++i) {
+          const uint32_t r = 2 * i + lane / 16, orow = mt * 128 + quad * 32 + r;
+          if (orow < nd && v < m) a.Yc[(uint64_t)(off + orow) * m + v] = oz::scratch_at(scr, r, j);
         }
-        if (row < nd) {
-          double *dst = a.Yc + (uint64_t)(off + row) * m + v0 + col;
-#pragma unroll
-          for (int q2 = 0; q2 < 16; ++q2) {
-            const uint32_t v = v0 + col + q2;
-            if (v < m) {
-              dst[q2] = oz::scale2(oz::df_to_double(hi[q2], lo[q2]), er + a.x_exp[v] + 2);
-            }
-          }
-        }
+        __syncwarp();
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
@@ -370,7 +381,7 @@ void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc) {
   k_colmax_final<<<(m + 127) / 128, 128, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, m, op->oz_xexp.p);
   count_launch(ctx, 2);
   const uint32_t vt = (m + OZ_N - 1) / OZ_N;
-  const uint32_t smem = OZ_STAGES * OZ_STAGE + 1024 + 512;
+  const uint32_t smem = OZ_SMEM;
   static bool attr_set = false;  // once: not a stream operation, so it stays out of graph captures
   if (!attr_set) {
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

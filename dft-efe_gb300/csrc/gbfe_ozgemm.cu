@@ -39,7 +39,9 @@ constexpr int OG_STAGES = 2;
 constexpr uint32_t A_PART = 128 * KC * 2;  // one slice of a 128 x KC tile (bytes)
 constexpr uint32_t B_PART = OG_N * KC * 2;
 constexpr uint32_t OG_STAGE = oz::S * (A_PART + B_PART);
-constexpr uint32_t OG_SMEM = OG_STAGES * OG_STAGE + 1024 + 512;
+constexpr uint32_t OG_EPI = PW * oz::EPI_SCRATCH_DOUBLES * 8;  // rotation epilogue staging, 4 KB per warp
+constexpr uint32_t OG_SMEM = OG_STAGES * OG_STAGE + OG_EPI + 1024 + 512;
+static_assert(OG_SMEM <= 227 * 1024, "sliced dense products: shared memory");
 constexpr uint32_t CHUNK = oz::K_EXACT;    // Gram rows per exact TMEM accumulation
 constexpr uint32_t STAGES_PER_CHUNK = CHUNK / KC;
 constexpr uint32_t TILE = 128 * OG_N;      // elements of one partial tile
@@ -81,39 +83,28 @@ __device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t abase, uint
 
 // sum_g L_g 2^-7g for 16 columns of this thread's TMEM lane
 __device__ __forceinline__ void combine16(uint32_t taddr, float *hi, float *lo) {
-#pragma unroll
-  for (int q = 0; q < 16; ++q) hi[q] = lo[q] = 0.f;
-  for (int g = oz::S + 1; g >= 2; --g) {  // smallest level first
-    float L[16];
-    tmem_ld16(taddr + (g - 2) * OG_N, L);
-    const float w = oz::level_weight(g);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      float s2, e2;
-      oz::two_sum(hi[q], L[q] * w, s2, e2);
-      hi[q] = s2;
-      lo[q] += e2;
-    }
-  }
+  oz::combine16(taddr, OG_N, hi, lo);
 }
 
 struct Barriers {
-  uint64_t *full, *full_b, *empty, *tfull, *tempty;
+  uint64_t *full, *full_b, *empty, *tfull, *tempty, *spare;
   uint32_t *tmem_slot;
   volatile int *abort_flag;
 };
 
-// barrier block after the stages: full[S], full_b[S], empty[S], tfull, tempty,
-// then the TMEM address and the abort flag
+// after the stages the epilogue scratch (OG_EPI), then the barrier block:
+// full[S], full_b[S], empty[S], tfull, tempty, spare, the TMEM address and the
+// abort flag
 __device__ __forceinline__ Barriers carve(uint8_t *smem) {
   Barriers b;
-  uint64_t *bars = (uint64_t *)(smem + OG_STAGES * OG_STAGE);
+  uint64_t *bars = (uint64_t *)(smem + OG_STAGES * OG_STAGE + OG_EPI);
   b.full = bars;
   b.full_b = bars + OG_STAGES;
   b.empty = bars + 2 * OG_STAGES;
   b.tfull = bars + 3 * OG_STAGES;
   b.tempty = b.tfull + 1;
-  b.tmem_slot = (uint32_t *)(b.tempty + 1);
+  b.spare = b.tempty + 1;  // drain_mmas before TMEM is freed
+  b.tmem_slot = (uint32_t *)(b.spare + 1);
   b.abort_flag = (volatile int *)(b.tmem_slot + 1);
   return b;
 }
@@ -145,6 +136,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
     }
     mbar_init(br.tfull, 1);
     mbar_init(br.tempty, PW);
+    mbar_init(br.spare, 1);
     *br.abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -199,6 +191,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
           if (ok) umma_commit(br.tfull);
         }
       }
+      drain_mmas(br.spare);
     }
     __syncwarp();
   } else if (warp < PW) {
@@ -341,6 +334,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
     }
     mbar_init(br.tfull, 1);
     mbar_init(br.tempty, PW);
+    mbar_init(br.spare, 1);
     *br.abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -383,6 +377,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
           for (int sl = 0; sl < oz::S; ++sl) bulk_g2s(Bt + sl * B_PART, src + (uint64_t)sl * OG_N * KC, B_PART, &full_b[s]);
         }
       }
+      drain_copies(full_b, q, OG_STAGES);
     }
     __syncwarp();
   } else if (warp == PW + 1) {
@@ -408,6 +403,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
         if (!ok) break;
         umma_commit(br.tfull);
       }
+      drain_mmas(br.spare);
     }
     __syncwarp();
   } else {
@@ -451,17 +447,22 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint64_t orow = (uint64_t)rt * 128 + quad * 32 + lane;
       const int oe = orow < a.N ? a.rexp[(uint64_t)op * a.N + orow] : 0;
-#pragma unroll
+      double *scr = (double *)(smem + OG_STAGES * OG_STAGE) + warp * oz::EPI_SCRATCH_DOUBLES;
+#pragma unroll 1
       for (int cg = 0; cg < 2; ++cg) {
-        float hi[16], lo[16];
-        combine16(tmem + ((quad * 32) << 16) + colh * 32 + cg * 16, hi, lo);
         const uint32_t j0 = ct * OG_N + colh * 32 + cg * 16;
-        if (orow < a.N) {
-          double *dst = a.out[op] + orow * a.mo + j0;
+        int te[16];
 #pragma unroll
-          for (int i = 0; i < 16; ++i)
-            if (j0 + i < a.mo) dst[i] = oz::scale2(oz::df_to_double(hi[i], lo[i]), oe + a.texp[j0 + i] + 2);
+        for (int i = 0; i < 16; ++i) te[i] = (j0 + i < a.mo) ? a.texp[j0 + i] : 0;
+        oz::combine16_to_scratch(tmem + ((quad * 32) << 16) + colh * 32 + cg * 16, OG_N, scr, lane, oe, te);
+        const uint32_t j = lane % 16;
+#pragma unroll 4
+        for (uint32_t i = 0; i < 16; ++i) {
+          const uint32_t r = 2 * i + lane / 16;
+          const uint64_t grow = (uint64_t)rt * 128 + quad * 32 + r;
+          if (grow < a.N && j0 + j < a.mo) a.out[op][grow * a.mo + j0 + j] = oz::scratch_at(scr, r, j);
         }
+        __syncwarp();
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();

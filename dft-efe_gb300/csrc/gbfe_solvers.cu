@@ -35,13 +35,20 @@ __global__ void k_axpby(uint64_t n, double a, const T *__restrict__ x, double b,
 template <class T>
 __global__ void k_axpby_blocked(uint64_t rows, uint32_t m, double a1, const double *__restrict__ alpha,
                                 const T *__restrict__ x, double b1, const double *__restrict__ beta,
-                                const T *__restrict__ y, T *__restrict__ z, const FastDiv fm) {
+                                const T *__restrict__ y, T *__restrict__ z, const FastDiv fm, bool sh) {
+  extern __shared__ __align__(16) unsigned char col_sh[];
+  T *fa = reinterpret_cast<T *>(col_sh), *fb = fa + m;
+  if (sh) {
+    load_col_factors(fa, m, a1, alpha);
+    load_col_factors(fb, m, b1, beta);
+    __syncthreads();
+  }
   const uint64_t n = rows * m;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t i;
     uint32_t j;
     fm.divmod(t, i, j);
-    z[t] = (T)(a1 * alpha[j]) * x[t] + (T)(b1 * beta[j]) * y[t];
+    z[t] = (sh ? fa[j] : (T)(a1 * alpha[j])) * x[t] + (sh ? fb[j] : (T)(b1 * beta[j])) * y[t];
   }
 }
 
@@ -50,14 +57,21 @@ __global__ void k_axpby_blocked(uint64_t rows, uint32_t m, double a1, const doub
 template <class T>
 __global__ void k_cheb_step(uint64_t n, uint32_t m, double alpha1, double c, double alpha2,
                             const T *__restrict__ AS, const T *__restrict__ RN, T *__restrict__ R,
-                            const double *__restrict__ eF2, const T *__restrict__ Y, const FastDiv fm) {
+                            const double *__restrict__ eF2, const T *__restrict__ Y, const FastDiv fm, bool sh) {
+  extern __shared__ __align__(16) unsigned char col_sh[];
+  T *g = reinterpret_cast<T *>(col_sh);
+  if (sh) {
+    load_col_factors(g, m, alpha1, eF2);
+    __syncthreads();
+  }
+  const T a1 = (T)alpha1, b1 = (T)(-c * alpha1), a2 = (T)alpha2;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t i;
     uint32_t j;
     fm.divmod(t, i, j);
-    T s1 = (T)alpha1 * AS[t] + (T)(-c * alpha1) * RN[t];
-    T r = s1 + (T)alpha2 * R[t];
-    R[t] = r + (T)(alpha1 * eF2[j]) * Y[t];
+    T s1 = a1 * AS[t] + b1 * RN[t];
+    T r = s1 + a2 * R[t];
+    R[t] = r + (sh ? g[j] : (T)(alpha1 * eF2[j])) * Y[t];
   }
 }
 
@@ -66,15 +80,22 @@ __global__ void k_cheb_step(uint64_t n, uint32_t m, double alpha1, double c, dou
 template <class T>
 __global__ void k_cheb_step_dev(uint64_t n, uint32_t m, const double *__restrict__ coef, const T *__restrict__ AS,
                                 const T *__restrict__ RN, T *__restrict__ R, const double *__restrict__ eF2,
-                                const T *__restrict__ Y, const FastDiv fm) {
+                                const T *__restrict__ Y, const FastDiv fm, bool sh) {
+  extern __shared__ __align__(16) unsigned char col_sh[];
+  T *g = reinterpret_cast<T *>(col_sh);
   const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
+  if (sh) {
+    load_col_factors(g, m, alpha1, eF2);
+    __syncthreads();
+  }
+  const T a1 = (T)alpha1, b1 = (T)(-c * alpha1), a2 = (T)alpha2;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t i;
     uint32_t j;
     fm.divmod(t, i, j);
-    T s1 = (T)alpha1 * AS[t] + (T)(-c * alpha1) * RN[t];
-    T r = s1 + (T)alpha2 * R[t];
-    R[t] = r + (T)(alpha1 * eF2[j]) * Y[t];
+    T s1 = a1 * AS[t] + b1 * RN[t];
+    T r = s1 + a2 * R[t];
+    R[t] = r + (sh ? g[j] : (T)(alpha1 * eF2[j])) * Y[t];
   }
 }
 
@@ -173,12 +194,15 @@ void d_axpby(gbfe_ctx *ctx, double a, const gbfe_mv *x, double b, const gbfe_mv 
 void d_axpby_blocked(gbfe_ctx *ctx, double a1, const double *alpha_d, const gbfe_mv *x, double b1,
                      const double *beta_d, const gbfe_mv *y, gbfe_mv *z) {
   const uint64_t n = z->count();
-  if (z->dtype == GBFE_F64)
-    k_axpby_blocked<double><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(z->mesh->n_dofs, z->m, a1, alpha_d, x->d.p, b1,
-                                                                     beta_d, y->d.p, z->d.p, FastDiv(z->m));
-  else
-    k_axpby_blocked<float><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(z->mesh->n_dofs, z->m, a1, alpha_d, x->f.p, b1,
-                                                                    beta_d, y->f.p, z->f.p, FastDiv(z->m));
+  if (z->dtype == GBFE_F64) {
+    const size_t sh = col_factor_smem<double>(z->m, 2);
+    k_axpby_blocked<double><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(z->mesh->n_dofs, z->m, a1, alpha_d, x->d.p, b1,
+                                                                      beta_d, y->d.p, z->d.p, FastDiv(z->m), sh > 0);
+  } else {
+    const size_t sh = col_factor_smem<float>(z->m, 2);
+    k_axpby_blocked<float><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(z->mesh->n_dofs, z->m, a1, alpha_d, x->f.p, b1,
+                                                                     beta_d, y->f.p, z->f.p, FastDiv(z->m), sh > 0);
+  }
   check_launch(ctx, "axpby_blocked");
 }
 
@@ -390,15 +414,17 @@ void launch_cheb_step(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha1, doub
 template <>
 void launch_cheb_step<double>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha1, double c, double alpha2,
                               const gbfe_mv *AS, const gbfe_mv *RN, gbfe_mv *R, const double *eF2, const gbfe_mv *Y) {
-  k_cheb_step<double><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, alpha1, c, alpha2, AS->d.p, RN->d.p, R->d.p, eF2,
-                                                              Y->d.p, FastDiv(m));
+  const size_t sh = col_factor_smem<double>(m);
+  k_cheb_step<double><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(n, m, alpha1, c, alpha2, AS->d.p, RN->d.p, R->d.p, eF2,
+                                                               Y->d.p, FastDiv(m), sh > 0);
   check_launch(ctx, "cheb_step");
 }
 template <>
 void launch_cheb_step<float>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha1, double c, double alpha2,
                              const gbfe_mv *AS, const gbfe_mv *RN, gbfe_mv *R, const double *eF2, const gbfe_mv *Y) {
-  k_cheb_step<float><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, alpha1, c, alpha2, AS->f.p, RN->f.p, R->f.p, eF2,
-                                                             Y->f.p, FastDiv(m));
+  const size_t sh = col_factor_smem<float>(m);
+  k_cheb_step<float><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(n, m, alpha1, c, alpha2, AS->f.p, RN->f.p, R->f.p, eF2,
+                                                              Y->f.p, FastDiv(m), sh > 0);
   check_launch(ctx, "cheb_step_f32");
 }
 
@@ -521,12 +547,15 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
         continue;
       apply_op(BInv, rn, s1);
       apply_op(A, s1, s2);
-      if (mixed)
-        k_cheb_step_dev<float><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, w.coef.p + 3 * k, s2->f.p, rn->f.p,
-                                                                        r->f.p, w.tab.p + (size_t)k * m, Yr->f.p, FastDiv(m));
-      else
-        k_cheb_step_dev<double><<<sgrid(ctx, n), 256, 0, ctx->stream>>>(n, m, w.coef.p + 3 * k, s2->d.p, rn->d.p,
-                                                                         r->d.p, w.tab.p + (size_t)k * m, Yr->d.p, FastDiv(m));
+      if (mixed) {
+        const size_t sh = col_factor_smem<float>(m);
+        k_cheb_step_dev<float><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
+            n, m, w.coef.p + 3 * k, s2->f.p, rn->f.p, r->f.p, w.tab.p + (size_t)k * m, Yr->f.p, FastDiv(m), sh > 0);
+      } else {
+        const size_t sh = col_factor_smem<double>(m);
+        k_cheb_step_dev<double><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
+            n, m, w.coef.p + 3 * k, s2->d.p, rn->d.p, r->d.p, w.tab.p + (size_t)k * m, Yr->d.p, FastDiv(m), sh > 0);
+      }
       check_launch(ctx, "cheb_step");
     }
   };
@@ -749,8 +778,25 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   GBFE_CUSOLVER(cusolverDnDpotrf(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, ctx->lwork.p, lwork,
                                  ctx->info.p));
   count_launch(ctx);
+  const double one = 1.0, zero = 0.0;
+  auto trsm_sandwich = [&] {  // Hp = L^-1 S_H L^-T
+    GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
+                            m, m, &one, st.SM.p, m, st.SH.p, m));
+    GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT,
+                            m, m, &one, st.SM.p, m, st.SH.p, m));
+    count_launch(ctx, 2);
+  };
+  // host eigensolver: the factor checks, the sandwich's download and the
+  // eigensolve share one synchronisation (the sandwich of a failed factor is
+  // computed and discarded); the device eigensolver checks the factor first
+  const bool host_eig = ctx->small_eig_host && m <= SMALL_EIG_HOST_MAX;
   int info = 0;
-  std::vector<double> hL((size_t)m * m);
+  std::vector<double> hL((size_t)m * m), hS;
+  if (host_eig) {
+    trsm_sandwich();
+    hS.resize((size_t)m * m);
+    GBFE_CUDA(cudaMemcpyAsync(hS.data(), st.SH.p, hS.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  }
   GBFE_CUDA(cudaMemcpyAsync(&info, ctx->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GBFE_CUDA(cudaMemcpyAsync(hL.data(), st.SM.p, hL.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
   GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -763,14 +809,14 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
       msg = "Chol GS cannot orthogonalize the given multivector (near-zero diagonal of L)";
       return GBFE_ERR_NOT_ORTHONORMALIZABLE;
     }
-  const double one = 1.0, zero = 0.0;
-  // Hp = L^-1 S_H L^-T
-  GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, m,
-                          m, &one, st.SM.p, m, st.SH.p, m));
-  GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, m,
-                          m, &one, st.SM.p, m, st.SH.p, m));
-  count_launch(ctx, 2);
-  {
+  if (host_eig) {
+    if (host_sym_eig(m, hS.data(), eig_h) != 0) {
+      msg = "LAPACK_ERROR: FAILED_STANDARD_EIGENPROBLEM (QR iteration did not converge)";
+      return GBFE_ERR_LAPACK;
+    }
+    h2d_staged(ctx, ctx->pin_small, st.SH.p, hS.data(), hS.size() * 8);
+  } else {
+    trsm_sandwich();
     const int rc = small_syevd(ctx, m, st.SH.p, eig_h, msg);
     if (rc != GBFE_OK) return rc;
   }

@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_cell_apply_tc(
   const uint32_t tmem = *tmem_slot;
   const uint32_t idesc = instr_desc(128, (int)N);
   bool ok = true;
+  uint32_t issued = 0;  // thread 0: chunks whose copies were issued
 
   for (uint32_t kc = 0; kc < nk && ok; ++kc) {
     const uint32_t s = kc % STAGES;
@@ -152,6 +153,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_cell_apply_tc(
       mbar_arrive_expect_tx(&full[s], 2 * part);
       bulk_g2s(Ahi, src, part, &full[s]);
       bulk_g2s(Alo, src + (uint64_t)mt8 * KC, part, &full[s]);
+      ++issued;
     }
     // gather the X tile: warp-item = (8-dof K block, 32-vector group)
     const uint32_t nvg = N / 32 + ((N % 32) ? 1 : 0);
@@ -197,8 +199,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_cell_apply_tc(
     // all threads learn whether thread 0 saw a timeout
     ok = __syncthreads_and(ok ? 1 : 0);
   }
-  if (tid == 0 && ok) umma_commit(done);
-  if (ok) ok = mbar_wait(done, 0, status, 3);
+  if (tid == 0 && !ok) {
+    // a wait gave up: the copy of the chunk that failed may still be landing
+    drain_copies(full, issued, STAGES);
+  }
+  if (tid == 0) umma_commit(done);  // also drains the MMAs on the failure path
+  if (ok)
+    ok = mbar_wait(done, 0, status, 3);
+  else if (tid == 0)
+    mbar_wait(done, 0, nullptr, 0);
   ok = __syncthreads_and(ok ? 1 : 0);  // tcgen05.ld below is warp-collective
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
@@ -216,7 +225,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_cell_apply_tc(
 #pragma unroll
             for (int q = 0; q < 4; ++q) ((float4 *)dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
           } else {
-            for (uint32_t q = 0; q < nvalid; ++q) dst[q] = v[q];
+#pragma unroll
+            for (uint32_t q = 0; q < 16; ++q)
+              if (q < nvalid) dst[q] = v[q];
           }
         }
       }
@@ -266,6 +277,10 @@ struct Tc2Args {
   // overlap; the diagonal part of B^-1 is folded into the tiles)
   const float *xsub;
   uint32_t sub_begin, sub_n;
+  // > 0: float4 gather (m % 4 == 0, 16-byte aligned X / xsub): groups of wpc
+  // warps (a power of two, wpc * 32 lanes >= (KC / 8) * N / 4) each own every
+  // (GATHER_WARPS / wpc)-th chunk; 0: one scalar row element per lane
+  uint32_t wpc;
 };
 
 __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a) {
@@ -280,22 +295,30 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
   uint64_t *empty = bars + 2 * MAX_STAGES;
   uint64_t *tfull = bars + 3 * MAX_STAGES;
   uint64_t *tempty = tfull + 2;
-  uint32_t *tmem_slot = (uint32_t *)(tempty + 2);
+  uint64_t *spare = tempty + 2;  // drain_mmas before TMEM is freed
+  uint32_t *tmem_slot = (uint32_t *)(spare + 1);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
   const uint32_t tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
   const uint32_t n_items = a.ncells * a.vt;
 
+  // float4 gather: groups of wpc warps take ring chunks round robin.  A
+  // group's parity wait on a stage is only unambiguous when at most S chunks
+  // are in flight, so there are never more groups than stages.
+  uint32_t wpc = a.wpc;
+  if (wpc)
+    while (GATHER_WARPS / wpc > S) wpc *= 2;
   if (tid == 0) {
     for (uint32_t s = 0; s < MAX_STAGES; ++s) {
       mbar_init(&full_a[s], 1);
-      mbar_init(&full_b[s], GATHER_WARPS);
+      mbar_init(&full_b[s], wpc ? wpc : GATHER_WARPS);
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], GATHER_WARPS);
     }
+    mbar_init(spare, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -337,6 +360,7 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
           bulk_g2s(Ahi + a_part, src + (uint64_t)mt8 * KC, part, &full_a[s]);
         }
       }
+      drain_copies(full_a, q, S);
     }
     __syncwarp();  // lanes 1-31 wait for lane 0 before the CTA barrier
   } else if (warp == MMA_WARP2) {
@@ -378,10 +402,11 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
         if (!ok) break;
         umma_commit(&tfull[b]);
       }
+      drain_mmas(spare);
     }
     __syncwarp();
   } else {
-    // ---------------- gather warps (0-3) + epilogue
+    // ---------------- gather warps (0-7) + epilogue
     const uint32_t nvg = (N + 31) / 32;
     const uint32_t lag = nbuf - 1;  // with two TMEM buffers the epilogue trails by one cell
     auto epilogue = [&](uint32_t li, uint32_t it) -> bool {
@@ -407,7 +432,9 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
               for (int qq = 0; qq < 4; ++qq)
                 ((float4 *)dst)[qq] = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
             } else {
-              for (uint32_t qq = 0; qq < nvalid; ++qq) dst[qq] = v[qq];
+#pragma unroll
+              for (uint32_t qq = 0; qq < 16; ++qq)
+                if (qq < nvalid) dst[qq] = v[qq];
             }
           }
         }
@@ -419,6 +446,76 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
     };
     uint32_t q = 0, li = 0, prev_it = 0;
     bool ok = true;
+    if (wpc) {
+      // float4 gather.  Lane-item (kb, vq) of a chunk = 8 rows (kb*8 ..) x 4
+      // vectors (4*vq ..): 8 independent 16-byte row loads per lane, split and
+      // stored as four 16-byte K-major rows of the B tile.  A group of wpc
+      // warps covers one chunk; the G groups take chunks round robin, so G
+      // chunks are gathered concurrently (the loads are issued before the wait
+      // for the ring stage).
+      const uint32_t G = GATHER_WARPS / wpc, grp = warp / wpc;
+      const uint32_t nq = N / 4, L = (warp % wpc) * 32 + lane;
+      const uint32_t kb = L / nq, vq = L % nq;
+      const bool active = L < (KC / 8) * nq;
+      for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
+        const uint32_t c = a.cells[it / a.vt];
+        const uint32_t v0 = (it % a.vt) * N;
+        const uint32_t off = a.cell_off[c], nd = a.cell_off[c + 1] - off;
+        const uint32_t nk = (nd + KC - 1) / KC;
+        const bool vin = active && (v0 + 4 * vq) < m;
+        for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
+          if (q % G != grp) continue;
+          const uint32_t s = q % S;
+          const uint32_t k0 = kc * KC + kb * 8;
+          float4 xv[8];
+#pragma unroll
+          for (int kk = 0; kk < 8; ++kk)
+            xv[kk] = (vin && k0 + kk < nd)
+                         ? __ldg(reinterpret_cast<const float4 *>(a.X + (uint64_t)a.ids[off + k0 + kk] * m + v0 + 4 * vq))
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+          if (a.xsub && vin) {
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+              const uint32_t e = (k0 + kk < nd ? a.ids[off + k0 + kk] : a.sub_begin + a.sub_n) - a.sub_begin;
+              if (e < a.sub_n) xv[kk] = __ldg(reinterpret_cast<const float4 *>(a.xsub + (uint64_t)e * m + v0 + 4 * vq));
+            }
+          }
+          if (q >= S) {
+            ok = __all_sync(0xffffffffu, wait(&empty[s], ((q / S) - 1) & 1, 16));
+            if (!ok) break;
+          }
+          if (active) {
+            uint8_t *Bhi = smem + s * stage_bytes + 2 * a_part;
+            uint8_t *Blo = Bhi + b_part;
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+              uint32_t ph[4], pl[4];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                const float4 &x0 = xv[2 * j], &x1 = xv[2 * j + 1];
+                __nv_bfloat16 h0, l0, h1, l1;
+                split_bf16(w == 0 ? x0.x : w == 1 ? x0.y : w == 2 ? x0.z : x0.w, h0, l0);
+                split_bf16(w == 0 ? x1.x : w == 1 ? x1.y : w == 2 ? x1.z : x1.w, h1, l1);
+                ph[j] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                pl[j] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+              }
+              const uint32_t v = 4 * vq + w;
+              const uint32_t pos = (v / 8) * SBO + kb * LBO + (v % 8) * 16;
+              *(uint4 *)(Bhi + pos) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+              *(uint4 *)(Blo + pos) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+            }
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&full_b[s]);
+        }
+        if (!ok) break;
+        if (lag && li >= 1) ok = epilogue(li - 1, prev_it);
+        if (!lag) ok = ok && epilogue(li, it);
+        prev_it = it;
+      }
+      if (ok && lag && li >= 1) epilogue(li - 1, prev_it);
+    } else {
     for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
       const uint32_t c = a.cells[it / a.vt];
       const uint32_t v0 = (it % a.vt) * N;
@@ -487,6 +584,7 @@ __global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a)
       prev_it = it;
     }
     if (ok && lag && li >= 1) epilogue(li - 1, prev_it);
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -566,9 +664,15 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     attr_set = true;
   }
+  // float4 gather when every row of X (and of xsub) starts on a 16-byte boundary
+  uint32_t wpc = 0;
+  if (m % 4 == 0 && ((uintptr_t)X->f.p % 16) == 0 && ((uintptr_t)xsub % 16) == 0 && ctx->tc_gather4) {
+    wpc = 1;
+    while (wpc * 32 < (KC / 8) * (N / 4)) wpc *= 2;
+  }
   Tc2Args args{X->f.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, vt, op->tc_aoff.p,
                tiles ? tiles : op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xsub, sub_begin,
-               sub_n};
+               sub_n, wpc};
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
   k_cell_apply_tc2<<<grid, THREADS2, smem, ctx->stream>>>(args);
@@ -662,6 +766,12 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
         for (int r = 0; r < 3; ++r) launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st);
         GBFE_CUDA(cudaEventRecord(e1, ctx->stream));
         GBFE_CUDA(cudaEventSynchronize(e1));
+        int st_word = 0;
+        GBFE_CUDA(cudaMemcpy(&st_word, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (st_word)
+          throw Error(GBFE_ERR_TIMEOUT, "autotune: a bounded wait gave up (code " + std::to_string(st_word) +
+                                            ") at vector tile " + std::to_string(N) + ", " + std::to_string(st) +
+                                            " stages");
         float ms = 0.f;
         GBFE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         ms /= 3.f;

@@ -17,6 +17,7 @@ constexpr uint32_t CORE_BYTES = 128;             // one 8 x 16-byte core matrix
 constexpr uint32_t SBO = (KC / 8) * CORE_BYTES;  // stride between 8-row groups
 constexpr uint32_t LBO = CORE_BYTES;             // stride between K-adjacent core matrices
 constexpr uint32_t WAIT_LIMIT = 1u << 24;        // bounded mbarrier polls
+constexpr uint64_t WAIT_NS = 2000000000ull;      // and at most 2 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -41,9 +42,18 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
-// bounded wait on the given phase parity; false (and an error code) on timeout
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// bounded wait on the given phase parity (WAIT_LIMIT polls and WAIT_NS of
+// wall time, whichever ends first); false on timeout, and then, when status is
+// given, the error code goes into the device status word
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code) {
   const uint32_t a = smem_u32(bar);
+  uint64_t t0 = 0;
   for (uint32_t it = 0; it < WAIT_LIMIT; ++it) {
     uint32_t ok;
     asm volatile(
@@ -52,8 +62,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *s
         : "r"(a), "r"(parity)
         : "memory");
     if (ok) return true;
+    if ((it & 255u) == 255u) {
+      const uint64_t t = globaltimer_ns();
+      if (!t0)
+        t0 = t;
+      else if (t - t0 > WAIT_NS)
+        break;
+    }
   }
-  atomicCAS(status, 0, code);
+  if (status) atomicCAS(status, 0, code);
   return false;
 }
 
@@ -77,6 +94,21 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
                : "memory");
 }
 
+// After a timed-out wait the CTA leaves its loops early; before it frees TMEM
+// and exits, the asynchronous work its threads issued must have landed.
+//   drain_copies: the bulk copies of the last min(q, S) ring chunks issued
+//     (chunk j signals full[j % S], phase parity (j / S) & 1);
+//   drain_mmas: every tcgen05.mma this thread issued (a commit to a spare
+//     barrier that nothing else arrives on, used once).
+// Both waits are bounded and leave the status word alone.
+__device__ __forceinline__ void drain_copies(uint64_t *full, uint32_t q, uint32_t S) {
+  for (uint32_t j = q > S ? q - S : 0; j < q; ++j) mbar_wait(&full[j % S], (j / S) & 1, nullptr, 0);
+}
+__device__ __forceinline__ void drain_mmas(uint64_t *spare) {
+  umma_commit(spare);
+  mbar_wait(spare, 0, nullptr, 0);
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   uint32_t r[16];
   asm volatile(
@@ -87,6 +119,24 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// tcgen05.ld of 16 columns without the wait: tmem_wait_ld16 completes it.
+// The destination registers are in/out operands of the wait, so no read of
+// them is placed above it.
+__device__ __forceinline__ void tmem_ld16_issue(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld16(uint32_t (&r)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
 }
 
 __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {

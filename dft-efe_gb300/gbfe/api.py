@@ -69,7 +69,8 @@ class LinAlgOpContext:
         check(self.lib.gbfe_ctx_check_status(self.h), self.h, "device status")
 
     def set_tensor_cores(self, mode: int) -> None:
-        """2: persistent tcgen05 kernel (default), 1: one-CTA-per-cell tcgen05, 0: FP32 SIMT."""
+        """2: persistent tcgen05 kernel (default), 3: the same with scalar gathers,
+        1: one-CTA-per-cell tcgen05, 0: FP32 SIMT."""
         check(self.lib.gbfe_ctx_set_tensor_cores(self.h, int(mode)), self.h, "set_tensor_cores")
 
     def set_graphs(self, on: bool) -> None:

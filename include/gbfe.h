@@ -73,9 +73,10 @@ int gbfe_ctx_synchronize(gbfe_ctx *ctx);
  * when one of their bounded waits gives up: GBFE_OK or GBFE_ERR_TIMEOUT. */
 int gbfe_ctx_check_status(gbfe_ctx *ctx);
 /* Cell product of the FP32 apply: 2 (default) the persistent warp-specialised
- * split-BF16 tcgen05 kernel; 1 the one-CTA-per-cell tcgen05 kernel; 0 the FP32
- * SIMT kernel.  The environment variable GBFE_TENSOR_CORES=0|1 sets the
- * initial mode of a new context. */
+ * split-BF16 tcgen05 kernel (16-byte row gathers when m % 4 == 0); 3 the same
+ * kernel with one 4-byte element per gather load; 1 the one-CTA-per-cell
+ * tcgen05 kernel; 0 the FP32 SIMT kernel.  The environment variable
+ * GBFE_TENSOR_CORES=0|1 sets the initial mode of a new context. */
 int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode);
 /* ---- nonlocal pseudopotential part ---------------------------------------
  * Replaces basis::AtomCenterNonLocalOpContextFE

@@ -109,16 +109,21 @@ def test_gpu_enriched_fused_filter_matches_separate(gpu_ctx, enriched):
                          s.diag_block_op(1.0 / p.m_gll_diag, p.extra["enr_begin"], p.extra["enr_block_inv"]))
     wl, wu, uu = b[0], b[0] + 0.1 * (b[1] - b[0]), b[1] + b[2] / 10
     outs = {}
-    for fused in (True, False):
+    for fused, tc in ((True, 2), (False, 2), (True, 3)):
         gpu_ctx.set_fused_filter(fused)
+        gpu_ctx.set_tensor_cores(tc)
         try:
             X = api.MultiVector(basis, 12, init=X0)
             Y = api.MultiVector(basis, 12)
             api.ResidualChebyshevFilterGEP(H, Mo, Mi, eig0, X, 9, wl, wu, uu, Y, mixed=True)
             gpu_ctx.check_status()
-            outs[fused] = Y.numpy()
+            outs[fused, tc] = Y.numpy()
         finally:
             gpu_ctx.set_fused_filter(True)
-    err = rel_maxnorm(outs[True], outs[False])
-    print(f"enriched fused filter vs separate: {err:.2e}, bitwise {np.array_equal(outs[True], outs[False])}")
+            gpu_ctx.set_tensor_cores(2)
+    err = rel_maxnorm(outs[True, 2], outs[False, 2])
+    print(f"enriched fused filter vs separate: {err:.2e}, bitwise {np.array_equal(outs[True, 2], outs[False, 2])}")
     assert err <= 1e-3
+    # the 16-byte and the 4-byte gathers (enrichment rows substituted in both)
+    # hand the same operands to the same MMAs
+    assert np.array_equal(outs[True, 2], outs[True, 3])

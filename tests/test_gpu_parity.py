@@ -253,7 +253,7 @@ def test_mixed_apply_fp32_simt(gpu_ctx, small_problem):
 TC_TOL = 1e-4  # split-BF16 (3 products, FP32 accumulation): ~2^-18 per operand
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 @pytest.mark.parametrize("n,p,m", [(3, 3, 32), (3, 4, 64), (2, 5, 40), (2, 4, 300), (2, 3, 7), (5, 4, 24)])
 def test_mixed_apply_tensor_cores(gpu_ctx, n, p, m, mode):
     """tcgen05 split-BF16 cell product against the FP64 apply of the same X
@@ -282,8 +282,9 @@ def test_mixed_apply_tensor_cores(gpu_ctx, n, p, m, mode):
 
 
 def test_tensor_core_kernels_agree_bitwise(gpu_ctx):
-    """The persistent kernel and the one-CTA-per-cell kernel issue the same
-    MMAs in the same order per cell, so their results are identical."""
+    """The persistent kernel (16-byte and 4-byte gathers) and the
+    one-CTA-per-cell kernel issue the same MMAs on the same operands in the
+    same order per cell, so their results are identical."""
     from gbfe import api
 
     prob = M.ks_box(4, 4, 8.0, 1, 4.0, 0.5, seed=44)
@@ -291,7 +292,7 @@ def test_tensor_core_kernels_agree_bitwise(gpu_ctx):
     H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=True)
     X0 = M.random_block(prob.n_dofs, 48, 5).astype(np.float32)
     outs = []
-    for mode in (1, 2, 2):
+    for mode in (1, 2, 2, 3):
         Xf = api.MultiVector(basis, 48, dtype=np.float32, init=X0)
         Yf = api.MultiVector(basis, 48, dtype=np.float32)
         gpu_ctx.set_tensor_cores(mode)
@@ -299,7 +300,7 @@ def test_tensor_core_kernels_agree_bitwise(gpu_ctx):
         gpu_ctx.check_status()
         outs.append(Yf.numpy())
     gpu_ctx.set_tensor_cores(2)
-    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
 
 
 def test_mixed_apply_tensor_cores_variable_nd(gpu_ctx):
