@@ -156,15 +156,16 @@ __global__ void k_fold_scale(const double *__restrict__ d, const uint8_t *__rest
 // RN read as zero and are zeroed in place: the parent-to-child step that the
 // separate B^-1 apply runs on its input (the cell product never sees those
 // rows: their factor in the folded tiles is zero).
+template <bool SH>
 __global__ void k_assemble_cheb(const float *__restrict__ Yc, uint32_t m, uint64_t n_dofs,
                                 const uint32_t *__restrict__ slot_ptr, const uint32_t *__restrict__ slot,
                                 const uint8_t *__restrict__ is_row, const double *__restrict__ coef,
                                 float *__restrict__ RN, float *__restrict__ R, const double *__restrict__ eF2,
-                                const float *__restrict__ Y, const FastDiv fm, bool sh) {
+                                const float *__restrict__ Y, const FastDiv fm) {
   extern __shared__ __align__(16) unsigned char col_sh[];
   float *g = reinterpret_cast<float *>(col_sh);
   const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
-  if (sh) {
+  if (SH) {
     load_col_factors(g, m, alpha1, eF2);
     __syncthreads();
   }
@@ -181,7 +182,7 @@ __global__ void k_assemble_cheb(const float *__restrict__ Yc, uint32_t m, uint64
       for (uint32_t p = slot_ptr[i], e = slot_ptr[i + 1]; p < e; ++p) acc = acc + Yc[(uint64_t)slot[p] * m + v];
     const float s1 = a1 * acc + b1 * (crow ? 0.f : RN[t]);
     const float r = s1 + a2 * R[t];
-    R[t] = r + (sh ? g[v] : (float)(alpha1 * eF2[v])) * Y[t];
+    R[t] = r + (SH ? g[v] : (float)(alpha1 * eF2[v])) * Y[t];
     if (crow) RN[t] = 0.f;
   }
 }
@@ -224,15 +225,16 @@ __global__ void k_assemble_vec(const T *__restrict__ Yc, uint32_t m, uint64_t n_
 // k_assemble_cheb on float4 groups of vectors (m % 4 == 0): the same
 // per-component arithmetic in the same order, a quarter of the load
 // instructions and 16-byte transactions
+template <bool SH>
 __global__ void k_assemble_cheb4(const float *__restrict__ Yc, uint32_t m, uint64_t n_dofs,
                                  const uint32_t *__restrict__ slot_ptr, const uint32_t *__restrict__ slot,
                                  const uint8_t *__restrict__ is_row, const double *__restrict__ coef,
                                  float *__restrict__ RN, float *__restrict__ R, const double *__restrict__ eF2,
-                                 const float *__restrict__ Y, const FastDiv fq, bool sh) {
+                                 const float *__restrict__ Y, const FastDiv fq) {
   extern __shared__ __align__(16) unsigned char col_sh[];
   float *g = reinterpret_cast<float *>(col_sh);
   const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
-  if (sh) {
+  if (SH) {
     load_col_factors(g, m, alpha1, eF2);
     __syncthreads();
   }
@@ -259,7 +261,7 @@ __global__ void k_assemble_cheb4(const float *__restrict__ Yc, uint32_t m, uint6
     const float4 rn = crow ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(RN + o);
     const float4 r0 = *reinterpret_cast<const float4 *>(R + o);
     const float4 yy = *reinterpret_cast<const float4 *>(Y + o);
-    const float4 gg = sh ? *reinterpret_cast<const float4 *>(g + v)
+    const float4 gg = SH ? *reinterpret_cast<const float4 *>(g + v)
                          : make_float4((float)(alpha1 * eF2[v]), (float)(alpha1 * eF2[v + 1]),
                                        (float)(alpha1 * eF2[v + 2]), (float)(alpha1 * eF2[v + 3]));
     float4 out;
@@ -270,6 +272,39 @@ __global__ void k_assemble_cheb4(const float *__restrict__ Yc, uint32_t m, uint6
     *reinterpret_cast<float4 *>(R + o) = out;
     if (crow) *reinterpret_cast<float4 *>(RN + o) = make_float4(0.f, 0.f, 0.f, 0.f);
   }
+}
+
+// Rows of a dense block times rows of X: out[r][v] = sum_j blk(r, j) X[bb + j][v]
+// for r < nb (blk column-major nb x nb; out rows m apart), the j-sum in order
+// with fused multiply-adds.  One launch for the small enrichment blocks
+// (OrthoEFEOverlapInverseOpContextGLL's dense part) instead of a library GEMM
+// that splits the K dimension over two launches.
+constexpr uint32_t BLOCK_ROWS_MAX = 512;
+template <class T>
+__global__ void k_block_rows(const T *__restrict__ X, uint32_t m, uint64_t bb, uint32_t nb,
+                             const T *__restrict__ blk, T *__restrict__ out) {
+  const uint32_t r = blockIdx.x, v = blockIdx.y * blockDim.x + threadIdx.x;
+  if (r >= nb || v >= m) return;
+  T acc = (T)0;
+  for (uint32_t j = 0; j < nb; ++j) acc = fma(blk[r + (uint64_t)j * nb], X[(bb + j) * m + v], acc);
+  out[(uint64_t)r * m + v] = acc;
+}
+
+template <class T>
+void block_rows(gbfe_ctx *ctx, const T *X, uint32_t m, uint64_t bb, uint32_t nb, const T *blk, T *out) {
+  if (nb <= BLOCK_ROWS_MAX) {
+    k_block_rows<T><<<dim3(nb, (m + 127) / 128), 128, 0, ctx->stream>>>(X, m, bb, nb, blk, out);
+    check_launch(ctx, "block_rows");
+    return;
+  }
+  const T one = (T)1, zero = (T)0;
+  if constexpr (sizeof(T) == 8)
+    GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)m, (int)nb, (int)nb, &one, X + bb * m, (int)m,
+                            blk, (int)nb, &zero, out, (int)m));
+  else
+    GBFE_CUBLAS(cublasSgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)m, (int)nb, (int)nb, &one, X + bb * m, (int)m,
+                            blk, (int)nb, &zero, out, (int)m));
+  count_launch(ctx);
 }
 
 // Diagonal operator with the constraint epilogue fused in.
@@ -438,17 +473,11 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
       k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->f.p, m, me->n_dofs, op->diag.p, nullptr,
                                                                         nullptr, nullptr, nullptr, Y->f.p, FastDiv(m));
     check_launch(ctx, "diag_apply");
-    const int nb = (int)op->blk_n, mm = (int)m;
-    if (X->dtype == GBFE_F64) {
-      const double one = 1.0, zero = 0.0;
-      GBFE_CUBLAS(cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, mm, nb, nb, &one, X->d.p + op->blk_begin * m, mm,
-                              op->blk.p, nb, &zero, Y->d.p + op->blk_begin * m, mm));
-    } else {
-      const float one = 1.f, zero = 0.f;
-      GBFE_CUBLAS(cublasSgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, mm, nb, nb, &one, X->f.p + op->blk_begin * m, mm,
-                              op->blk_f32.p, nb, &zero, Y->f.p + op->blk_begin * m, mm));
-    }
-    count_launch(ctx);
+    if (X->dtype == GBFE_F64)
+      block_rows<double>(ctx, X->d.p, m, op->blk_begin, (uint32_t)op->blk_n, op->blk.p, Y->d.p + op->blk_begin * m);
+    else
+      block_rows<float>(ctx, X->f.p, m, op->blk_begin, (uint32_t)op->blk_n, op->blk_f32.p,
+                        Y->f.p + op->blk_begin * m);
     constraints_c2p(ctx, c, Y);
     return;
   }
@@ -561,13 +590,10 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
   const float *xsub = nullptr;
   if (BInv->kind == OP_DIAG_BLOCK) {
     // the enrichment rows of B^-1 RN: the dense block times those rows of RN,
-    // the same cuBLAS call as the separate B^-1 apply
-    const int nb = (int)BInv->blk_n, mm = (int)m;
+    // the same product as the separate B^-1 apply
     BInv->blk_out_f32.ensure((size_t)BInv->blk_n * m);
-    const float one = 1.f, zero = 0.f;
-    GBFE_CUBLAS(cublasSgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, mm, nb, nb, &one, RN->f.p + BInv->blk_begin * m,
-                            mm, BInv->blk_f32.p, nb, &zero, BInv->blk_out_f32.p, mm));
-    count_launch(ctx);
+    block_rows<float>(ctx, RN->f.p, m, BInv->blk_begin, (uint32_t)BInv->blk_n, BInv->blk_f32.p,
+                      BInv->blk_out_f32.p);
     xsub = BInv->blk_out_f32.p;
   }
   if (A->folded_for != BInv->serial) {
@@ -582,14 +608,15 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
   {
     ProfScope prof_k(ctx, "k:assemble_cheb", 0.0, 0.0);
     const size_t sh = col_factor_smem<float>(m);
+    const uint8_t *isr = c ? c->is_row.p : nullptr;
     if (m % 4 == 0)
-      k_assemble_cheb4<<<stride_grid(ctx, n / 4), 256, sh, ctx->stream>>>(
-          A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p, me->slot.p, c ? c->is_row.p : nullptr, coef, RN->f.p,
-          R->f.p, eF2, Y->f.p, FastDiv(m / 4), sh > 0);
+      (sh ? k_assemble_cheb4<true> : k_assemble_cheb4<false>)<<<stride_grid(ctx, n / 4), 256, sh, ctx->stream>>>(
+          A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr, coef, RN->f.p, R->f.p, eF2, Y->f.p,
+          FastDiv(m / 4));
     else
-      k_assemble_cheb<<<stride_grid(ctx, n), 256, sh, ctx->stream>>>(A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p,
-                                                                    me->slot.p, c ? c->is_row.p : nullptr, coef,
-                                                                    RN->f.p, R->f.p, eF2, Y->f.p, FastDiv(m), sh > 0);
+      (sh ? k_assemble_cheb<true> : k_assemble_cheb<false>)<<<stride_grid(ctx, n), 256, sh, ctx->stream>>>(
+          A->cellbuf_f32.p, m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr, coef, RN->f.p, R->f.p, eF2, Y->f.p,
+          FastDiv(m));
     check_launch(ctx, "assemble_cheb");
   }
   return true;

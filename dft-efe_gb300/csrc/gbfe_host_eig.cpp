@@ -17,6 +17,7 @@
 // Pure C++ (no intrinsics): identical code on x86 and Arm hosts.
 #include <algorithm>
 #include <cmath>
+#include <utility>
 #include <cstdint>
 #include <numeric>
 #include <vector>
@@ -162,6 +163,76 @@ int host_sym_eig(int n, double *a, double *w) {
     for (int i = 0; i < n; ++i) a[(size_t)i + N * j] = A(Z, i, ord[j]);
   }
   return 0;
+}
+
+// Cholesky factor of the symmetric positive definite a (n x n column-major,
+// lower triangle read), in place: a = L with L L^T = A, upper triangle zeroed.
+// Returns 0, or k + 1 when the leading minor of order k + 1 is not positive
+// definite (LAPACK potrf's info).  Column-oriented (left-looking) elimination:
+// every inner loop runs down a contiguous column.
+int host_cholesky(int n, double *a) {
+  const size_t N = (size_t)n;
+  for (int k = 0; k < n; ++k) {
+    double *ck = a + N * k;
+    // column k -= sum_{j<k} L(k, j) L(k:n, j)
+    for (int j = 0; j < k; ++j) {
+      const double *cj = a + N * j;
+      const double lkj = cj[k];
+      if (lkj == 0.0) continue;
+      for (int i = k; i < n; ++i) ck[i] -= lkj * cj[i];
+    }
+    const double d = ck[k];
+    if (!(d > 0.0)) return k + 1;
+    const double r = std::sqrt(d);
+    ck[k] = r;
+    const double inv = 1.0 / r;
+    for (int i = k + 1; i < n; ++i) ck[i] *= inv;
+    for (int i = 0; i < k; ++i) ck[i] = 0.0;
+  }
+  return 0;
+}
+
+// B <- L^-1 B for lower triangular L (both n x n column-major): forward
+// substitution on every column of B, column-oriented
+void host_trsm_lower(int n, const double *L, double *B) {
+  const size_t N = (size_t)n;
+  for (int j = 0; j < n; ++j) {
+    double *b = B + N * j;
+    for (int k = 0; k < n; ++k) {
+      const double *lk = L + N * k;
+      const double x = b[k] / lk[k];
+      b[k] = x;
+      if (x == 0.0) continue;
+      for (int i = k + 1; i < n; ++i) b[i] -= lk[i] * x;
+    }
+  }
+}
+
+// B <- L^-T B for lower triangular L: back substitution with the rows of L^T
+// (the columns of L), every dot product down a contiguous column
+void host_trsm_lower_t(int n, const double *L, double *B) {
+  const size_t N = (size_t)n;
+  for (int j = 0; j < n; ++j) {
+    double *b = B + N * j;
+    for (int k = n - 1; k >= 0; --k) {
+      const double *lk = L + N * k;
+      double s = b[k];
+      for (int i = k + 1; i < n; ++i) s -= lk[i] * b[i];
+      b[k] = s / lk[k];
+    }
+  }
+}
+
+// A <- L^-1 A L^-T for symmetric A (full storage): W = L^-1 A, then
+// L^-1 W^T = L^-1 A L^-T (A = A^T), symmetrised from its lower triangle
+void host_sandwich(int n, const double *L, double *A) {
+  const size_t N = (size_t)n;
+  host_trsm_lower(n, L, A);
+  for (int j = 0; j < n; ++j)
+    for (int i = j + 1; i < n; ++i) std::swap(A[i + N * j], A[j + N * i]);
+  host_trsm_lower(n, L, A);
+  for (int j = 0; j < n; ++j)
+    for (int i = j + 1; i < n; ++i) A[j + N * i] = A[i + N * j];
 }
 
 }  // namespace gbfe

@@ -322,7 +322,9 @@ struct FastDiv {
 // per element: GB300's FP64 pipe retires about two operations per SM clock,
 // too few for a DMUL and a conversion per element of an FP32 sweep.
 // col_factor_smem = the dynamic shared bytes of k factor arrays (0: the block
-// width is too large, the kernel computes the factors per element).
+// width is too large, the kernel computes the factors per element).  The
+// kernels take the choice as a template flag: with a runtime flag the
+// compiler predicates the per-element FP64 branch into every iteration.
 template <class T>
 inline size_t col_factor_smem(uint32_t m, int k = 1) {
   const size_t b = (size_t)k * m * sizeof(T);
@@ -428,6 +430,10 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log);
 bool oz_supported(const gbfe_mesh *me);
 // dense symmetric eigen-decomposition on the host (gbfe_host_eig.cpp)
 int host_sym_eig(int n, double *a, double *w);
+int host_cholesky(int n, double *a);
+void host_trsm_lower(int n, const double *L, double *B);
+void host_trsm_lower_t(int n, const double *L, double *B);
+void host_sandwich(int n, const double *L, double *A);
 // FP64-accurate sliced tensor-core products of the subspace stages (gbfe_ozgemm.cu)
 bool oz_gemm_supported(gbfe_ctx *ctx, uint32_t m);
 void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, const double *B, uint32_t mb,

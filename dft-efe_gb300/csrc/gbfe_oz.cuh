@@ -89,6 +89,45 @@ __device__ __forceinline__ void digits_pair_bf16(double v0, double v1, int e, ui
                             0x7632);
 }
 
+// Stage 1 of the per-column exponent scan of up to two stacked N x m row-major
+// blocks (column c < m of A0, else column c - m of A1): the block of this CTA's
+// rows, max of the exponent bits per column into part[blockIdx.x][na m].
+// Threads are (row lane, column) with consecutive threads on consecutive
+// columns, so every pass reads whole rows; four rows per lane are loaded
+// before they are reduced.  max is order-free: any split gives the same bits.
+constexpr int COLMAX_THREADS = 256;
+__device__ __forceinline__ void colmax_partial_block(const double *__restrict__ A0, const double *__restrict__ A1,
+                                                     uint32_t na, uint32_t m, uint64_t N, int *__restrict__ part) {
+  __shared__ int red[COLMAX_THREADS];
+  const uint32_t cols = na * m;
+  const uint64_t per = (N + gridDim.x - 1) / gridDim.x;
+  const uint64_t r0 = blockIdx.x * per, r1 = min(N, r0 + per);
+  const uint32_t tcols = min(cols, (uint32_t)COLMAX_THREADS), rpb = COLMAX_THREADS / tcols;
+  const uint32_t rl = threadIdx.x / tcols, cl = threadIdx.x % tcols;
+  for (uint32_t cb = 0; cb < cols; cb += tcols) {
+    const uint32_t c = cb + cl;
+    int mx = EXP_NONE;
+    if (rl < rpb && c < cols) {
+      const double *A = c < m ? A0 : A1;
+      const uint32_t j = c < m ? c : c - m;
+      uint64_t i = r0 + rl;
+      for (; i + 3 * (uint64_t)rpb < r1; i += 4 * (uint64_t)rpb) {
+        const double x0 = A[i * m + j], x1 = A[(i + rpb) * m + j], x2 = A[(i + 2 * rpb) * m + j],
+                     x3 = A[(i + 3 * rpb) * m + j];
+        mx = max(max(mx, max(exp_bits(x0), exp_bits(x1))), max(exp_bits(x2), exp_bits(x3)));
+      }
+      for (; i < r1; i += rpb) mx = max(mx, exp_bits(A[i * m + j]));
+    }
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    if (rl == 0 && c < cols) {
+      for (uint32_t q = 1; q < rpb; ++q) mx = max(mx, red[q * tcols + cl]);
+      part[(uint64_t)blockIdx.x * cols + c] = mx;
+    }
+    __syncthreads();
+  }
+}
+
 // out-of-line, so that the rare call is a branch and not FP64 work that the
 // compiler predicates into every lane
 static __device__ __noinline__ double ldexp_outlined(double v, int k) { return ldexp(v, k); }

@@ -88,13 +88,7 @@ __global__ void k_build_oz_mats(const double *__restrict__ mats, const uint64_t 
 // per-vector exponent of the largest |X[i][v]| (two-stage max of the exponent
 // bits, integer instructions; max is order-free)
 __global__ void k_colmax_partial(const double *__restrict__ X, uint64_t rows, uint32_t m, int *__restrict__ part) {
-  const uint64_t per = (rows + gridDim.x - 1) / gridDim.x;
-  const uint64_t r0 = blockIdx.x * per, r1 = min(rows, r0 + per);
-  for (uint32_t v = threadIdx.x; v < m; v += blockDim.x) {
-    int mx = oz::EXP_NONE;
-    for (uint64_t i = r0; i < r1; ++i) mx = max(mx, oz::exp_bits(X[i * m + v]));
-    part[(uint64_t)blockIdx.x * m + v] = mx;
-  }
+  oz::colmax_partial_block(X, X, 1, m, rows, part);
 }
 
 __global__ void k_colmax_final(const int *__restrict__ part, uint32_t nb, uint32_t m, int *__restrict__ ex) {
@@ -374,10 +368,10 @@ void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc) {
   gbfe_ctx *ctx = me->ctx;
   const uint32_t m = X->m;
   const uint64_t rows = me->n_dofs;
-  const unsigned nb = (unsigned)std::min<uint64_t>(304, std::max<uint64_t>(1, rows));
+  const unsigned nb = (unsigned)std::min<uint64_t>(8 * (uint64_t)ctx->sm_count, std::max<uint64_t>(1, rows));
   ctx->oz_ipart.ensure((size_t)nb * m);
   op->oz_xexp.ensure(m);
-  k_colmax_partial<<<nb, 128, 0, ctx->stream>>>(X->d.p, rows, m, ctx->oz_ipart.p);
+  k_colmax_partial<<<nb, oz::COLMAX_THREADS, 0, ctx->stream>>>(X->d.p, rows, m, ctx->oz_ipart.p);
   k_colmax_final<<<(m + 127) / 128, 128, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, m, op->oz_xexp.p);
   count_launch(ctx, 2);
   const uint32_t vt = (m + OZ_N - 1) / OZ_N;

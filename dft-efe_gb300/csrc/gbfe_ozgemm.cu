@@ -482,15 +482,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
 // the exponent bits (integer instructions: the FP64 pipe is the slow one)
 __global__ void k_oz_colmax_partial(const double *__restrict__ A0, const double *__restrict__ A1, uint32_t na,
                                     uint32_t m, uint64_t N, int *__restrict__ part) {
-  const uint64_t per = (N + gridDim.x - 1) / gridDim.x;
-  const uint64_t r0 = blockIdx.x * per, r1 = min(N, r0 + per);
-  for (uint32_t c = threadIdx.x; c < na * m; c += blockDim.x) {
-    const double *A = c < m ? A0 : A1;
-    const uint32_t j = c % m;
-    int mx = oz::EXP_NONE;
-    for (uint64_t i = r0; i < r1; ++i) mx = max(mx, oz::exp_bits(A[i * m + j]));
-    part[(uint64_t)blockIdx.x * na * m + c] = mx;
-  }
+  oz::colmax_partial_block(A0, A1, na, m, N, part);
 }
 
 __global__ void k_oz_colmax_final(const int *__restrict__ part, uint32_t nb, uint32_t cols, int *__restrict__ ex) {
@@ -578,12 +570,13 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
   const uint32_t splits = (chunks + cps - 1) / cps;
   const uint32_t items = tiles * splits;
   // exponents
-  const unsigned nb = (unsigned)std::min<uint64_t>(304, std::max<uint64_t>(1, N));
+  const unsigned nb = (unsigned)std::min<uint64_t>(8 * (uint64_t)ctx->sm_count, std::max<uint64_t>(1, N));
   ctx->oz_exp.ensure((size_t)rows + mb);
   ctx->oz_ipart.ensure((size_t)nb * std::max(rows, mb));
-  k_oz_colmax_partial<<<nb, 256, 0, ctx->stream>>>(A[0], na > 1 ? A[1] : A[0], na, ma, N, ctx->oz_ipart.p);
+  k_oz_colmax_partial<<<nb, oz::COLMAX_THREADS, 0, ctx->stream>>>(A[0], na > 1 ? A[1] : A[0], na, ma, N,
+                                                                  ctx->oz_ipart.p);
   k_oz_colmax_final<<<(rows + 255) / 256, 256, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, rows, ctx->oz_exp.p);
-  k_oz_colmax_partial<<<nb, 256, 0, ctx->stream>>>(B, B, 1, mb, N, ctx->oz_ipart.p);
+  k_oz_colmax_partial<<<nb, oz::COLMAX_THREADS, 0, ctx->stream>>>(B, B, 1, mb, N, ctx->oz_ipart.p);
   k_oz_colmax_final<<<(mb + 255) / 256, 256, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, mb, ctx->oz_exp.p + rows);
   count_launch(ctx, 4);
   ctx->oz_part.ensure((size_t)items * TILE);

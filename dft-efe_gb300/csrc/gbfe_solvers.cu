@@ -32,13 +32,13 @@ __global__ void k_axpby(uint64_t n, double a, const T *__restrict__ x, double b,
 }
 
 // z[i][j] = a1*alpha[j]*x[i][j] + b1*beta[j]*y[i][j] (blasLapack::axpbyBlocked)
-template <class T>
+template <class T, bool SH>
 __global__ void k_axpby_blocked(uint64_t rows, uint32_t m, double a1, const double *__restrict__ alpha,
                                 const T *__restrict__ x, double b1, const double *__restrict__ beta,
-                                const T *__restrict__ y, T *__restrict__ z, const FastDiv fm, bool sh) {
+                                const T *__restrict__ y, T *__restrict__ z, const FastDiv fm) {
   extern __shared__ __align__(16) unsigned char col_sh[];
   T *fa = reinterpret_cast<T *>(col_sh), *fb = fa + m;
-  if (sh) {
+  if (SH) {
     load_col_factors(fa, m, a1, alpha);
     load_col_factors(fb, m, b1, beta);
     __syncthreads();
@@ -48,19 +48,19 @@ __global__ void k_axpby_blocked(uint64_t rows, uint32_t m, double a1, const doub
     uint64_t i;
     uint32_t j;
     fm.divmod(t, i, j);
-    z[t] = (sh ? fa[j] : (T)(a1 * alpha[j])) * x[t] + (sh ? fb[j] : (T)(b1 * beta[j])) * y[t];
+    z[t] = (SH ? fa[j] : (T)(a1 * alpha[j])) * x[t] + (SH ? fb[j] : (T)(b1 * beta[j])) * y[t];
   }
 }
 
 // R = alpha1*AS + (-c*alpha1)*RN + alpha2*R + alpha1*eF2[j]*Y, one sweep
 // (the axpby, axpby and axpbyBlocked of ChebyshevFilter.t.cpp:375-409 fused)
-template <class T>
+template <class T, bool SH>
 __global__ void k_cheb_step(uint64_t n, uint32_t m, double alpha1, double c, double alpha2,
                             const T *__restrict__ AS, const T *__restrict__ RN, T *__restrict__ R,
-                            const double *__restrict__ eF2, const T *__restrict__ Y, const FastDiv fm, bool sh) {
+                            const double *__restrict__ eF2, const T *__restrict__ Y, const FastDiv fm) {
   extern __shared__ __align__(16) unsigned char col_sh[];
   T *g = reinterpret_cast<T *>(col_sh);
-  if (sh) {
+  if (SH) {
     load_col_factors(g, m, alpha1, eF2);
     __syncthreads();
   }
@@ -71,20 +71,20 @@ __global__ void k_cheb_step(uint64_t n, uint32_t m, double alpha1, double c, dou
     fm.divmod(t, i, j);
     T s1 = a1 * AS[t] + b1 * RN[t];
     T r = s1 + a2 * R[t];
-    R[t] = r + (sh ? g[j] : (T)(alpha1 * eF2[j])) * Y[t];
+    R[t] = r + (SH ? g[j] : (T)(alpha1 * eF2[j])) * Y[t];
   }
 }
 
 // the same step with its scalars read from a device table {alpha1, c, alpha2},
 // so one captured graph serves every pass
-template <class T>
+template <class T, bool SH>
 __global__ void k_cheb_step_dev(uint64_t n, uint32_t m, const double *__restrict__ coef, const T *__restrict__ AS,
                                 const T *__restrict__ RN, T *__restrict__ R, const double *__restrict__ eF2,
-                                const T *__restrict__ Y, const FastDiv fm, bool sh) {
+                                const T *__restrict__ Y, const FastDiv fm) {
   extern __shared__ __align__(16) unsigned char col_sh[];
   T *g = reinterpret_cast<T *>(col_sh);
   const double alpha1 = coef[0], c = coef[1], alpha2 = coef[2];
-  if (sh) {
+  if (SH) {
     load_col_factors(g, m, alpha1, eF2);
     __syncthreads();
   }
@@ -95,7 +95,7 @@ __global__ void k_cheb_step_dev(uint64_t n, uint32_t m, const double *__restrict
     fm.divmod(t, i, j);
     T s1 = a1 * AS[t] + b1 * RN[t];
     T r = s1 + a2 * R[t];
-    R[t] = r + (sh ? g[j] : (T)(alpha1 * eF2[j])) * Y[t];
+    R[t] = r + (SH ? g[j] : (T)(alpha1 * eF2[j])) * Y[t];
   }
 }
 
@@ -196,12 +196,12 @@ void d_axpby_blocked(gbfe_ctx *ctx, double a1, const double *alpha_d, const gbfe
   const uint64_t n = z->count();
   if (z->dtype == GBFE_F64) {
     const size_t sh = col_factor_smem<double>(z->m, 2);
-    k_axpby_blocked<double><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(z->mesh->n_dofs, z->m, a1, alpha_d, x->d.p, b1,
-                                                                      beta_d, y->d.p, z->d.p, FastDiv(z->m), sh > 0);
+    (sh ? k_axpby_blocked<double, true> : k_axpby_blocked<double, false>)<<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
+        z->mesh->n_dofs, z->m, a1, alpha_d, x->d.p, b1, beta_d, y->d.p, z->d.p, FastDiv(z->m));
   } else {
     const size_t sh = col_factor_smem<float>(z->m, 2);
-    k_axpby_blocked<float><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(z->mesh->n_dofs, z->m, a1, alpha_d, x->f.p, b1,
-                                                                     beta_d, y->f.p, z->f.p, FastDiv(z->m), sh > 0);
+    (sh ? k_axpby_blocked<float, true> : k_axpby_blocked<float, false>)<<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
+        z->mesh->n_dofs, z->m, a1, alpha_d, x->f.p, b1, beta_d, y->f.p, z->f.p, FastDiv(z->m));
   }
   check_launch(ctx, "axpby_blocked");
 }
@@ -415,16 +415,16 @@ template <>
 void launch_cheb_step<double>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha1, double c, double alpha2,
                               const gbfe_mv *AS, const gbfe_mv *RN, gbfe_mv *R, const double *eF2, const gbfe_mv *Y) {
   const size_t sh = col_factor_smem<double>(m);
-  k_cheb_step<double><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(n, m, alpha1, c, alpha2, AS->d.p, RN->d.p, R->d.p, eF2,
-                                                               Y->d.p, FastDiv(m), sh > 0);
+  (sh ? k_cheb_step<double, true> : k_cheb_step<double, false>)<<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
+      n, m, alpha1, c, alpha2, AS->d.p, RN->d.p, R->d.p, eF2, Y->d.p, FastDiv(m));
   check_launch(ctx, "cheb_step");
 }
 template <>
 void launch_cheb_step<float>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha1, double c, double alpha2,
                              const gbfe_mv *AS, const gbfe_mv *RN, gbfe_mv *R, const double *eF2, const gbfe_mv *Y) {
   const size_t sh = col_factor_smem<float>(m);
-  k_cheb_step<float><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(n, m, alpha1, c, alpha2, AS->f.p, RN->f.p, R->f.p, eF2,
-                                                              Y->f.p, FastDiv(m), sh > 0);
+  (sh ? k_cheb_step<float, true> : k_cheb_step<float, false>)<<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
+      n, m, alpha1, c, alpha2, AS->f.p, RN->f.p, R->f.p, eF2, Y->f.p, FastDiv(m));
   check_launch(ctx, "cheb_step_f32");
 }
 
@@ -549,12 +549,12 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
       apply_op(A, s1, s2);
       if (mixed) {
         const size_t sh = col_factor_smem<float>(m);
-        k_cheb_step_dev<float><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
-            n, m, w.coef.p + 3 * k, s2->f.p, rn->f.p, r->f.p, w.tab.p + (size_t)k * m, Yr->f.p, FastDiv(m), sh > 0);
+        (sh ? k_cheb_step_dev<float, true> : k_cheb_step_dev<float, false>)<<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
+            n, m, w.coef.p + 3 * k, s2->f.p, rn->f.p, r->f.p, w.tab.p + (size_t)k * m, Yr->f.p, FastDiv(m));
       } else {
         const size_t sh = col_factor_smem<double>(m);
-        k_cheb_step_dev<double><<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
-            n, m, w.coef.p + 3 * k, s2->d.p, rn->d.p, r->d.p, w.tab.p + (size_t)k * m, Yr->d.p, FastDiv(m), sh > 0);
+        (sh ? k_cheb_step_dev<double, true> : k_cheb_step_dev<double, false>)<<<sgrid(ctx, n), 256, sh, ctx->stream>>>(
+            n, m, w.coef.p + 3 * k, s2->d.p, rn->d.p, r->d.p, w.tab.p + (size_t)k * m, Yr->d.p, FastDiv(m));
       }
       check_launch(ctx, "cheb_step");
     }
@@ -771,59 +771,69 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   }
   // potrf, L^-1 S_H L^-T, syevd, L^-T V: the m x m stages, timed as one block
   auto eig_prof = std::make_unique<ProfScope>(ctx, "eig_small_f64", 0.0, 0.0);
-  int lwork = 0;
-  GBFE_CUSOLVER(cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, &lwork));
-  ctx->lwork.ensure(std::max(lwork, 1));
-  ctx->info.ensure(1);
-  GBFE_CUSOLVER(cusolverDnDpotrf(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, ctx->lwork.p, lwork,
-                                 ctx->info.p));
-  count_launch(ctx);
-  const double one = 1.0, zero = 0.0;
-  auto trsm_sandwich = [&] {  // Hp = L^-1 S_H L^-T
+  const bool host_eig = ctx->small_eig_host && m <= SMALL_EIG_HOST_MAX;
+  const char *chol_fail = "Chol GS cannot orthogonalize the given multivector (near-zero diagonal of L)";
+  if (host_eig) {
+    // the whole block on one host core after one download: the FP64 library
+    // kernels for 64 x 64 factors and solves run on one SM's FP64 pipe and
+    // take longer than the host (and each adds a launch)
+    std::vector<double> hL((size_t)m * m), hS((size_t)m * m);
+    GBFE_CUDA(cudaMemcpyAsync(hL.data(), st.SM.p, hL.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    GBFE_CUDA(cudaMemcpyAsync(hS.data(), st.SH.p, hS.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int info = host_cholesky(m, hL.data());
+    if (info != 0) {
+      msg = "LAPACK_ERROR: FAILED_CHOLESKY_FACTORIZATION (potrf info " + std::to_string(info) + ")";
+      return GBFE_ERR_LAPACK;
+    }
+    for (int i = 0; i < m; ++i)
+      if (std::fabs(hL[(size_t)i * m + i]) < 1e-14) {
+        msg = chol_fail;
+        return GBFE_ERR_NOT_ORTHONORMALIZABLE;
+      }
+    host_sandwich(m, hL.data(), hS.data());
+    if (host_sym_eig(m, hS.data(), eig_h) != 0) {
+      msg = "LAPACK_ERROR: FAILED_STANDARD_EIGENPROBLEM (QR iteration did not converge)";
+      return GBFE_ERR_LAPACK;
+    }
+    host_trsm_lower_t(m, hL.data(), hS.data());  // T = L^-T V
+    h2d_staged(ctx, ctx->pin_small, st.SH.p, hS.data(), hS.size() * 8);
+  } else {
+    int lwork = 0;
+    GBFE_CUSOLVER(cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, &lwork));
+    ctx->lwork.ensure(std::max(lwork, 1));
+    ctx->info.ensure(1);
+    GBFE_CUSOLVER(cusolverDnDpotrf(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, ctx->lwork.p, lwork,
+                                   ctx->info.p));
+    count_launch(ctx);
+    int info = 0;
+    std::vector<double> hL((size_t)m * m);
+    GBFE_CUDA(cudaMemcpyAsync(&info, ctx->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GBFE_CUDA(cudaMemcpyAsync(hL.data(), st.SM.p, hL.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (info != 0) {
+      msg = "LAPACK_ERROR: FAILED_CHOLESKY_FACTORIZATION (potrf info " + std::to_string(info) + ")";
+      return GBFE_ERR_LAPACK;
+    }
+    for (int i = 0; i < m; ++i)
+      if (std::fabs(hL[(size_t)i * m + i]) < 1e-14) {
+        msg = chol_fail;
+        return GBFE_ERR_NOT_ORTHONORMALIZABLE;
+      }
+    const double one = 1.0;
+    // Hp = L^-1 S_H L^-T
     GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
                             m, m, &one, st.SM.p, m, st.SH.p, m));
     GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT,
                             m, m, &one, st.SM.p, m, st.SH.p, m));
     count_launch(ctx, 2);
-  };
-  // host eigensolver: the factor checks, the sandwich's download and the
-  // eigensolve share one synchronisation (the sandwich of a failed factor is
-  // computed and discarded); the device eigensolver checks the factor first
-  const bool host_eig = ctx->small_eig_host && m <= SMALL_EIG_HOST_MAX;
-  int info = 0;
-  std::vector<double> hL((size_t)m * m), hS;
-  if (host_eig) {
-    trsm_sandwich();
-    hS.resize((size_t)m * m);
-    GBFE_CUDA(cudaMemcpyAsync(hS.data(), st.SH.p, hS.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
-  }
-  GBFE_CUDA(cudaMemcpyAsync(&info, ctx->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  GBFE_CUDA(cudaMemcpyAsync(hL.data(), st.SM.p, hL.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
-  GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (info != 0) {
-    msg = "LAPACK_ERROR: FAILED_CHOLESKY_FACTORIZATION (potrf info " + std::to_string(info) + ")";
-    return GBFE_ERR_LAPACK;
-  }
-  for (int i = 0; i < m; ++i)
-    if (std::fabs(hL[(size_t)i * m + i]) < 1e-14) {
-      msg = "Chol GS cannot orthogonalize the given multivector (near-zero diagonal of L)";
-      return GBFE_ERR_NOT_ORTHONORMALIZABLE;
-    }
-  if (host_eig) {
-    if (host_sym_eig(m, hS.data(), eig_h) != 0) {
-      msg = "LAPACK_ERROR: FAILED_STANDARD_EIGENPROBLEM (QR iteration did not converge)";
-      return GBFE_ERR_LAPACK;
-    }
-    h2d_staged(ctx, ctx->pin_small, st.SH.p, hS.data(), hS.size() * 8);
-  } else {
-    trsm_sandwich();
     const int rc = small_syevd(ctx, m, st.SH.p, eig_h, msg);
     if (rc != GBFE_OK) return rc;
+    // T = L^-T V (in place in SH)
+    GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT,
+                            m, m, &one, st.SM.p, m, st.SH.p, m));
+    count_launch(ctx);
   }
-  // T = L^-T V (in place in SH)
-  GBFE_CUBLAS(cublasDtrsm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, m,
-                          m, &one, st.SM.p, m, st.SH.p, m));
-  count_launch(ctx);
   eig_prof.reset();
   const double *T = st.SH.p;
   if (oz_dense) {
@@ -832,6 +842,7 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
     oz_rotate(ctx, T, (uint32_t)m, (uint32_t)m, in, out, 3, (uint64_t)N);
   } else {
     ProfScope prof(ctx, "rotate_f64_dgemm", 6.0 * (double)N * m * m, 48.0 * (double)N * m);
+    const double one = 1.0, zero = 0.0;
     // rows times T: col-major (m x N) out = T^T * in
     GBFE_CUBLAS(
         cublasDgemm(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, m, N, m, &one, T, m, st.Y->d.p, m, &zero, X->d.p, m));

@@ -1,7 +1,10 @@
-"""The host symmetric eigen-decomposition used for the small Rayleigh-Ritz
-matrices (csrc/gbfe_host_eig.cpp), compiled on its own and checked against
-numpy.linalg.eigh: eigenvalues within 1e-13 ||A||, residual ||A V - V L|| and
-orthogonality ||V^T V - I|| within 1e-13 (||A|| for the residual)."""
+"""The host dense kernels of the small Rayleigh-Ritz block
+(csrc/gbfe_host_eig.cpp), compiled on their own and checked against numpy:
+the symmetric eigen-decomposition (eigenvalues within 1e-13 ||A||, residual
+||A V - V L|| and orthogonality ||V^T V - I|| within 1e-13, ||A|| for the
+residual), the Cholesky factor (1e-13 relative, LAPACK potrf's info on a
+matrix that is not positive definite) and the solves L^-1 A L^-T and L^-T B
+(1e-12 relative)."""
 import ctypes as C
 import shutil
 import subprocess
@@ -20,12 +23,19 @@ def eig(tmp_path_factory):
     d = tmp_path_factory.mktemp("host_eig")
     wrap = d / "wrap.cpp"
     wrap.write_text(f'#include "{SRC}"\nextern "C" int eig(int n, double *a, double *w) '
-                    '{ return gbfe::host_sym_eig(n, a, w); }\n')
+                    '{ return gbfe::host_sym_eig(n, a, w); }\n'
+                    'extern "C" int chol(int n, double *a) { return gbfe::host_cholesky(n, a); }\n'
+                    'extern "C" void sandwich(int n, const double *L, double *A) { gbfe::host_sandwich(n, L, A); }\n'
+                    'extern "C" void trsm_lt(int n, const double *L, double *B) { gbfe::host_trsm_lower_t(n, L, B); }\n')
     lib = d / "libeig.so"
     subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", str(wrap), "-o", str(lib)], check=True)
     L = C.CDLL(str(lib))
     L.eig.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
     L.eig.restype = C.c_int
+    L.chol.argtypes = [C.c_int, C.c_void_p]
+    L.chol.restype = C.c_int
+    L.sandwich.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+    L.trsm_lt.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
 
     def run(A):
         n = A.shape[0]
@@ -34,6 +44,7 @@ def eig(tmp_path_factory):
         rc = L.eig(n, a.ctypes.data, w.ctypes.data)
         return rc, w, a
 
+    run.lib = L
     return run
 
 
@@ -67,3 +78,32 @@ def test_host_sym_eig_matches_eigh(eig, name, A):
     assert np.abs(w - ref).max() <= 1e-13 * nrm * max(1, n / 10)
     assert np.abs(A @ V - V * w).max() <= 1e-13 * nrm * max(1, n / 10)
     assert np.abs(V.T @ V - np.eye(n)).max() <= 1e-13 * max(1, n / 10)
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 64, 128])
+def test_host_cholesky_and_solves(eig, n):
+    L_ = eig.lib
+    rng = np.random.default_rng(n)
+    G = rng.standard_normal((n, n))
+    A = G @ G.T + n * np.eye(n)
+    Lh = np.asfortranarray(A.copy())
+    assert L_.chol(n, Lh.ctypes.data) == 0
+    Lr = np.linalg.cholesky(A)
+    assert np.abs(Lh - Lr).max() <= 1e-13 * np.abs(Lr).max()
+    H = rng.standard_normal((n, n))
+    H = H + H.T
+    S = np.asfortranarray(H.copy())
+    L_.sandwich(n, Lh.ctypes.data, S.ctypes.data)
+    Li = np.linalg.inv(Lr)
+    Sr = Li @ H @ Li.T
+    assert np.abs(S - Sr).max() <= 1e-12 * np.abs(Sr).max()
+    assert np.array_equal(S, S.T)
+    B = np.asfortranarray(rng.standard_normal((n, n)))
+    Br = np.linalg.solve(Lr.T, B)
+    L_.trsm_lt(n, Lh.ctypes.data, B.ctypes.data)
+    assert np.abs(B - Br).max() <= 1e-12 * np.abs(Br).max()
+
+
+def test_host_cholesky_reports_the_failing_minor(eig):
+    A = np.asfortranarray(np.diag([1.0, 2.0, -1.0, 4.0]))
+    assert eig.lib.chol(4, A.ctypes.data) == 3
