@@ -10,7 +10,7 @@
 //      explicitly by applying the reflectors in reverse order;
 //   2. implicit symmetric QR steps with the Wilkinson shift on the unreduced
 //      trailing block, each a chase of Givens rotations G^T T G applied to the
-//      band of T and accumulated into Z = Q G_1 G_2 ...;
+//      tridiagonal held as two arrays and accumulated into Z = Q G_1 G_2 ...;
 //      an off-diagonal entry is set to zero once it is below
 //      eps (|t_ii| + |t_i+1,i+1|);
 //   3. eigenvalues ascending with their eigenvector columns.
@@ -87,32 +87,21 @@ int host_sym_eig(int n, double *a, double *w) {
     }
   }
 
-  // ---- 2. implicit symmetric QR with Wilkinson shifts
+  // ---- 2. implicit symmetric QR with Wilkinson shifts on the tridiagonal
+  // held as arrays (diagonal d, off-diagonal e): one step on the unreduced
+  // block [lo, hi] chases the bulge with rotations G_k on (k, k+1); with
+  // G^T = [c -s; s c] the rows and columns of T and the columns of Z change as
+  //   e[k-1] <- c e[k-1] - s bulge                 (the bulge is annihilated)
+  //   d[k]   <- c^2 a - 2cs b + s^2 c'   d[k+1] <- s^2 a + 2cs b + c^2 c'
+  //   e[k]   <- cs (a - c') + (c^2 - s^2) b      (a = d[k], b = e[k], c' = d[k+1])
+  //   bulge  <- -s e[k+1],  e[k+1] <- c e[k+1]
+  std::vector<double> d(N), e(N, 0.0);
+  for (int i = 0; i < n; ++i) d[i] = A(T, i, i);
+  for (int i = 0; i + 1 < n; ++i) e[i] = A(T, i + 1, i);
   const double eps = std::ldexp(1.0, -53);
-  auto negligible = [&](int i) {  // t_{i+1,i}
-    return std::fabs(A(T, i + 1, i)) <= eps * (std::fabs(A(T, i, i)) + std::fabs(A(T, i + 1, i + 1)));
-  };
-  auto rotate = [&](int k, double c, double s, int lo, int hi) {
-    // T <- G^T T G on rows / columns k, k+1 (band entries lo..hi only); Z <- Z G
-    const int i0 = std::max(lo, k - 1), i1 = std::min(hi, k + 2);
-    for (int j = i0; j <= i1; ++j) {
-      const double x = A(T, k, j), y = A(T, k + 1, j);
-      A(T, k, j) = c * x - s * y;
-      A(T, k + 1, j) = s * x + c * y;
-    }
-    for (int i = i0; i <= i1; ++i) {
-      const double x = A(T, i, k), y = A(T, i, k + 1);
-      A(T, i, k) = c * x - s * y;
-      A(T, i, k + 1) = s * x + c * y;
-    }
-    for (int i = 0; i < n; ++i) {
-      const double x = A(Z, i, k), y = A(Z, i, k + 1);
-      A(Z, i, k) = c * x - s * y;
-      A(Z, i, k + 1) = s * x + c * y;
-    }
-  };
+  auto negligible = [&](int i) { return std::fabs(e[i]) <= eps * (std::fabs(d[i]) + std::fabs(d[i + 1])); };
   auto givens = [](double x, double z, double &c, double &s) {
-    // [c s; -s c]^T [x; z] = [r; 0]
+    // [c -s; s c] [x; z] = [r; 0]
     if (z == 0.0) {
       c = 1.0;
       s = 0.0;
@@ -131,28 +120,42 @@ int host_sym_eig(int n, double *a, double *w) {
   const long max_iter = 60L * n;
   while (hi > 0) {
     if (negligible(hi - 1)) {
-      A(T, hi, hi - 1) = A(T, hi - 1, hi) = 0.0;
+      e[hi - 1] = 0.0;
       --hi;
       continue;
     }
     if (++iter > max_iter) return 1;
     int lo = hi - 1;
     while (lo > 0 && !negligible(lo - 1)) --lo;
-    if (lo > 0) A(T, lo, lo - 1) = A(T, lo - 1, lo) = 0.0;
-    const double tnn = A(T, hi, hi), tn1 = A(T, hi, hi - 1);
-    const double dd = 0.5 * (A(T, hi - 1, hi - 1) - tnn);
+    if (lo > 0) e[lo - 1] = 0.0;
+    const double tnn = d[hi], tn1 = e[hi - 1];
+    const double dd = 0.5 * (d[hi - 1] - tnn);
     const double mu = tnn - tn1 * tn1 / (dd + (dd >= 0.0 ? 1.0 : -1.0) * std::hypot(dd, tn1));
-    double x = A(T, lo, lo) - mu, z = A(T, lo + 1, lo);
+    double x = d[lo] - mu, z = e[lo], bulge = 0.0;
     for (int k = lo; k < hi; ++k) {
       double c, s;
       givens(x, z, c, s);
-      rotate(k, c, s, lo, hi);
+      if (k > lo) e[k - 1] = c * e[k - 1] - s * bulge;
+      const double a = d[k], b = e[k], cp = d[k + 1];
+      const double cc = c * c, ss = s * s, cs = c * s;
+      d[k] = cc * a - 2.0 * cs * b + ss * cp;
+      d[k + 1] = ss * a + 2.0 * cs * b + cc * cp;
+      e[k] = cs * (a - cp) + (cc - ss) * b;
       if (k + 1 < hi) {
-        x = A(T, k + 1, k);
-        z = A(T, k + 2, k);
+        bulge = -s * e[k + 1];
+        e[k + 1] = c * e[k + 1];
       }
+      double *zk = &A(Z, 0, k), *zk1 = &A(Z, 0, k + 1);
+      for (int i = 0; i < n; ++i) {
+        const double p = zk[i], q = zk1[i];
+        zk[i] = c * p - s * q;
+        zk1[i] = s * p + c * q;
+      }
+      x = e[k];
+      z = bulge;
     }
   }
+  for (int i = 0; i < n; ++i) A(T, i, i) = d[i];
 
   // ---- 3. ascending order
   std::vector<int> ord(N);
