@@ -267,6 +267,7 @@ struct gbfe_op {
   mutable gbfe::DBuf<int> oz_xexp;    // per-vector exponent of the current X
   gbfe::DBuf<float> mats_f32;         // FP32 copy for the SIMT mixed apply
   gbfe::DBuf<double> diag;
+  gbfe::DBuf<float> diag_f32;  // the diagonal rounded to FP32 (mixed-precision applies)
   gbfe::DBuf<double> fold_scale;  // per-dof factor of this B^-1 folded into A (0 on Dirichlet rows)
   uint64_t serial = gbfe_next_serial();  // identity (folded tiles name their B^-1 by it)
   mutable gbfe::DBuf<__nv_bfloat16> mats_hi_folded;  // split tiles of A diag(fold_scale of folded_for)

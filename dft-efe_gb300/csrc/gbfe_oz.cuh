@@ -128,6 +128,26 @@ __device__ __forceinline__ void colmax_partial_block(const double *__restrict__ 
   }
 }
 
+// Stage 2: ex[c] = max over the nb partial rows, for 32 columns per CTA of
+// COLMAX_FINAL_THREADS threads (32 row lanes x 32 columns, coalesced reads),
+// the lanes' maxima combined through shared memory; EXP_NONE becomes 0.
+constexpr int COLMAX_FINAL_THREADS = 1024;
+__device__ __forceinline__ void colmax_final_block(const int *__restrict__ part, uint32_t nb, uint32_t cols,
+                                                   int *__restrict__ ex) {
+  __shared__ int red[COLMAX_FINAL_THREADS];
+  const uint32_t cl = threadIdx.x % 32, rl = threadIdx.x / 32, rows = COLMAX_FINAL_THREADS / 32;
+  const uint32_t c = blockIdx.x * 32 + cl;
+  int mx = EXP_NONE;
+  if (c < cols)
+    for (uint32_t b = rl; b < nb; b += rows) mx = max(mx, part[(uint64_t)b * cols + c]);
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  if (rl == 0 && c < cols) {
+    for (uint32_t q = 1; q < rows; ++q) mx = max(mx, red[q * 32 + cl]);
+    ex[c] = exp_or_zero(mx);
+  }
+}
+
 // out-of-line, so that the rare call is a branch and not FP64 work that the
 // compiler predicates into every lane
 static __device__ __noinline__ double ldexp_outlined(double v, int k) { return ldexp(v, k); }

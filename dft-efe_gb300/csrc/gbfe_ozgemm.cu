@@ -486,11 +486,7 @@ __global__ void k_oz_colmax_partial(const double *__restrict__ A0, const double 
 }
 
 __global__ void k_oz_colmax_final(const int *__restrict__ part, uint32_t nb, uint32_t cols, int *__restrict__ ex) {
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
-    int mx = oz::EXP_NONE;
-    for (uint32_t b = 0; b < nb; ++b) mx = max(mx, part[(uint64_t)b * cols + c]);
-    ex[c] = oz::exp_or_zero(mx);
-  }
+  oz::colmax_final_block(part, nb, cols, ex);
 }
 
 // per-row exponents of the rotation inputs: one warp per row
@@ -575,9 +571,11 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
   ctx->oz_ipart.ensure((size_t)nb * std::max(rows, mb));
   k_oz_colmax_partial<<<nb, oz::COLMAX_THREADS, 0, ctx->stream>>>(A[0], na > 1 ? A[1] : A[0], na, ma, N,
                                                                   ctx->oz_ipart.p);
-  k_oz_colmax_final<<<(rows + 255) / 256, 256, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, rows, ctx->oz_exp.p);
+  k_oz_colmax_final<<<(rows + 31) / 32, oz::COLMAX_FINAL_THREADS, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, rows,
+                                                                                    ctx->oz_exp.p);
   k_oz_colmax_partial<<<nb, oz::COLMAX_THREADS, 0, ctx->stream>>>(B, B, 1, mb, N, ctx->oz_ipart.p);
-  k_oz_colmax_final<<<(mb + 255) / 256, 256, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, mb, ctx->oz_exp.p + rows);
+  k_oz_colmax_final<<<(mb + 31) / 32, oz::COLMAX_FINAL_THREADS, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, mb,
+                                                                                  ctx->oz_exp.p + rows);
   count_launch(ctx, 4);
   ctx->oz_part.ensure((size_t)items * TILE);
   GramArgs args{A[0], na > 1 ? A[1] : A[0], na, ma, B, mb, N, ctx->oz_exp.p, ctx->oz_exp.p + rows, row_tiles,
