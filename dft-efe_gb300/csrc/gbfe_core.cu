@@ -308,8 +308,10 @@ void block_rows(gbfe_ctx *ctx, const T *X, uint32_t m, uint64_t bb, uint32_t nb,
 }
 
 // Diagonal operator with the constraint epilogue fused in.
+// (d in the vectors' precision: the FP32 path reads a float copy of the
+// diagonal, no FP64 conversion per element)
 template <class T>
-__global__ void k_diag_apply(const T *__restrict__ X, uint32_t m, uint64_t n_dofs, const double *__restrict__ d,
+__global__ void k_diag_apply(const T *__restrict__ X, uint32_t m, uint64_t n_dofs, const T *__restrict__ d,
                              const uint8_t *__restrict__ is_row, const uint32_t *__restrict__ par_ptr,
                              const uint32_t *__restrict__ par_row, const double *__restrict__ par_w,
                              T *__restrict__ Y, const FastDiv fm) {
@@ -323,11 +325,11 @@ __global__ void k_diag_apply(const T *__restrict__ X, uint32_t m, uint64_t n_dof
       Y[t] = (T)0;
       continue;
     }
-    T acc = (T)d[i] * X[t];
+    T acc = d[i] * X[t];
     if (par_ptr) {
       for (uint32_t q = par_ptr[i], qe = par_ptr[i + 1]; q < qe; ++q) {
         const uint32_t r = par_row[q];
-        acc += (T)par_w[q] * ((T)d[r] * X[(uint64_t)r * m + v]);
+        acc += (T)par_w[q] * (d[r] * X[(uint64_t)r * m + v]);
       }
     }
     Y[t] = acc;
@@ -457,7 +459,7 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
       k_diag_apply<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->d.p, m, me->n_dofs, op->diag.p, nullptr,
                                                                          nullptr, nullptr, nullptr, Y->d.p, FastDiv(m));
     else
-      k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->f.p, m, me->n_dofs, op->diag.p, nullptr,
+      k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->f.p, m, me->n_dofs, op->diag_f32.p, nullptr,
                                                                         nullptr, nullptr, nullptr, Y->f.p, FastDiv(m));
     check_launch(ctx, "jacobi_apply");
     return;
@@ -470,7 +472,7 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
       k_diag_apply<double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->d.p, m, me->n_dofs, op->diag.p, nullptr,
                                                                          nullptr, nullptr, nullptr, Y->d.p, FastDiv(m));
     else
-      k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->f.p, m, me->n_dofs, op->diag.p, nullptr,
+      k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(X->f.p, m, me->n_dofs, op->diag_f32.p, nullptr,
                                                                         nullptr, nullptr, nullptr, Y->f.p, FastDiv(m));
     check_launch(ctx, "diag_apply");
     if (X->dtype == GBFE_F64)
@@ -490,7 +492,7 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
           has_par ? c->par_w.p : nullptr, Y->d.p, FastDiv(m));
     else
       k_diag_apply<float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
-          X->f.p, m, me->n_dofs, op->diag.p, isr, has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr,
+          X->f.p, m, me->n_dofs, op->diag_f32.p, isr, has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr,
           has_par ? c->par_w.p : nullptr, Y->f.p, FastDiv(m));
     check_launch(ctx, "diag_apply");
     return;
@@ -1173,10 +1175,13 @@ static int diag_upload_impl(gbfe_mesh *mesh, const gbfe_cons *cons, const double
     op->mesh = mesh;
     op->cons = cons;
     op->kind = kind;
+    std::vector<double> dv(diag, diag + mesh->n_dofs);
+    if (kind == OP_JACOBI)
+      for (double &x : dv) x = 1.0 / x;
+    std::vector<float> df(dv.begin(), dv.end());
+    op->diag_f32.upload(df.data(), mesh->n_dofs, mesh->ctx->stream);
     if (kind == OP_JACOBI) {
-      std::vector<double> inv(mesh->n_dofs);
-      for (uint64_t i = 0; i < mesh->n_dofs; ++i) inv[i] = 1.0 / diag[i];
-      op->diag.upload(inv.data(), mesh->n_dofs, mesh->ctx->stream);
+      op->diag.upload(dv.data(), mesh->n_dofs, mesh->ctx->stream);
       GBFE_CUDA(cudaStreamSynchronize(mesh->ctx->stream));
     } else {
       op->diag.upload(diag, mesh->n_dofs, mesh->ctx->stream);
