@@ -92,11 +92,7 @@ __global__ void k_colmax_partial(const double *__restrict__ X, uint64_t rows, ui
 }
 
 __global__ void k_colmax_final(const int *__restrict__ part, uint32_t nb, uint32_t m, int *__restrict__ ex) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < m; v += gridDim.x * blockDim.x) {
-    int mx = oz::EXP_NONE;
-    for (uint32_t b = 0; b < nb; ++b) mx = max(mx, part[(uint64_t)b * m + v]);
-    ex[v] = oz::exp_or_zero(mx);
-  }
+  oz::colmax_final_block(part, nb, m, ex);
 }
 
 struct OzArgs {
@@ -175,6 +171,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
     // ---------------- TMA producer: 8 slice tiles per chunk
     if (lane == 0) {
       uint32_t q = 0;
+      const uint64_t pol = l2_evict_first_policy();  // slices are read once per launch
       for (uint32_t it = blockIdx.x; it < n_items && !*abort_flag; it += gridDim.x) {
         uint32_t c, mt, v0;
         decode(it, c, mt, v0);
@@ -190,7 +187,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_cell_apply_oz(const OzArgs a)
           mbar_arrive_expect_tx(&full_a[s], OZ_S * bytes);
           for (int sl = 0; sl < OZ_S; ++sl) {
             const __nv_bfloat16 *src = Acell + ((uint64_t)kc * OZ_S + sl) * mt8 * KC + (uint64_t)mt * 128 * KC;
-            bulk_g2s(Ast + sl * OZ_A_PART, src, bytes, &full_a[s]);
+            bulk_g2s_stream(Ast + sl * OZ_A_PART, src, bytes, &full_a[s], pol);
           }
         }
       }
@@ -372,7 +369,8 @@ void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc) {
   ctx->oz_ipart.ensure((size_t)nb * m);
   op->oz_xexp.ensure(m);
   k_colmax_partial<<<nb, oz::COLMAX_THREADS, 0, ctx->stream>>>(X->d.p, rows, m, ctx->oz_ipart.p);
-  k_colmax_final<<<(m + 127) / 128, 128, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, m, op->oz_xexp.p);
+  k_colmax_final<<<(m + 31) / 32, oz::COLMAX_FINAL_THREADS, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, m,
+                                                                             op->oz_xexp.p);
   count_launch(ctx, 2);
   const uint32_t vt = (m + OZ_N - 1) / OZ_N;
   const uint32_t smem = OZ_SMEM;
