@@ -339,10 +339,10 @@ def run_gpu(args, cfg_name, rank, world):
     for _ in range(args.warmup):
         solve(True)
     ctx.synchronize()
-    # inside the timed region only the roofline candidates carry CUDA events
-    ctx.set_profiling(True)
-    ctx.set_profile_filter(ROOFLINE_CANDIDATES)
-    ctx.reset_kernel_stats()
+    # the timed region runs without CUDA events (they cost ~7 % of a solve
+    # inside the captured filter graphs); the per-kernel times for the
+    # roofline come from a second region of the same K solves right after it
+    ctx.set_profiling(False)
     launches0 = ctx.kernel_launches()
     lat, errs, passes, ok, eigs, rcs = [], [], [], 0, [], []
     clocks = ClockSampler(ROOT / "gpurun_out" / "bench_clocks.csv" if (ROOT / "gpurun_out").is_dir() else None)
@@ -362,11 +362,21 @@ def run_gpu(args, cfg_name, rank, world):
         ctx.synchronize()
         barrier()
         t_total = time.perf_counter() - t_start
+    launches = ctx.kernel_launches() - launches0
+    # roofline region: the same K solves, CUDA events on the roofline candidates only
+    ctx.set_profiling(True)
+    ctx.set_profile_filter(ROOFLINE_CANDIDATES)
+    ctx.reset_kernel_stats()
+    ctx.synchronize()
+    tp = time.perf_counter()
+    for _ in range(args.steps):
+        solve(True)
+    ctx.synchronize()
+    t_prof = (time.perf_counter() - tp) / args.steps
     for rc, eig in zip(rcs, eigs):
         err = float(np.abs(eig[:nw] - eig64[:nw]).max())
         errs.append(err)
         ok += int(rc == 0 and err <= EIG_TOL)
-    launches = ctx.kernel_launches() - launches0
     st_mixed = ctx.kernel_stats("cell_apply_mixed")
     st_f64 = ctx.kernel_stats("cell_apply_f64")
     st_oz = ctx.kernel_stats("cell_apply_f64_oz")
@@ -404,7 +414,7 @@ def run_gpu(args, cfg_name, rank, world):
     fp64_peak = ctx.probe_fp64_peak()
     return dict(cfg=cfg, prob=prob, deg=deg, bounds=(wl, wu, uu), tuned=tuned, fp64_times=fp64_times, passes64=passes64,
                 rc64=rc64, lat=lat, errs=errs, passes=passes, ok=ok, t_total=t_total, launches=launches,
-                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, st_dense=st_dense, st_eig=st_eig, breakdown=breakdown, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak,
+                st_mixed=st_mixed, st_f64=st_f64, st_oz=st_oz, st_dense=st_dense, st_eig=st_eig, breakdown=breakdown, clocks=clocks.summary(), e2e_lat=e2e_lat, fp64_peak=fp64_peak, t_prof=t_prof,
                 h2d=prob.n_dofs * m * 8, d2h=prob.n_dofs * m * 8 + 2 * m * 8)
 
 
@@ -721,8 +731,10 @@ def main():
     dom = max(cand, key=lambda k: cand[k]["ms"])
     roof = roofline(dom, cand[dom], r["fp64_peak"])
     roof["traffic"] = NCU_TRAFFIC_PER_LAUNCH.get((args.config, dom))
+    roof["timed_region"] = (f"{args.steps} solves right after the value's timed region, CUDA events around the "
+                            f"roofline candidates: {r['t_prof'] * 1e3:.1f} ms per solve")
     others = {k: v for k, v in cand.items() if k != dom and v["launches"]}
-    others["eig_small_f64 (potrf, trsm, syevd block; includes its host sync)"] = r["st_eig"]
+    others["eig_small_f64 (the m x m block, host or device; includes its host sync)"] = r["st_eig"]
     e2e_sps = world / float(np.mean(r["e2e_lat"]))
     line = {
         "metric": "ChFSI solves/s at |d_eps|<=1e-6 Ha (mixed precision), FP64 beside it",

@@ -689,11 +689,14 @@ int gbfe_ctx_create(int device, gbfe_ctx **out) {
       ctx->tune_cache = cache;
       FILE *f = fopen(cache, "r");
       if (f) {
-        char kind[16];
-        unsigned nd, mt, mm, N, st;
+        // "tc2 nd_max mtiles m N stages occupancy ms" (lines of other shapes are skipped)
+        char line[256], kind[16];
+        unsigned nd, mt, mm, N, st, occ;
         float ms;
-        while (fscanf(f, "%15s %u %u %u %u %u %f", kind, &nd, &mt, &mm, &N, &st, &ms) == 7)
-          if (std::string(kind) == "tc2") ctx->tc_tune[std::make_tuple(nd, mt, mm)] = TcTune{N, st, ms};
+        while (fgets(line, sizeof line, f))
+          if (sscanf(line, "%15s %u %u %u %u %u %u %f", kind, &nd, &mt, &mm, &N, &st, &occ, &ms) == 8 &&
+              std::string(kind) == "tc2")
+            ctx->tc_tune[std::make_tuple(nd, mt, mm)] = TcTune{N, st, ms, occ};
         fclose(f);
       }
     }

@@ -130,6 +130,7 @@ struct GraphProf {
 struct TcTune {
   uint32_t N = 0, stages = 0;
   float ms = 0.f;
+  uint32_t occ = 2;  // resident CTAs per SM the kernel is compiled for (2 or 3)
 };
 
 // Pinned host staging for small host-to-device copies issued inside a solve:

@@ -283,7 +283,10 @@ struct Tc2Args {
   uint32_t wpc;
 };
 
-__global__ void __launch_bounds__(THREADS2, 2) k_cell_apply_tc2(const Tc2Args a) {
+// MINB: resident CTAs per SM the registers are budgeted for (2: 96 per thread;
+// 3: 64, a few spilled) -- more CTAs keep more gather loads in flight
+template <int MINB>
+__global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t N = a.N, mtiles = a.mtiles, S = a.stages, nbuf = a.nbuf, m = a.m;
@@ -630,10 +633,11 @@ bool tc_supported(const gbfe_mesh *me) { return me->nd_max <= 256; }
 
 // v2 launch: persistent grid over (cell, vector tile) items of one M-tile group.
 // N_req / stages_req = 0: the tuned shape if one exists, else the heuristic.
-static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg, uint32_t ncell,
-                       uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0, uint32_t stages_req = 0,
-                       const __nv_bfloat16 *tiles = nullptr, const float *xsub = nullptr, uint32_t sub_begin = 0,
-                       uint32_t sub_n = 0) {
+// returns the resident CTAs per SM the launch used
+static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg,
+                           uint32_t ncell, uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0,
+                           uint32_t stages_req = 0, const __nv_bfloat16 *tiles = nullptr, const float *xsub = nullptr,
+                           uint32_t sub_begin = 0, uint32_t sub_n = 0, uint32_t occ_req = 0) {
   gbfe_mesh *me = op->mesh;
   const uint32_t m = X->m;
   if (!N_req) {
@@ -641,8 +645,10 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
     if (it != ctx->tc_tune.end()) {
       N_req = it->second.N;
       stages_req = it->second.stages;
+      occ_req = it->second.occ;
     }
   }
+  const uint32_t occ = occ_req >= 3 ? 3u : 2u;
   uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
   if (N_req) N = std::min<uint32_t>(N, N_req);
   const uint32_t vt = (m + N - 1) / N;
@@ -657,12 +663,16 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
   const uint32_t nbuf = (2 * mtiles * N <= 512) ? 2 : 1;
   uint32_t cols = 32;
   while (cols < nbuf * mtiles * N) cols *= 2;
-  const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(std::min<uint32_t>((227 * 1024) / smem, 512 / cols), 2));
+  // CTAs per SM: shared memory (228 KB per SM, 1 KB of it reserved per CTA),
+  // TMEM columns and the register budget of the instantiation
+  const uint32_t per_sm =
+      std::max<uint32_t>(1, std::min<uint32_t>(std::min<uint32_t>((228 * 1024) / (smem + 1024), 512 / cols), occ));
   const uint32_t items = ncell * vt;
   const uint32_t grid = std::min<uint32_t>(items, per_sm * (uint32_t)ctx->sm_count);
   static bool attr_set = false;
   if (!attr_set) {
-    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     attr_set = true;
   }
   // float4 gather when every row of X (and of xsub) starts on a 16-byte boundary
@@ -676,8 +686,12 @@ static void launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float
                sub_n, wpc};
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
-  k_cell_apply_tc2<<<grid, THREADS2, smem, ctx->stream>>>(args);
+  if (per_sm >= 3)
+    k_cell_apply_tc2<3><<<grid, THREADS2, smem, ctx->stream>>>(args);
+  else
+    k_cell_apply_tc2<2><<<grid, THREADS2, smem, ctx->stream>>>(args);
   check_launch(ctx, "cell_apply_tc2");
+  return per_sm;
 }
 
 // Yc (FP32 cell-wise buffer) = split-BF16 tensor-core products, size-binned by
@@ -761,10 +775,15 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
     best.ms = 1e30f;
     for (uint32_t N : {16u, 32u, 64u, 128u, 256u}) {
       if (N > std::max<uint32_t>(16, (m + 15) / 16 * 16) && N != 16) continue;
-      for (uint32_t st : {2u, 3u, 4u}) {
-        launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st);  // warm
+      for (uint32_t st : {2u, 3u, 4u})
+      for (uint32_t occ : {2u, 3u}) {
+        // warm; a shape that cannot hold 3 CTAs per SM runs as the 2-CTA one: not timed twice
+        const uint32_t used =
+            launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st, nullptr, nullptr, 0, 0, occ);
+        if (occ > 2 && used < occ) continue;
         GBFE_CUDA(cudaEventRecord(e0, ctx->stream));
-        for (int r = 0; r < 3; ++r) launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st);
+        for (int r = 0; r < 3; ++r)
+          launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st, nullptr, nullptr, 0, 0, occ);
         GBFE_CUDA(cudaEventRecord(e1, ctx->stream));
         GBFE_CUDA(cudaEventSynchronize(e1));
         int st_word = 0;
@@ -780,12 +799,14 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
           best.ms = ms;
           best.N = N;
           best.stages = st;
+          best.occ = occ;
         }
       }
     }
     ctx->tc_tune[std::make_tuple(nd_max, mtiles, m)] = best;
     log.push_back("tc2 " + std::to_string(nd_max) + " " + std::to_string(mtiles) + " " + std::to_string(m) + " " +
-                  std::to_string(best.N) + " " + std::to_string(best.stages) + " " + std::to_string(best.ms));
+                  std::to_string(best.N) + " " + std::to_string(best.stages) + " " + std::to_string(best.occ) + " " +
+                  std::to_string(best.ms));
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
