@@ -16,13 +16,104 @@
 //   3. eigenvalues ascending with their eigenvector columns.
 // Pure C++ (no intrinsics): identical code on x86 and Arm hosts.
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <utility>
 #include <cstdint>
 #include <numeric>
 #include <vector>
 
 namespace gbfe {
+
+namespace {
+
+// Fork-join pool for the row- and column-independent parts of the m x m block
+// (the accumulation of the QR rotations into the eigenvectors, the triangular
+// solves).  HOST_THREADS - 1 workers; a worker spins on the job counter for a
+// while after each job (the next one comes a few milliseconds later, one per
+// ChFSI pass) and then sleeps on a condition variable.  A job's split depends
+// only on the problem size, never on timing, so results are the same
+// whatever thread runs which part.
+constexpr int HOST_THREADS = 4;
+
+class HostPool {
+ public:
+  static HostPool &get() {
+    static HostPool pool;
+    return pool;
+  }
+  // f(part) for part = 0 .. parts-1, parts <= HOST_THREADS; the caller runs part 0
+  void run(int parts, const std::function<void(int)> &f) {
+    if (parts <= 1 || workers_.empty()) {
+      for (int t = 0; t < parts; ++t) f(t);
+      return;
+    }
+    std::lock_guard<std::mutex> serial(run_mu_);  // one job at a time
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      job_ = &f;
+      parts_ = parts;
+      pending_.store(parts - 1, std::memory_order_relaxed);
+      gen_.fetch_add(1, std::memory_order_release);
+    }
+    cv_.notify_all();
+    f(0);
+    while (pending_.load(std::memory_order_acquire) != 0) std::this_thread::yield();
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+      gen_.fetch_add(1, std::memory_order_release);
+    }
+    cv_.notify_all();
+    for (auto &t : workers_) t.join();
+  }
+
+ private:
+  HostPool() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int n = hw >= 8 ? HOST_THREADS - 1 : 0;  // leave small hosts alone
+    for (int i = 0; i < n; ++i) workers_.emplace_back([this, i] { loop(i + 1); });
+  }
+  void loop(int part) {
+    uint64_t seen = 0;
+    for (;;) {
+      // spin ~2 ms for the next job, then sleep
+      const auto t0 = std::chrono::steady_clock::now();
+      while (gen_.load(std::memory_order_acquire) == seen &&
+             std::chrono::steady_clock::now() - t0 < std::chrono::milliseconds(2))
+        std::this_thread::yield();
+      std::unique_lock<std::mutex> lk(mu_);
+      cv_.wait(lk, [&] { return gen_.load(std::memory_order_acquire) != seen; });
+      seen = gen_.load(std::memory_order_acquire);
+      if (stop_) return;
+      const std::function<void(int)> *job = job_;
+      const int parts = parts_;
+      lk.unlock();
+      if (part < parts) (*job)(part);
+      if (part < parts) pending_.fetch_sub(1, std::memory_order_acq_rel);
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex mu_, run_mu_;
+  std::condition_variable cv_;
+  std::atomic<uint64_t> gen_{0};
+  std::atomic<int> pending_{0};
+  const std::function<void(int)> *job_ = nullptr;
+  int parts_ = 0;
+  bool stop_ = false;
+};
+
+// parts of an n-wide independent range worth a thread each
+inline int host_parts(int n) { return n >= 48 ? HOST_THREADS : 1; }
+
+}  // namespace
 
 // a: n x n column-major; the lower triangle is read.  On success a holds the
 // orthonormal eigenvectors (column j belongs to w[j]) and w the eigenvalues in
@@ -115,6 +206,10 @@ int host_sym_eig(int n, double *a, double *w) {
       s = c * t;
     }
   };
+  std::vector<int> rot_k;
+  std::vector<double> rot_cs;
+  rot_k.reserve(N * 40);
+  rot_cs.reserve(N * 80);
   int hi = n - 1;
   long iter = 0;
   const long max_iter = 60L * n;
@@ -145,17 +240,41 @@ int host_sym_eig(int n, double *a, double *w) {
         bulge = -s * e[k + 1];
         e[k + 1] = c * e[k + 1];
       }
-      double *zk = &A(Z, 0, k), *zk1 = &A(Z, 0, k + 1);
-      for (int i = 0; i < n; ++i) {
-        const double p = zk[i], q = zk1[i];
-        zk[i] = c * p - s * q;
-        zk1[i] = s * p + c * q;
-      }
+      rot_k.push_back(k);
+      rot_cs.push_back(c);
+      rot_cs.push_back(s);
       x = e[k];
       z = bulge;
     }
   }
   for (int i = 0; i < n; ++i) A(T, i, i) = d[i];
+  // Z <- Z G_1 G_2 ...: every row of Z sees the rotations in order, rows are
+  // independent, so blocks of rows go to the pool (each block copied into a
+  // small column-major tile so a rotation updates two contiguous columns)
+  {
+    const int parts = host_parts(n);
+    const size_t nrot = rot_k.size();
+    HostPool::get().run(parts, [&](int part) {
+      const int r0 = (int)((int64_t)n * part / parts), r1 = (int)((int64_t)n * (part + 1) / parts);
+      const int rb = r1 - r0;
+      if (rb <= 0) return;
+      std::vector<double> tile((size_t)rb * N);
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < rb; ++i) tile[(size_t)j * rb + i] = A(Z, r0 + i, j);
+      for (size_t r = 0; r < nrot; ++r) {
+        const int k = rot_k[r];
+        const double c = rot_cs[2 * r], sn = rot_cs[2 * r + 1];
+        double *zk = &tile[(size_t)k * rb], *zk1 = zk + rb;
+        for (int i = 0; i < rb; ++i) {
+          const double p = zk[i], q = zk1[i];
+          zk[i] = c * p - sn * q;
+          zk1[i] = sn * p + c * q;
+        }
+      }
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < rb; ++i) A(Z, r0 + i, j) = tile[(size_t)j * rb + i];
+    });
+  }
 
   // ---- 3. ascending order
   std::vector<int> ord(N);
@@ -199,7 +318,9 @@ int host_cholesky(int n, double *a) {
 // substitution on every column of B, column-oriented
 void host_trsm_lower(int n, const double *L, double *B) {
   const size_t N = (size_t)n;
-  for (int j = 0; j < n; ++j) {
+  const int parts = host_parts(n);
+  HostPool::get().run(parts, [&](int part) {
+  for (int j = (int)((int64_t)n * part / parts); j < (int)((int64_t)n * (part + 1) / parts); ++j) {
     double *b = B + N * j;
     for (int k = 0; k < n; ++k) {
       const double *lk = L + N * k;
@@ -209,13 +330,16 @@ void host_trsm_lower(int n, const double *L, double *B) {
       for (int i = k + 1; i < n; ++i) b[i] -= lk[i] * x;
     }
   }
+  });
 }
 
 // B <- L^-T B for lower triangular L: back substitution with the rows of L^T
 // (the columns of L), every dot product down a contiguous column
 void host_trsm_lower_t(int n, const double *L, double *B) {
   const size_t N = (size_t)n;
-  for (int j = 0; j < n; ++j) {
+  const int parts = host_parts(n);
+  HostPool::get().run(parts, [&](int part) {
+  for (int j = (int)((int64_t)n * part / parts); j < (int)((int64_t)n * (part + 1) / parts); ++j) {
     double *b = B + N * j;
     for (int k = n - 1; k >= 0; --k) {
       const double *lk = L + N * k;
@@ -224,6 +348,7 @@ void host_trsm_lower_t(int n, const double *L, double *B) {
       b[k] = s / lk[k];
     }
   }
+  });
 }
 
 // A <- L^-1 A L^-T for symmetric A (full storage): W = L^-1 A, then

@@ -68,7 +68,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             if log:
                 print(f"--- {obj.name}\n{log}", file=sys.stderr)
     if force or _stale(LIB, objs):
-        cmd = [nv, *GENCODE, "-shared", "-o", str(LIB), *map(str, objs), "-lcublas", "-lcusolver", "-lcudart"]
+        cmd = [nv, *GENCODE, "-shared", "-o", str(LIB), *map(str, objs), "-lcublas", "-lcusolver", "-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
