@@ -143,12 +143,19 @@ int host_sym_eig(int n, double *a, double *w) {
     for (int i = 0; i < L; ++i) vv += v[i] * v[i];
     if (vv == 0.0) continue;
     const double b = 2.0 / vv;
-    // p = b A22 v;  q = p - (b/2)(v^T p) v;  A22 -= v q^T + q v^T
+    // p = b A22 v;  q = p - (b/2)(v^T p) v;  A22 -= v q^T + q v^T, on the
+    // lower triangle of A22 only (symmetric: one pass down each column gives
+    // both its axpy into p and its dot with v)
     for (int i = 0; i < L; ++i) p[i] = 0.0;
-    for (int j = 0; j < L; ++j) {  // column-major: contiguous inner loop
+    for (int j = 0; j < L; ++j) {  // column-major: contiguous inner loops
       const double vj = b * v[j];
       const double *col = &A(T, k + 1, k + 1 + j);
-      for (int i = 0; i < L; ++i) p[i] += col[i] * vj;
+      double dot = 0.0;
+      for (int i = j + 1; i < L; ++i) {
+        p[i] += col[i] * vj;
+        dot += col[i] * v[i];
+      }
+      p[j] += col[j] * vj + b * dot;
     }
     double vp = 0.0;
     for (int i = 0; i < L; ++i) vp += v[i] * p[i];
@@ -157,25 +164,32 @@ int host_sym_eig(int n, double *a, double *w) {
     for (int j = 0; j < L; ++j) {
       double *col = &A(T, k + 1, k + 1 + j);
       const double qj = q[j], vj = v[j];
-      for (int i = 0; i < L; ++i) col[i] -= v[i] * qj + q[i] * vj;
+      for (int i = j; i < L; ++i) col[i] -= v[i] * qj + q[i] * vj;
     }
     A(T, k + 1, k) = A(T, k, k + 1) = alpha;
     for (int i = 1; i < L; ++i) A(T, k + 1 + i, k) = A(T, k, k + 1 + i) = 0.0;
     for (int i = 0; i < L; ++i) refl[(size_t)k * N + i] = v[i];
     beta[k] = b;
   }
-  // Q = H_0 H_1 ... H_{n-3}, built as H_k Q for k descending
+  // Q = H_0 H_1 ... H_{n-3}, built as H_k Q for k descending.  Column j is
+  // touched by the reflectors k < j only, each column independently: the
+  // columns are dealt round robin to the pool (column j costs ~j reflectors)
   for (int i = 0; i < n; ++i) A(Z, i, i) = 1.0;
-  for (int k = n - 3; k >= 0; --k) {
-    if (beta[k] == 0.0) continue;
-    const int L = n - k - 1;
-    const double *vk = &refl[(size_t)k * N];
-    for (int j = k + 1; j < n; ++j) {
-      double s = 0.0;
-      for (int i = 0; i < L; ++i) s += vk[i] * A(Z, k + 1 + i, j);
-      s *= beta[k];
-      for (int i = 0; i < L; ++i) A(Z, k + 1 + i, j) -= s * vk[i];
-    }
+  {
+    const int parts = host_parts(n);
+    HostPool::get().run(parts, [&](int part) {
+      for (int j = 1 + part; j < n; j += parts)
+        for (int k = std::min(j - 1, n - 3); k >= 0; --k) {
+          if (beta[k] == 0.0) continue;
+          const int L = n - k - 1;
+          const double *vk = &refl[(size_t)k * N];
+          double *z = &A(Z, k + 1, j);
+          double s = 0.0;
+          for (int i = 0; i < L; ++i) s += vk[i] * z[i];
+          s *= beta[k];
+          for (int i = 0; i < L; ++i) z[i] -= s * vk[i];
+        }
+    });
   }
 
   // ---- 2. implicit symmetric QR with Wilkinson shifts on the tridiagonal
