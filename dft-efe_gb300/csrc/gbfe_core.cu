@@ -589,6 +589,10 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
   // below; before it only the dense block reads rows of RN, so it runs here
   // only when a constrained row lies inside the block
   if (BInv->blk_cons) constraints_p2c(ctx, c, RN);
+  // fork point of the size groups that do not read the substituted rows
+  // (they need not wait for the block rows below)
+  const bool fork = ctx->split_groups && !ctx->profiling && ctx->side_stream;
+  if (fork) GBFE_CUDA(cudaEventRecord(ctx->fork_ev, ctx->stream));
   const float *xsub = nullptr;
   if (BInv->kind == OP_DIAG_BLOCK) {
     // the enrichment rows of B^-1 RN: the dense block times those rows of RN,
@@ -605,7 +609,7 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
   }
   A->cellbuf_f32.ensure((size_t)me->total_cell_dofs * m);
   cell_apply_tc(A, RN, A->cellbuf_f32.p, A->mats_hi_folded.p, xsub, (uint32_t)BInv->blk_begin,
-                xsub ? (uint32_t)BInv->blk_n : 0u);
+                xsub ? (uint32_t)BInv->blk_n : 0u, fork);
   const uint64_t n = (uint64_t)me->n_dofs * m;
   {
     ProfScope prof_k(ctx, "k:assemble_cheb", 0.0, 0.0);
@@ -727,6 +731,12 @@ int gbfe_ctx_destroy(gbfe_ctx *ctx) {
       cudaEventDestroy(pr.second);
     }
   for (cudaEvent_t e : ctx->event_free) cudaEventDestroy(e);
+  if (ctx->side_stream) {
+    cudaStreamSynchronize(ctx->side_stream);
+    cudaStreamDestroy(ctx->side_stream);
+  }
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+  if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
   if (ctx->cusolver) cusolverDnDestroy(ctx->cusolver);
   if (ctx->cublas) cublasDestroy(ctx->cublas);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -767,6 +777,12 @@ int gbfe_ctx_check_status(gbfe_ctx *ctx) {
   });
   if (rc != GBFE_OK) return rc;
   return st ? GBFE_ERR_TIMEOUT : GBFE_OK;
+}
+
+int gbfe_ctx_set_split_groups(gbfe_ctx *ctx, int on) {
+  if (!ctx) return GBFE_ERR_ARG;
+  ctx->split_groups = on ? 1 : 0;
+  return GBFE_OK;
 }
 
 int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode) {

@@ -161,6 +161,11 @@ struct gbfe_ctx {
   std::vector<std::string> prof_only;   // profiling restricted to these scope names (empty: all)
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  // second stream for the split-BF16 size groups that do not wait on the
+  // enrichment rows: forked from `stream` by fork_ev, joined by join_ev
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  int split_groups = 1;      // 1: independent size groups of a cell product run concurrently
   cublasHandle_t cublas = nullptr;
   cusolverDnHandle_t cusolver = nullptr;
   std::string last_error;
@@ -413,7 +418,8 @@ void build_mixed_mats(gbfe_op *op);
 void build_tc_mats(gbfe_op *op);
 bool tc_supported(const gbfe_mesh *me);
 void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const __nv_bfloat16 *tiles = nullptr,
-                   const float *xsub = nullptr, uint32_t sub_begin = 0, uint32_t sub_n = 0);
+                   const float *xsub = nullptr, uint32_t sub_begin = 0, uint32_t sub_n = 0,
+                   bool fork_recorded = false);
 void build_tc_mats_folded(const gbfe_op *op, const double *kscale, gbfe::DBuf<__nv_bfloat16> &out);
 // one step of the mixed Chebyshev recurrence in two launches:
 //   R = alpha1 (A B^-1 RN - c RN) + alpha2 R + alpha1 eF2[j] Y

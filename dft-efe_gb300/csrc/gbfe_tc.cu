@@ -637,9 +637,11 @@ bool tc_supported(const gbfe_mesh *me) { return me->nd_max <= 256; }
 static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg,
                            uint32_t ncell, uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0,
                            uint32_t stages_req = 0, const __nv_bfloat16 *tiles = nullptr, const float *xsub = nullptr,
-                           uint32_t sub_begin = 0, uint32_t sub_n = 0, uint32_t occ_req = 0) {
+                           uint32_t sub_begin = 0, uint32_t sub_n = 0, uint32_t occ_req = 0,
+                           cudaStream_t stream = nullptr) {
   gbfe_mesh *me = op->mesh;
   const uint32_t m = X->m;
+  if (!stream) stream = ctx->stream;
   if (!N_req) {
     auto it = ctx->tc_tune.find(std::make_tuple(nd_max, mtiles, m));
     if (it != ctx->tc_tune.end()) {
@@ -687,21 +689,70 @@ static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, f
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
   if (per_sm >= 3)
-    k_cell_apply_tc2<3><<<grid, THREADS2, smem, ctx->stream>>>(args);
+    k_cell_apply_tc2<3><<<grid, THREADS2, smem, stream>>>(args);
   else
-    k_cell_apply_tc2<2><<<grid, THREADS2, smem, ctx->stream>>>(args);
+    k_cell_apply_tc2<2><<<grid, THREADS2, smem, stream>>>(args);
   check_launch(ctx, "cell_apply_tc2");
   return per_sm;
 }
 
 // Yc (FP32 cell-wise buffer) = split-BF16 tensor-core products, size-binned by
 // the number of 128-row M tiles a cell needs.
+// Independent size groups run concurrently (profiling off): one group that
+// does not read the substituted rows goes to the side stream, forked at the
+// fork event (recorded by the caller before it computed xsub, or here), and
+// joins the context stream before the assembly.
 void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const __nv_bfloat16 *tiles, const float *xsub,
-                   uint32_t sub_begin, uint32_t sub_n) {
+                   uint32_t sub_begin, uint32_t sub_n, bool fork_recorded) {
   gbfe_mesh *me = op->mesh;
   gbfe_ctx *ctx = me->ctx;
   const uint32_t m = X->m;
   GBFE_REQUIRE((!tiles && !xsub) || ctx->tc_version == 2, "folded tiles need the persistent tensor-core kernel");
+  if (ctx->tc_version == 2) {
+    struct Group {
+      uint32_t cbeg, ncell, mtiles, nd_max;
+      bool sub;
+    };
+    std::vector<Group> groups;
+    for (uint32_t mtiles = 1; mtiles <= 2; ++mtiles) {
+      uint32_t b0 = UINT32_MAX, b1 = 0;
+      for (uint32_t b = 0; b < me->bin_nd.size(); ++b)
+        if ((me->bin_nd[b] + 127) / 128 == mtiles) {
+          b0 = std::min(b0, b);
+          b1 = b + 1;
+        }
+      if (b0 == UINT32_MAX) continue;
+      // substitution only where the group's cells hold substituted rows
+      uint32_t max_id = 0;
+      for (uint32_t b = b0; b < b1; ++b) max_id = std::max(max_id, me->bin_max_id[b]);
+      groups.push_back(Group{me->bin_begin[b0], me->bin_begin[b1] - me->bin_begin[b0], mtiles, me->bin_nd[b1 - 1],
+                             xsub && max_id >= sub_begin});
+    }
+    int side = -1;
+    if (ctx->split_groups && !ctx->profiling && groups.size() >= 2)
+      for (size_t g = 0; g < groups.size() && side < 0; ++g)
+        if (!groups[g].sub) side = (int)g;
+    if (side >= 0) {
+      if (!ctx->side_stream) {
+        GBFE_CUDA(cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
+        GBFE_CUDA(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
+        GBFE_CUDA(cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming));
+      }
+      if (!fork_recorded) GBFE_CUDA(cudaEventRecord(ctx->fork_ev, ctx->stream));
+      GBFE_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0));
+    }
+    for (size_t g = 0; g < groups.size(); ++g) {
+      const Group &G = groups[g];
+      launch_tc2(ctx, op, X, Yc, G.cbeg, G.ncell, G.mtiles, (double)G.ncell / me->n_cells, G.nd_max, 0, 0, tiles,
+                 G.sub ? xsub : nullptr, sub_begin, G.sub ? sub_n : 0u, 0,
+                 (int)g == side ? ctx->side_stream : ctx->stream);
+    }
+    if (side >= 0) {
+      GBFE_CUDA(cudaEventRecord(ctx->join_ev, ctx->side_stream));
+      GBFE_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0));
+    }
+    return;
+  }
   // group bins (distinct nd) into launches by M-tile count
   for (uint32_t mtiles = 1; mtiles <= 2; ++mtiles) {
     uint32_t b0 = UINT32_MAX, b1 = 0;
@@ -716,15 +767,6 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const __nv_bf
     // bins are sorted by nd, so the cells of [b0, b1) are contiguous in bin_cells
     const uint32_t cbeg = me->bin_begin[b0], cend = me->bin_begin[b1];
     const uint32_t ncell = cend - cbeg;
-    if (ctx->tc_version == 2) {
-      // substitution only where the group's cells hold substituted rows
-      uint32_t max_id = 0;
-      for (uint32_t b = b0; b < b1; ++b) max_id = std::max(max_id, me->bin_max_id[b]);
-      const bool sub = xsub && max_id >= sub_begin;
-      launch_tc2(ctx, op, X, Yc, cbeg, ncell, mtiles, (double)ncell / me->n_cells, me->bin_nd[b1 - 1], 0, 0, tiles,
-                 sub ? xsub : nullptr, sub_begin, sub ? sub_n : 0u);
-      continue;
-    }
     uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
     const uint32_t vt = (m + N - 1) / N;
     N = ((m + vt - 1) / vt + 15) / 16 * 16;  // balance the vector tiles

@@ -53,6 +53,7 @@ SIGNATURES = {
     "gbfe_ctx_kernel_launches": (i32, [p, C.POINTER(u64)]),
     "gbfe_ctx_check_status": (i32, [p]),
     "gbfe_ctx_set_tensor_cores": (i32, [p, i32]),
+    "gbfe_ctx_set_split_groups": (i32, [p, i32]),
     "gbfe_ctx_set_profiling": (i32, [p, i32]),
     "gbfe_ctx_set_fp64_apply": (i32, [p, i32]),
     "gbfe_ctx_set_graphs": (i32, [p, i32]),

@@ -73,6 +73,10 @@ class LinAlgOpContext:
         1: one-CTA-per-cell tcgen05, 0: FP32 SIMT."""
         check(self.lib.gbfe_ctx_set_tensor_cores(self.h, int(mode)), self.h, "set_tensor_cores")
 
+    def set_split_groups(self, on: bool) -> None:
+        """Size groups of a split-BF16 cell product on two streams (default) or one."""
+        check(self.lib.gbfe_ctx_set_split_groups(self.h, 1 if on else 0), self.h, "set_split_groups")
+
     def set_graphs(self, on: bool) -> None:
         check(self.lib.gbfe_ctx_set_graphs(self.h, 1 if on else 0), self.h, "set_graphs")
 

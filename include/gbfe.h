@@ -78,6 +78,11 @@ int gbfe_ctx_check_status(gbfe_ctx *ctx);
  * tcgen05 kernel; 0 the FP32 SIMT kernel.  The environment variable
  * GBFE_TENSOR_CORES=0|1 sets the initial mode of a new context. */
 int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode);
+/* 1 (default): the size groups of a split-BF16 cell product (cells needing one
+ * or two 128-row tiles) run concurrently on a second stream when one of them
+ * does not read the enrichment rows computed just before (profiling off);
+ * 0: one after the other on the context's stream. */
+int gbfe_ctx_set_split_groups(gbfe_ctx *ctx, int on);
 /* ---- nonlocal pseudopotential part ---------------------------------------
  * Replaces basis::AtomCenterNonLocalOpContextFE
  * (basis/AtomCenterNonLocalOpContextFE.h:47-179): Y = sum_atoms C^T V C X.
