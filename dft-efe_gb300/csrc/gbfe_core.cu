@@ -513,6 +513,39 @@ void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
   assemble_cells(me, c, GBFE_F64, op->cellbuf.p, Y);
 }
 
+void apply_pair_f64(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X, gbfe_mv *AX, gbfe_mv *BX) {
+  gbfe_ctx *ctx = A->mesh->ctx;
+  const bool pair = X->dtype == GBFE_F64 && A->kind == OP_CELL && B->kind == OP_CELL && A->mesh == B->mesh &&
+                    X->mesh == A->mesh && A->cons == B->cons && !A->nl && !B->nl && ctx->fp64_tc &&
+                    A->oz_aoff.p && B->oz_aoff.p && ctx->split_groups && !ctx->profiling && X->m > 0 &&
+                    AX != BX && AX != X && BX != X && AX->m == X->m && BX->m == X->m &&
+                    AX->dtype == GBFE_F64 && BX->dtype == GBFE_F64;
+  if (!pair) {
+    apply_op(B, X, BX);
+    apply_op(A, X, AX);
+    return;
+  }
+  gbfe_mesh *me = A->mesh;
+  const uint32_t m = X->m;
+  constraints_p2c(ctx, A->cons, X);  // once: both applies read the same constrained X
+  const int *xexp = oz_column_exponents(A, X);
+  if (!ctx->side_stream) {
+    GBFE_CUDA(cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
+    GBFE_CUDA(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
+    GBFE_CUDA(cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming));
+  }
+  GBFE_CUDA(cudaEventRecord(ctx->fork_ev, ctx->stream));
+  GBFE_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0));
+  B->cellbuf.ensure((size_t)me->total_cell_dofs * m);
+  A->cellbuf.ensure((size_t)me->total_cell_dofs * m);
+  cell_apply_oz(B, X, B->cellbuf.p, xexp, ctx->side_stream);
+  assemble_cells(me, B->cons, GBFE_F64, B->cellbuf.p, BX, ctx->side_stream);
+  cell_apply_oz(A, X, A->cellbuf.p, xexp, ctx->stream);
+  assemble_cells(me, A->cons, GBFE_F64, A->cellbuf.p, AX, ctx->stream);
+  GBFE_CUDA(cudaEventRecord(ctx->join_ev, ctx->side_stream));
+  GBFE_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0));
+}
+
 void h2d_staged(gbfe_ctx *ctx, PinnedSlot &slot, void *dst, const void *src, size_t n) {
   if (!n) return;
   if (slot.done) GBFE_CUDA(cudaEventSynchronize(slot.done));  // the previous staged copy has left
@@ -528,19 +561,20 @@ void h2d_staged(gbfe_ctx *ctx, PinnedSlot &slot, void *dst, const void *src, siz
   GBFE_CUDA(cudaEventRecord(slot.done, ctx->stream));
 }
 
-void assemble_cells(gbfe_mesh *me, const gbfe_cons *c, int dtype, const void *Yc, gbfe_mv *Y) {
+void assemble_cells(gbfe_mesh *me, const gbfe_cons *c, int dtype, const void *Yc, gbfe_mv *Y, cudaStream_t stream) {
   gbfe_ctx *ctx = me->ctx;
+  if (!stream) stream = ctx->stream;
   const bool has_par = c && !c->pure_dirichlet;
   const uint64_t n = (uint64_t)me->n_dofs * Y->m;
   const uint8_t *isr = c ? c->is_row.p : nullptr;
   if (!has_par && Y->m % (dtype == GBFE_F64 ? 2 : 4) == 0) {
     ProfScope prof_k(ctx, dtype == GBFE_F64 ? "k:assemble_f64" : "k:assemble_f32", 0.0, 0.0);
     if (dtype == GBFE_F64)
-      k_assemble_vec<double, 2><<<stride_grid(ctx, n / 2), 256, 0, ctx->stream>>>(
+      k_assemble_vec<double, 2><<<stride_grid(ctx, n / 2), 256, 0, stream>>>(
           static_cast<const double *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr, Y->d.p,
           FastDiv(Y->m / 2));
     else
-      k_assemble_vec<float, 4><<<stride_grid(ctx, n / 4), 256, 0, ctx->stream>>>(
+      k_assemble_vec<float, 4><<<stride_grid(ctx, n / 4), 256, 0, stream>>>(
           static_cast<const float *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr, Y->f.p,
           FastDiv(Y->m / 4));
     check_launch(ctx, "assemble_vec");
@@ -549,7 +583,7 @@ void assemble_cells(gbfe_mesh *me, const gbfe_cons *c, int dtype, const void *Yc
   if (dtype == GBFE_F64) {
     {
       ProfScope prof_k(ctx, "k:assemble_f64", 0.0, 0.0);
-      k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+      k_assemble<double, double><<<stride_grid(ctx, n), 256, 0, stream>>>(
           static_cast<const double *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
           has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->d.p,
           FastDiv(Y->m));
@@ -558,7 +592,7 @@ void assemble_cells(gbfe_mesh *me, const gbfe_cons *c, int dtype, const void *Yc
   } else {
     {
       ProfScope prof_k(ctx, "k:assemble_f32", 0.0, 0.0);
-      k_assemble<float, float><<<stride_grid(ctx, n), 256, 0, ctx->stream>>>(
+      k_assemble<float, float><<<stride_grid(ctx, n), 256, 0, stream>>>(
           static_cast<const float *>(Yc), Y->m, me->n_dofs, me->slot_ptr.p, me->slot.p, isr,
           has_par ? c->par_ptr.p : nullptr, has_par ? c->par_row.p : nullptr, has_par ? c->par_w.p : nullptr, Y->f.p,
           FastDiv(Y->m));
@@ -737,6 +771,7 @@ int gbfe_ctx_destroy(gbfe_ctx *ctx) {
   }
   if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
   if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
+  if (ctx->host_ev) cudaEventDestroy(ctx->host_ev);
   if (ctx->cusolver) cusolverDnDestroy(ctx->cusolver);
   if (ctx->cublas) cublasDestroy(ctx->cublas);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);

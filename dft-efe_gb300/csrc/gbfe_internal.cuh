@@ -165,6 +165,7 @@ struct gbfe_ctx {
   // enrichment rows: forked from `stream` by fork_ev, joined by join_ev
   cudaStream_t side_stream = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  cudaEvent_t host_ev = nullptr;  // the host waits on this one, not on the stream, when work follows a download
   int split_groups = 1;      // 1: independent size groups of a cell product run concurrently
   cublasHandle_t cublas = nullptr;
   cusolverDnHandle_t cusolver = nullptr;
@@ -431,7 +432,12 @@ bool filter_step_fused(const gbfe_op *A, const gbfe_op *BInv, gbfe_mv *RN, gbfe_
 // host -> device copy of n bytes through a pinned staging slot (no stream sync)
 void h2d_staged(gbfe_ctx *ctx, PinnedSlot &slot, void *dst, const void *src, size_t n);
 // Y = assembled cell-wise buffer Yc with the constraint epilogue of `cons`
-void assemble_cells(gbfe_mesh *me, const gbfe_cons *cons, int dtype, const void *Yc, gbfe_mv *Y);
+void assemble_cells(gbfe_mesh *me, const gbfe_cons *cons, int dtype, const void *Yc, gbfe_mv *Y,
+                    cudaStream_t stream = nullptr);
+// AX = A X and BX = B X for two FP64 cell operators on the same mesh and
+// constraints: the column exponents of X once, the two sliced products and
+// assemblies on two streams (else two apply_op calls)
+void apply_pair_f64(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X, gbfe_mv *AX, gbfe_mv *BX);
 void nonlocal_project(const gbfe_nl *nl, const gbfe_mv *X);
 void nonlocal_add(const gbfe_nl *nl, uint32_t m, int dtype, void *Yc);
 void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log);
@@ -446,10 +452,15 @@ void host_sandwich(int n, const double *L, double *A);
 bool oz_gemm_supported(gbfe_ctx *ctx, uint32_t m);
 void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, const double *B, uint32_t mb,
              uint64_t N, double *const *S);
+// rows_ready: oz_rotate_rows already ran for these Y since they last changed
 void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const double *const *Y, double *const *out,
-               uint32_t nops, uint64_t N);
+               uint32_t nops, uint64_t N, bool rows_ready = false);
+void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N);
 void build_oz_mats(gbfe_op *op);
-void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc);
+// xexp: column exponents of X computed beforehand (nullptr: computed here)
+void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc, const int *xexp = nullptr,
+                   cudaStream_t stream = nullptr);
+const int *oz_column_exponents(const gbfe_op *op, const gbfe_mv *X);
 
 // vector kernels (solvers)
 void axpby(gbfe_ctx *ctx, size_t n, double a, const gbfe_mv *x, double b, const gbfe_mv *y, gbfe_mv *z);

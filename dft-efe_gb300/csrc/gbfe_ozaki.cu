@@ -360,7 +360,8 @@ void build_oz_mats(gbfe_op *op) {
 }
 
 // Yc (FP64 cell-wise buffer) = FP64-accurate sliced tensor-core products
-void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc) {
+// per-column exponents of X into op's buffer (context stream)
+const int *oz_column_exponents(const gbfe_op *op, const gbfe_mv *X) {
   gbfe_mesh *me = op->mesh;
   gbfe_ctx *ctx = me->ctx;
   const uint32_t m = X->m;
@@ -372,6 +373,15 @@ void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc) {
   k_colmax_final<<<(m + 31) / 32, oz::COLMAX_FINAL_THREADS, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, m,
                                                                              op->oz_xexp.p);
   count_launch(ctx, 2);
+  return op->oz_xexp.p;
+}
+
+void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc, const int *xexp, cudaStream_t stream) {
+  gbfe_mesh *me = op->mesh;
+  gbfe_ctx *ctx = me->ctx;
+  const uint32_t m = X->m;
+  if (!stream) stream = ctx->stream;
+  if (!xexp) xexp = oz_column_exponents(op, X);
   const uint32_t vt = (m + OZ_N - 1) / OZ_N;
   const uint32_t smem = OZ_SMEM;
   static bool attr_set = false;  // once: not a stream operation, so it stays out of graph captures
@@ -391,11 +401,11 @@ void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc) {
     const uint32_t items = ncell * mts * vt;
     const uint32_t grid = std::min<uint32_t>(items, (uint32_t)ctx->sm_count);
     OzArgs args{X->d.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, mts, vt, op->oz_aoff.p,
-                op->oz_mats.p, op->oz_row_exp.p, op->oz_xexp.p, Yc, 512, ctx->status.p};
+                op->oz_mats.p, op->oz_row_exp.p, xexp, Yc, 512, ctx->status.p};
     const double frac = (double)ncell / me->n_cells;
     ProfScope prof(ctx, "cell_apply_f64_oz", 2.0 * m * (double)me->total_mat * frac,
                    8.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
-    k_cell_apply_oz<<<grid, OZ_THREADS, smem, ctx->stream>>>(args);
+    k_cell_apply_oz<<<grid, OZ_THREADS, smem, stream>>>(args);
     check_launch(ctx, "cell_apply_oz");
   }
 }

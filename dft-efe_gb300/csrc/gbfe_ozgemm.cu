@@ -594,19 +594,26 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
 }
 
 // out_o (N x mo, row-major) = Y_o (N x m, row-major) T (m x mo, column-major) for o < nops (<= 3)
+// per-row exponents of the rotation inputs (they depend on Y alone, so a
+// caller can issue this before T is known)
+void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N) {
+  ctx->oz_rexp.ensure((size_t)nops * N);
+  k_oz_rowexp<<<(unsigned)std::min<uint64_t>((nops * N + 7) / 8, (uint64_t)ctx->sm_count * 32), 256, 0,
+                ctx->stream>>>(Y[0], nops > 1 ? Y[1] : Y[0], nops > 2 ? Y[2] : Y[0], nops, m, N, ctx->oz_rexp.p);
+  count_launch(ctx, 1);
+}
+
 void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const double *const *Y, double *const *out,
-               uint32_t nops, uint64_t N) {
+               uint32_t nops, uint64_t N, bool rows_ready) {
   GBFE_REQUIRE(nops >= 1 && nops <= 3 && m > 0 && m <= (uint32_t)oz::K_EXACT && mo > 0, "oz_rotate: bad shape");
   set_attrs_once();
   const uint32_t kchunks = (m + KC - 1) / KC, col_tiles = (mo + OG_N - 1) / OG_N;
   const uint32_t row_tiles = (uint32_t)((N + 127) / 128);
-  ctx->oz_rexp.ensure((size_t)nops * N);
   ctx->oz_exp.ensure(mo);
   ctx->oz_tdig.ensure((size_t)col_tiles * kchunks * oz::S * OG_N * KC);
-  k_oz_rowexp<<<(unsigned)std::min<uint64_t>((nops * N + 7) / 8, (uint64_t)ctx->sm_count * 32), 256, 0,
-                ctx->stream>>>(Y[0], nops > 1 ? Y[1] : Y[0], nops > 2 ? Y[2] : Y[0], nops, m, N, ctx->oz_rexp.p);
+  if (!rows_ready) oz_rotate_rows(ctx, Y, m, nops, N);
   k_oz_build_t<<<col_tiles, 256, 0, ctx->stream>>>(T, m, mo, kchunks, ctx->oz_exp.p, ctx->oz_tdig.p);
-  count_launch(ctx, 2);
+  count_launch(ctx, 1);
   RotArgs args{};
   for (uint32_t o = 0; o < nops; ++o) {
     args.Y[o] = Y[o];

@@ -523,8 +523,7 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
     GBFE_CUDA(cudaMemcpyAsync(Y->d.p, R0->d.p, Y->count() * 8, cudaMemcpyDeviceToDevice, ctx->stream));
   } else {
     auto s3 = make_like(X, GBFE_F64);
-    apply_op(B, X, Y);
-    apply_op(A, X, s3.get());
+    apply_pair_f64(A, B, X, s3.get(), Y);
     d_axpby_blocked(ctx, 1.0, d_ones.p, s3.get(), -1.0, d_eig.p, Y, Y);  // Y = AX - lambda BX
   }
   const gbfe_mv *Yr = Y;
@@ -701,8 +700,7 @@ int residual_norms_impl(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X, const do
   gbfe_ctx *ctx = X->mesh->ctx;
   const uint32_t m = X->m;
   auto HX = make_like(X, GBFE_F64), MX = make_like(X, GBFE_F64), Rr = make_like(X, GBFE_F64);
-  apply_op(A, X, HX.get());
-  apply_op(B, X, MX.get());
+  apply_pair_f64(A, B, X, HX.get(), MX.get());
   std::vector<double> nOnes(m, -1.0);
   DevVec d_no(ctx, m), d_e(ctx, m);
   d_no.set(ctx, nOnes.data(), m);
@@ -753,8 +751,7 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   }
   {
     ProfScope prof(ctx, "pass_fp64_applies", 0.0, 0.0);
-    apply_op(B, st.Y.get(), st.MY.get());
-    apply_op(A, st.Y.get(), st.HY.get());
+    apply_pair_f64(A, B, st.Y.get(), st.HY.get(), st.MY.get());
   }
   // FP64 Gram matrices and rotations: the sliced tensor-core products when
   // the FP64 applies use them, else DGEMM
@@ -769,6 +766,8 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
     gram(ctx, st.Y.get(), st.MY.get(), st.SM.p);
     gram(ctx, st.Y.get(), st.HY.get(), st.SH.p);
   }
+  const double *rot_in[3] = {st.Y->d.p, st.HY->d.p, st.MY->d.p};
+  bool rows_ready = false;
   // potrf, L^-1 S_H L^-T, syevd, L^-T V: the m x m stages, timed as one block
   auto eig_prof = std::make_unique<ProfScope>(ctx, "eig_small_f64", 0.0, 0.0);
   const bool host_eig = ctx->small_eig_host && m <= SMALL_EIG_HOST_MAX;
@@ -780,7 +779,15 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
     std::vector<double> hL((size_t)m * m), hS((size_t)m * m);
     GBFE_CUDA(cudaMemcpyAsync(hL.data(), st.SM.p, hL.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
     GBFE_CUDA(cudaMemcpyAsync(hS.data(), st.SH.p, hS.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (!ctx->host_ev) GBFE_CUDA(cudaEventCreateWithFlags(&ctx->host_ev, cudaEventDisableTiming));
+    GBFE_CUDA(cudaEventRecord(ctx->host_ev, ctx->stream));
+    // the row exponents of the rotation inputs run on the device while the
+    // host works on the m x m block (the host waits for the download only)
+    if (oz_dense) {
+      oz_rotate_rows(ctx, rot_in, (uint32_t)m, 3, (uint64_t)N);
+      rows_ready = true;
+    }
+    GBFE_CUDA(cudaEventSynchronize(ctx->host_ev));
     const int info = host_cholesky(m, hL.data());
     if (info != 0) {
       msg = "LAPACK_ERROR: FAILED_CHOLESKY_FACTORIZATION (potrf info " + std::to_string(info) + ")";
@@ -837,9 +844,8 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   eig_prof.reset();
   const double *T = st.SH.p;
   if (oz_dense) {
-    const double *in[3] = {st.Y->d.p, st.HY->d.p, st.MY->d.p};
     double *out[3] = {X->d.p, st.HX->d.p, st.MX->d.p};
-    oz_rotate(ctx, T, (uint32_t)m, (uint32_t)m, in, out, 3, (uint64_t)N);
+    oz_rotate(ctx, T, (uint32_t)m, (uint32_t)m, rot_in, out, 3, (uint64_t)N, rows_ready);
   } else {
     ProfScope prof(ctx, "rotate_f64_dgemm", 6.0 * (double)N * m * m, 48.0 * (double)N * m);
     const double one = 1.0, zero = 0.0;
@@ -877,8 +883,7 @@ int ks_solve_fused(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe
   st.SM.alloc((size_t)m * m);
   st.SH.alloc((size_t)m * m);
   // initial residual of the input block: R = A X - Lambda B X
-  apply_op(A, X, st.HX.get());
-  apply_op(B, X, st.MX.get());
+  apply_pair_f64(A, B, X, st.HX.get(), st.MX.get());
   {
     std::vector<double> ones(m, 1.0);
     DevVec d_o(ctx, m), d_e(ctx, m);
