@@ -455,7 +455,12 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
 // rows_ready: oz_rotate_rows already ran for these Y since they last changed
 void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const double *const *Y, double *const *out,
                uint32_t nops, uint64_t N, bool rows_ready = false);
-void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N);
+void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N,
+                    bool pair12 = false);
+// X = Y T and R = HY T - MY T diag(eps) in one launch (2m <= 512)
+bool oz_rotate_residual_supported(gbfe_ctx *ctx, uint32_t m);
+void oz_rotate_residual(gbfe_ctx *ctx, const double *T, const double *eps, uint32_t m, const double *Y,
+                        const double *HY, const double *MY, double *X, double *R, uint64_t N, bool rows_ready);
 void build_oz_mats(gbfe_op *op);
 // xexp: column exponents of X computed beforehand (nullptr: computed here)
 void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc, const int *xexp = nullptr,

@@ -19,7 +19,9 @@
 //   * k_oz_rot: work item = (operand, 128 rows, 64 output columns); the m x m
 //     factor is sliced once per call (k_oz_build_t) and lands by bulk copies;
 //     Y rows are sliced by the producers with per-row exponents; one TMEM pass
-//     covers K = m <= 512.
+//     covers K = m <= 512.  An operand may be two row blocks side by side
+//     (K = 2m) with its own factor: the residual HY T - MY T diag(eps) of the
+//     rotated block is [HY | MY] [T; -T diag(eps)], one product.
 // Every wait is bounded (error status, no hang); TMEM is freed on every exit.
 #include "gbfe_internal.cuh"
 #include "gbfe_oz.cuh"
@@ -309,13 +311,15 @@ __global__ void k_oz_gram_final(const double *__restrict__ part, uint32_t na, ui
 // ---------------------------------------------------------------- rotation
 struct RotArgs {
   const double *Y[3];
+  const double *Y2[3];  // second K half of operand o (N x m, K = 2m), or nullptr (K = m)
   double *out[3];
-  uint32_t nops, m, mo;  // K = m inputs, mo output columns
+  const __nv_bfloat16 *Tdig[3];  // factor of operand o: [col tile][K chunk][slice][OG_N x KC]
+  const int *texp[3];            // its per-column exponents [mo]
+  uint32_t kchunks[3];           // its K chunks
+  uint32_t nops, m, mo;          // m: row width of each input block, mo output columns
   uint64_t N;
-  const int *rexp;  // [nops][N] row exponents
-  const __nv_bfloat16 *Tdig;  // [col tile][K chunk][slice][OG_N x KC]
-  const int *texp;            // [mo]
-  uint32_t row_tiles, col_tiles, kchunks;
+  const int *rexp;  // [nops][N] row exponents (over both halves of a K = 2m operand)
+  uint32_t row_tiles, col_tiles;
   int *status;
 };
 
@@ -368,12 +372,13 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
       for (uint32_t it = blockIdx.x; it < n_items && !*br.abort_flag; it += gridDim.x) {
         uint32_t op, rt, ct;
         decode(it, op, rt, ct);
-        for (uint32_t kc = 0; kc < a.kchunks; ++kc, ++q) {
+        const uint32_t nk = a.kchunks[op];
+        for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
           const uint32_t s = q % OG_STAGES;
           if (q >= OG_STAGES && !wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 51)) break;
           uint8_t *Bt = smem + s * OG_STAGE + oz::S * A_PART;
           mbar_arrive_expect_tx(&full_b[s], oz::S * B_PART);
-          const __nv_bfloat16 *src = a.Tdig + ((uint64_t)(ct * a.kchunks + kc) * oz::S) * (OG_N * KC);
+          const __nv_bfloat16 *src = a.Tdig[op] + ((uint64_t)(ct * nk + kc) * oz::S) * (OG_N * KC);
           for (int sl = 0; sl < oz::S; ++sl) bulk_g2s(Bt + sl * B_PART, src + (uint64_t)sl * OG_N * KC, B_PART, &full_b[s]);
         }
       }
@@ -388,7 +393,8 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
       for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
         if (li >= 1 && !wait(br.tempty, (li - 1) & 1, 52)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        for (uint32_t kc = 0; kc < a.kchunks; ++kc, ++q) {
+        const uint32_t nk = a.kchunks[it / (a.row_tiles * a.col_tiles)];
+        for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
           const uint32_t s = q % OG_STAGES;
           if (!wait(&br.full[s], (q / OG_STAGES) & 1, 53) || !wait(&full_b[s], (q / OG_STAGES) & 1, 54)) {
             ok = false;
@@ -418,8 +424,11 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
       const uint64_t row = (uint64_t)rt * 128 + ar;
       const bool rin = row < a.N;
       const double *src = rin ? a.Y[op] + row * a.m : nullptr;
+      const double *src2 = (rin && a.Y2[op]) ? a.Y2[op] + row * a.m : nullptr;
+      const uint32_t K = a.Y2[op] ? 2 * a.m : a.m;
       const int re = rin ? a.rexp[(uint64_t)op * a.N + row] : 0;
-      for (uint32_t kc = 0; kc < a.kchunks; ++kc, ++q) {
+      const uint32_t nk = a.kchunks[op];
+      for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
         const uint32_t s = q % OG_STAGES;
         if (q >= OG_STAGES) {
           ok = __all_sync(0xffffffffu, wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 55));
@@ -433,7 +442,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
 #pragma unroll
           for (int kk = 0; kk < 8; ++kk) {
             const uint32_t k = kc * KC + kb * 8 + kk;
-            v[kk] = (rin && k < a.m) ? __ldg(src + k) : 0.0;
+            v[kk] = (rin && k < K) ? __ldg(k < a.m ? src + k : src2 + (k - a.m)) : 0.0;
           }
           store_core_rows(At, A_PART, (ar / 8) * SBO + kb * LBO + (ar % 8) * 16, v, re);
         }
@@ -453,7 +462,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
         const uint32_t j0 = ct * OG_N + colh * 32 + cg * 16;
         int te[16];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) te[i] = (j0 + i < a.mo) ? a.texp[j0 + i] : 0;
+        for (int i = 0; i < 16; ++i) te[i] = (j0 + i < a.mo) ? a.texp[op][j0 + i] : 0;
         oz::combine16_to_scratch(tmem + ((quad * 32) << 16) + colh * 32 + cg * 16, OG_N, scr, lane, oe, te);
         const uint32_t j = lane % 16;
 #pragma unroll 4
@@ -489,9 +498,10 @@ __global__ void k_oz_colmax_final(const int *__restrict__ part, uint32_t nb, uin
   oz::colmax_final_block(part, nb, cols, ex);
 }
 
-// per-row exponents of the rotation inputs: one warp per row
+// per-row exponents of the rotation inputs: one warp per row.  pair12: two
+// operands, the second made of the rows of Y1 and Y2 side by side.
 __global__ void k_oz_rowexp(const double *__restrict__ Y0, const double *__restrict__ Y1,
-                            const double *__restrict__ Y2, uint32_t nops, uint32_t m, uint64_t N,
+                            const double *__restrict__ Y2, uint32_t nops, uint32_t m, uint64_t N, bool pair12,
                             int *__restrict__ rexp) {
   const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x / 32);
   const uint32_t lane = threadIdx.x % 32;
@@ -501,21 +511,31 @@ __global__ void k_oz_rowexp(const double *__restrict__ Y0, const double *__restr
     const double *Y = op == 0 ? Y0 : (op == 1 ? Y1 : Y2);
     int mx = oz::EXP_NONE;
     for (uint32_t j = lane; j < m; j += 32) mx = max(mx, oz::exp_bits(Y[row * m + j]));
+    if (pair12 && op == 1)
+      for (uint32_t j = lane; j < m; j += 32) mx = max(mx, oz::exp_bits(Y2[row * m + j]));
     mx = __reduce_max_sync(0xffffffffu, mx);
     if (lane == 0) rexp[w] = oz::exp_or_zero(mx);
   }
 }
 
-// slices of the m x mo column-major factor T as the B operand (rows = output
-// columns j, K = input index i) with per-column exponents
-__global__ void k_oz_build_t(const double *__restrict__ T, uint32_t m, uint32_t mo, uint32_t kchunks,
-                             int *__restrict__ texp, __nv_bfloat16 *__restrict__ out) {
+// entry (i, j) of the factor: T (m x mo, column-major), or with neg_scale the
+// 2m x mo factor [T; -T diag(neg_scale)]
+__device__ __forceinline__ double factor_at(const double *__restrict__ T, const double *__restrict__ neg_scale,
+                                            uint32_t m, uint32_t i, uint32_t j) {
+  return i < m ? T[i + (uint64_t)m * j] : -(T[(i - m) + (uint64_t)m * j] * neg_scale[j]);
+}
+
+// slices of the factor as the B operand (rows = output columns j, K = input
+// index i) with per-column exponents
+__global__ void k_oz_build_t(const double *__restrict__ T, const double *__restrict__ neg_scale, uint32_t m,
+                             uint32_t mo, uint32_t kchunks, int *__restrict__ texp, __nv_bfloat16 *__restrict__ out) {
   const uint32_t ct = blockIdx.x;  // one block per 64-column tile
+  const uint32_t K = neg_scale ? 2 * m : m;
   for (uint32_t jr = threadIdx.x; jr < OG_N; jr += blockDim.x) {
     const uint32_t j = ct * OG_N + jr;
     double mx = 0.0;
     if (j < mo)
-      for (uint32_t i = 0; i < m; ++i) mx = fmax(mx, fabs(T[i + (uint64_t)m * j]));
+      for (uint32_t i = 0; i < K; ++i) mx = fmax(mx, fabs(factor_at(T, neg_scale, m, i, j)));
     if (j < mo) texp[j] = oz::exponent_of(mx);
   }
   __syncthreads();
@@ -525,7 +545,7 @@ __global__ void k_oz_build_t(const double *__restrict__ T, uint32_t m, uint32_t 
     const uint32_t jr = rem / KC, kk = rem % KC;
     const uint32_t j = ct * OG_N + jr, i = kc * KC + kk;
     int d[oz::S] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (j < mo && i < m) oz::digits(T[i + (uint64_t)m * j], texp[j], d);
+    if (j < mo && i < K) oz::digits(factor_at(T, neg_scale, m, i, j), texp[j], d);
     const uint32_t pos = (jr / 8) * (KC / 8) * 64 + (kk / 8) * 64 + (jr % 8) * 8 + (kk % 8);
     __nv_bfloat16 *base = out + ((uint64_t)(ct * kchunks + kc) * oz::S) * per_slice;
 #pragma unroll
@@ -596,10 +616,14 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
 // out_o (N x mo, row-major) = Y_o (N x m, row-major) T (m x mo, column-major) for o < nops (<= 3)
 // per-row exponents of the rotation inputs (they depend on Y alone, so a
 // caller can issue this before T is known)
-void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N) {
+// (pair12: two operands, Y[0] and the rows of Y[1], Y[2] side by side, as
+// oz_rotate_residual takes them)
+void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N, bool pair12) {
+  if (pair12) nops = 2;
   ctx->oz_rexp.ensure((size_t)nops * N);
   k_oz_rowexp<<<(unsigned)std::min<uint64_t>((nops * N + 7) / 8, (uint64_t)ctx->sm_count * 32), 256, 0,
-                ctx->stream>>>(Y[0], nops > 1 ? Y[1] : Y[0], nops > 2 ? Y[2] : Y[0], nops, m, N, ctx->oz_rexp.p);
+                ctx->stream>>>(Y[0], nops > 1 ? Y[1] : Y[0], (nops > 2 || pair12) ? Y[2] : Y[0], nops, m, N, pair12,
+                               ctx->oz_rexp.p);
   count_launch(ctx, 1);
 }
 
@@ -611,30 +635,78 @@ void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const do
   const uint32_t row_tiles = (uint32_t)((N + 127) / 128);
   ctx->oz_exp.ensure(mo);
   ctx->oz_tdig.ensure((size_t)col_tiles * kchunks * oz::S * OG_N * KC);
-  if (!rows_ready) oz_rotate_rows(ctx, Y, m, nops, N);
-  k_oz_build_t<<<col_tiles, 256, 0, ctx->stream>>>(T, m, mo, kchunks, ctx->oz_exp.p, ctx->oz_tdig.p);
+  if (!rows_ready) oz_rotate_rows(ctx, Y, m, nops, N, false);
+  k_oz_build_t<<<col_tiles, 256, 0, ctx->stream>>>(T, nullptr, m, mo, kchunks, ctx->oz_exp.p, ctx->oz_tdig.p);
   count_launch(ctx, 1);
   RotArgs args{};
   for (uint32_t o = 0; o < nops; ++o) {
     args.Y[o] = Y[o];
     args.out[o] = out[o];
+    args.Tdig[o] = ctx->oz_tdig.p;
+    args.texp[o] = ctx->oz_exp.p;
+    args.kchunks[o] = kchunks;
   }
   args.nops = nops;
   args.m = m;
   args.mo = mo;
   args.N = N;
   args.rexp = ctx->oz_rexp.p;
-  args.Tdig = ctx->oz_tdig.p;
-  args.texp = ctx->oz_exp.p;
   args.row_tiles = row_tiles;
   args.col_tiles = col_tiles;
-  args.kchunks = kchunks;
   args.status = ctx->status.p;
   const uint32_t items = nops * row_tiles * col_tiles;
   const uint32_t grid = std::min<uint32_t>(items, (uint32_t)ctx->sm_count);
   ProfScope prof(ctx, "rotate_f64_oz", 2.0 * (double)N * m * mo * nops, 8.0 * (double)N * (m + mo) * nops);
   k_oz_rot<<<grid, OG_THREADS, OG_SMEM, ctx->stream>>>(args);
   check_launch(ctx, "oz_rotate");
+}
+
+bool oz_rotate_residual_supported(gbfe_ctx *ctx, uint32_t m) { return oz_gemm_supported(ctx, 2 * m); }
+
+// X = Y T and R = HY T - MY T diag(eps) (all N x m row-major, T m x m
+// column-major, eps on the device) in one launch: R is the product of the rows
+// [HY | MY] (K = 2m) with the factor [T; -T diag(eps)], so the rotated HY and
+// MY are never stored.  rows_ready: oz_rotate_rows(..., pair12 = true) ran on
+// these blocks already.
+void oz_rotate_residual(gbfe_ctx *ctx, const double *T, const double *eps, uint32_t m, const double *Y,
+                        const double *HY, const double *MY, double *X, double *R, uint64_t N, bool rows_ready) {
+  GBFE_REQUIRE(m > 0 && oz_rotate_residual_supported(ctx, m), "oz_rotate_residual: bad shape");
+  set_attrs_once();
+  const uint32_t k0 = (m + KC - 1) / KC, k1 = (2 * m + KC - 1) / KC, col_tiles = (m + OG_N - 1) / OG_N;
+  const uint32_t row_tiles = (uint32_t)((N + 127) / 128);
+  const size_t fac0 = (size_t)col_tiles * k0 * oz::S * OG_N * KC;
+  ctx->oz_exp.ensure(2 * (size_t)m);
+  ctx->oz_tdig.ensure(fac0 + (size_t)col_tiles * k1 * oz::S * OG_N * KC);
+  const double *in[3] = {Y, HY, MY};
+  if (!rows_ready) oz_rotate_rows(ctx, in, m, 3, N, true);
+  k_oz_build_t<<<col_tiles, 256, 0, ctx->stream>>>(T, nullptr, m, m, k0, ctx->oz_exp.p, ctx->oz_tdig.p);
+  k_oz_build_t<<<col_tiles, 256, 0, ctx->stream>>>(T, eps, m, m, k1, ctx->oz_exp.p + m, ctx->oz_tdig.p + fac0);
+  count_launch(ctx, 2);
+  RotArgs args{};
+  args.Y[0] = Y;
+  args.Y[1] = HY;
+  args.Y2[1] = MY;
+  args.out[0] = X;
+  args.out[1] = R;
+  args.Tdig[0] = ctx->oz_tdig.p;
+  args.Tdig[1] = ctx->oz_tdig.p + fac0;
+  args.texp[0] = ctx->oz_exp.p;
+  args.texp[1] = ctx->oz_exp.p + m;
+  args.kchunks[0] = k0;
+  args.kchunks[1] = k1;
+  args.nops = 2;
+  args.m = m;
+  args.mo = m;
+  args.N = N;
+  args.rexp = ctx->oz_rexp.p;
+  args.row_tiles = row_tiles;
+  args.col_tiles = col_tiles;
+  args.status = ctx->status.p;
+  const uint32_t items = 2 * row_tiles * col_tiles;
+  const uint32_t grid = std::min<uint32_t>(items, (uint32_t)ctx->sm_count);
+  ProfScope prof(ctx, "rotate_f64_oz", 6.0 * (double)N * m * m, 40.0 * (double)N * m);
+  k_oz_rot<<<grid, OG_THREADS, OG_SMEM, ctx->stream>>>(args);
+  check_launch(ctx, "oz_rotate_residual");
 }
 
 }  // namespace gbfe

@@ -728,6 +728,8 @@ int chfsi_pass_impl(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbf
 //   Hp   = L^-1 S_H L^-T = V diag(eps) V^T              (syevd, FP64)
 //   T    = L^-T V;   X = Y T,  HX = HY T,  MX = MY T
 //   R    = HX - MX diag(eps)                            (next pass's filter input)
+// (with the sliced products, X and R come from one launch: R = [HY | MY]
+// [T; -T diag(eps)], and HX, MX are never stored)
 // This is the reference's filter -> Cholesky-GS -> Rayleigh-Ritz -> residual
 // sequence (ChebyshevFilteredEigenSolver.t.cpp:194-437,
 // KohnShamEigenSolver.t.cpp:574-684) with H X and M X carried through the
@@ -768,6 +770,8 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   }
   const double *rot_in[3] = {st.Y->d.p, st.HY->d.p, st.MY->d.p};
   bool rows_ready = false;
+  // X and the residual R straight from Y, HY, MY (the rotated HY, MY are not kept)
+  const bool oz_resid = oz_dense && oz_rotate_residual_supported(ctx, (uint32_t)m);
   // potrf, L^-1 S_H L^-T, syevd, L^-T V: the m x m stages, timed as one block
   auto eig_prof = std::make_unique<ProfScope>(ctx, "eig_small_f64", 0.0, 0.0);
   const bool host_eig = ctx->small_eig_host && m <= SMALL_EIG_HOST_MAX;
@@ -784,7 +788,7 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
     // the row exponents of the rotation inputs run on the device while the
     // host works on the m x m block (the host waits for the download only)
     if (oz_dense) {
-      oz_rotate_rows(ctx, rot_in, (uint32_t)m, 3, (uint64_t)N);
+      oz_rotate_rows(ctx, rot_in, (uint32_t)m, 3, (uint64_t)N, oz_resid);
       rows_ready = true;
     }
     GBFE_CUDA(cudaEventSynchronize(ctx->host_ev));
@@ -843,6 +847,15 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   }
   eig_prof.reset();
   const double *T = st.SH.p;
+  std::vector<double> nOnes(m, -1.0);
+  DevVec d_no(ctx, m), d_e(ctx, m);
+  d_e.set(ctx, eig_h, m);
+  if (oz_resid) {
+    oz_rotate_residual(ctx, T, d_e.p, (uint32_t)m, st.Y->d.p, st.HY->d.p, st.MY->d.p, X->d.p, st.R->d.p,
+                       (uint64_t)N, rows_ready);
+    host_coldots(ctx, st.R.get(), st.R.get(), res_h, true);
+    return GBFE_OK;
+  }
   if (oz_dense) {
     double *out[3] = {X->d.p, st.HX->d.p, st.MX->d.p};
     oz_rotate(ctx, T, (uint32_t)m, (uint32_t)m, rot_in, out, 3, (uint64_t)N, rows_ready);
@@ -858,10 +871,7 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
                             st.MX->d.p, m));
     count_launch(ctx, 3);
   }
-  std::vector<double> nOnes(m, -1.0);
-  DevVec d_no(ctx, m), d_e(ctx, m);
   d_no.set(ctx, nOnes.data(), m);
-  d_e.set(ctx, eig_h, m);
   // R = HX - MX diag(eps)   (getLinearEigenSolveResidual's axpbyBlocked with the sign flipped)
   d_axpby_blocked(ctx, -1.0, d_no.p, st.HX.get(), -1.0, d_e.p, st.MX.get(), st.R.get());
   host_coldots(ctx, st.R.get(), st.R.get(), res_h, true);

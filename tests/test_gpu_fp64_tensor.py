@@ -98,6 +98,11 @@ def test_ks_solve_with_fp64_tensor_products(gpu_ctx, small_problem):
         gpu_ctx.check_status()
         assert rc == 0
         res[key] = eig
+        # the residual norms the solver returns (with the sliced products: R
+        # straight from [HY | MY] [T; -T diag(eps)]) against plain FP64 applies
+        # on the returned block: 1e-11 absolute (the tolerance is 1e-8)
+        rr = api.eigen_residual_norms(H, Mo, X, eig)
+        assert np.abs(rr - r).max() <= 1e-11, (key, rr, r)
     assert np.abs(res["tensor"][:6] - res["fma"][:6]).max() <= 1e-8
     assert np.abs(res["tensor_cells"][:6] - res["fma"][:6]).max() <= 1e-8
     assert np.abs(res["mixed_tensor"][:6] - res["fma"][:6]).max() <= 1e-6
