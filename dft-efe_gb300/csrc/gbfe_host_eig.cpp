@@ -34,11 +34,14 @@ namespace {
 
 // Fork-join pool for the row- and column-independent parts of the m x m block
 // (the accumulation of the QR rotations into the eigenvectors, the triangular
-// solves).  HOST_THREADS - 1 workers; a worker spins on the job counter for a
-// while after each job (the next one comes a few milliseconds later, one per
-// ChFSI pass) and then sleeps on a condition variable.  A job's split depends
-// only on the problem size, never on timing, so results are the same
-// whatever thread runs which part.
+// solves).  HOST_THREADS - 1 workers.  While the pool is armed (a caller about
+// to run a whole m x m block: host_pool_arm) the workers spin on the job
+// counter, so consecutive jobs start without a wake-up; otherwise a worker
+// spins briefly after a job and then sleeps on a condition variable, so the
+// pool burns no CPU time between blocks (on a host with a CPU quota, idle
+// spinning is charged like work and can get the whole process throttled).  A
+// job's split depends only on the problem size, never on timing, so results
+// are the same whatever thread runs which part.
 constexpr int HOST_THREADS = 4;
 
 class HostPool {
@@ -65,6 +68,14 @@ class HostPool {
     f(0);
     while (pending_.load(std::memory_order_acquire) != 0) std::this_thread::yield();
   }
+  void arm(bool on) {
+    if (workers_.empty()) return;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      armed_.store(on, std::memory_order_release);
+    }
+    if (on) cv_.notify_all();
+  }
   ~HostPool() {
     {
       std::lock_guard<std::mutex> lk(mu_);
@@ -84,13 +95,18 @@ class HostPool {
   void loop(int part) {
     uint64_t seen = 0;
     for (;;) {
-      // spin ~2 ms for the next job, then sleep
+      // spin while armed, else ~200 us after a job; then sleep until a job
+      // comes or the pool is armed
       const auto t0 = std::chrono::steady_clock::now();
       while (gen_.load(std::memory_order_acquire) == seen &&
-             std::chrono::steady_clock::now() - t0 < std::chrono::milliseconds(2))
+             (armed_.load(std::memory_order_acquire) ||
+              std::chrono::steady_clock::now() - t0 < std::chrono::microseconds(200)))
         std::this_thread::yield();
       std::unique_lock<std::mutex> lk(mu_);
-      cv_.wait(lk, [&] { return gen_.load(std::memory_order_acquire) != seen; });
+      cv_.wait(lk, [&] {
+        return gen_.load(std::memory_order_acquire) != seen || armed_.load(std::memory_order_acquire);
+      });
+      if (gen_.load(std::memory_order_acquire) == seen) continue;  // armed, no job yet: spin
       seen = gen_.load(std::memory_order_acquire);
       if (stop_) return;
       const std::function<void(int)> *job = job_;
@@ -105,6 +121,7 @@ class HostPool {
   std::condition_variable cv_;
   std::atomic<uint64_t> gen_{0};
   std::atomic<int> pending_{0};
+  std::atomic<bool> armed_{false};
   const std::function<void(int)> *job_ = nullptr;
   int parts_ = 0;
   bool stop_ = false;
@@ -306,6 +323,8 @@ int host_sym_eig(int n, double *a, double *w) {
 // Returns 0, or k + 1 when the leading minor of order k + 1 is not positive
 // definite (LAPACK potrf's info).  Column-oriented (left-looking) elimination:
 // every inner loop runs down a contiguous column.
+void host_pool_arm(bool on) { HostPool::get().arm(on); }
+
 int host_cholesky(int n, double *a) {
   const size_t N = (size_t)n;
   for (int k = 0; k < n; ++k) {

@@ -445,6 +445,9 @@ bool oz_supported(const gbfe_mesh *me);
 // dense symmetric eigen-decomposition on the host (gbfe_host_eig.cpp)
 int host_sym_eig(int n, double *a, double *w);
 int host_cholesky(int n, double *a);
+// keep the host pool's workers spinning (true) for the m x m block about to
+// run, or let them sleep between blocks (false)
+void host_pool_arm(bool on);
 void host_trsm_lower(int n, const double *L, double *B);
 void host_trsm_lower_t(int n, const double *L, double *B);
 void host_sandwich(int n, const double *L, double *A);

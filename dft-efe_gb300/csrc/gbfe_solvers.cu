@@ -758,6 +758,17 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   // FP64 Gram matrices and rotations: the sliced tensor-core products when
   // the FP64 applies use them, else DGEMM
   const bool oz_dense = ctx->fp64_tc && ctx->fp64_tc_dense && oz_gemm_supported(ctx, (uint32_t)m);
+  // the host pool's workers wake while the device forms the Gram matrices and
+  // sleep again after the m x m block
+  struct PoolArm {
+    bool on;
+    explicit PoolArm(bool o) : on(o) {
+      if (on) host_pool_arm(true);
+    }
+    ~PoolArm() {
+      if (on) host_pool_arm(false);
+    }
+  } pool_arm(ctx->small_eig_host && m <= SMALL_EIG_HOST_MAX);
   if (oz_dense) {
     // S = (MY|HY)^T Y: the transposes of Y^T MY and Y^T HY (both symmetric)
     const double *As[2] = {st.MY->d.p, st.HY->d.p};
@@ -808,6 +819,8 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
       return GBFE_ERR_LAPACK;
     }
     host_trsm_lower_t(m, hL.data(), hS.data());  // T = L^-T V
+    host_pool_arm(false);
+    pool_arm.on = false;
     h2d_staged(ctx, ctx->pin_small, st.SH.p, hS.data(), hS.size() * 8);
   } else {
     int lwork = 0;
