@@ -192,6 +192,14 @@ __device__ __forceinline__ float level_weight(int g) { return __int_as_float((12
 // sum_g L_g 2^-7g (g = 9 .. 2, smallest level first) for 16 columns of this
 // thread's TMEM lane; level g's accumulator at taddr + (g - 2) * stride.  The
 // load of the next level is in flight while the current one is added.
+// Levels 9, 8, 7 are summed with plain FP32 fused multiply-adds: with
+// |L_g| <= K 2^15 their partial sum is below K 2^-34 and its two roundings
+// below K 2^-57, i.e. 2^-55 of the product bound K/4 (in the same units); the
+// operand truncation already contributes 2^-54.  Levels 6 .. 2 go through
+// error-free TwoSums into the (hi, lo) pair.  EXACT_FROM = 9: every level
+// through TwoSums (the Gram kernel: its FP64 chunk accumulators leave no
+// registers for the shorter schedule).
+template <int EXACT_FROM = 6>
 __device__ __forceinline__ void combine16(uint32_t taddr, uint32_t stride, float *hi, float *lo) {
 #pragma unroll
   for (int q = 0; q < 16; ++q) hi[q] = lo[q] = 0.f;
@@ -199,12 +207,17 @@ __device__ __forceinline__ void combine16(uint32_t taddr, uint32_t stride, float
   auto step = [&](uint32_t(&cur)[16], uint32_t(&nxt)[16], int g) {
     if (g > 2) tc::tmem_ld16_issue(taddr + (uint32_t)(g - 3) * stride, nxt);
     const float w = level_weight(g);
+    if (g > EXACT_FROM) {
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      float s2, e2;
-      two_sum(hi[q], __uint_as_float(cur[q]) * w, s2, e2);
-      hi[q] = s2;
-      lo[q] += e2;
+      for (int q = 0; q < 16; ++q) hi[q] = fmaf(__uint_as_float(cur[q]), w, hi[q]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        float s2, e2;
+        two_sum(hi[q], __uint_as_float(cur[q]) * w, s2, e2);
+        hi[q] = s2;
+        lo[q] += e2;
+      }
     }
     if (g > 2) tc::tmem_wait_ld16(nxt);
   };

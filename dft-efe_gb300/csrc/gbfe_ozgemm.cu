@@ -83,9 +83,9 @@ __device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t abase, uint
   }
 }
 
-// sum_g L_g 2^-7g for 16 columns of this thread's TMEM lane
+// sum_g L_g 2^-7g for 16 columns of this thread's TMEM lane (every level exact)
 __device__ __forceinline__ void combine16(uint32_t taddr, float *hi, float *lo) {
-  oz::combine16(taddr, OG_N, hi, lo);
+  oz::combine16<9>(taddr, OG_N, hi, lo);
 }
 
 struct Barriers {
