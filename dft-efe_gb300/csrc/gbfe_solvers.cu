@@ -99,6 +99,19 @@ __global__ void k_cheb_step_dev(uint64_t n, uint32_t m, const double *__restrict
   }
 }
 
+// Start of the mixed filter from a residual R0 held in FP64, in one sweep:
+// Yf = float(R0), RN = alpha1 Yf (the same expression as k_axpby<float> with
+// b = 0), R = 0 -- what a copy, a conversion, an axpby and a fill would leave
+__global__ void k_filter_start_mixed(uint64_t n, double a, const double *__restrict__ R0, float *__restrict__ Yf,
+                                     float *__restrict__ RN, float *__restrict__ R) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+    const float y = (float)R0[t];
+    Yf[t] = y;
+    RN[t] = (float)a * y + (float)0.0 * y;
+    R[t] = 0.f;
+  }
+}
+
 // Y = R + eF2[j] * X, with R in FP32 and X, Y in FP64 (mixed filter epilogue)
 __global__ void k_cheb_final_mixed(uint64_t n, uint32_t m, const float *__restrict__ R, const double *__restrict__ eF2,
                                    const double *__restrict__ X, double *__restrict__ Y, const FastDiv fm) {
@@ -517,7 +530,16 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
   h2d_staged(ctx, w.pin_coef, w.coef.p, coef.data(), coef.size() * 8);
   gbfe_mv *s1 = w.s1.get(), *s2 = w.s2.get();
   std::unique_ptr<gbfe_mv> &R = w.R, &RN = w.RN;
-  if (R0) {
+  const gbfe_mv *Yr = Y;
+  if (R0 && mixed) {
+    // the caller holds A X - Lambda B X in FP64: Y itself is only written by
+    // the final step, so the FP32 start reads R0 directly
+    const uint64_t n0 = X->count();
+    k_filter_start_mixed<<<sgrid(ctx, n0), 256, 0, ctx->stream>>>(n0, s.alpha1_init, R0->d.p, w.Yf->f.p, RN->f.p,
+                                                                  R->f.p);
+    check_launch(ctx, "filter_start_mixed");
+    Yr = w.Yf.get();
+  } else if (R0) {
     // the caller already holds A X - Lambda B X (the residual of the previous
     // Rayleigh-Ritz step), so the two initial applies are skipped
     GBFE_CUDA(cudaMemcpyAsync(Y->d.p, R0->d.p, Y->count() * 8, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -526,13 +548,14 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
     apply_pair_f64(A, B, X, s3.get(), Y);
     d_axpby_blocked(ctx, 1.0, d_ones.p, s3.get(), -1.0, d_eig.p, Y, Y);  // Y = AX - lambda BX
   }
-  const gbfe_mv *Yr = Y;
-  if (mixed) {
-    convert_mv(ctx, Y, w.Yf.get());
-    Yr = w.Yf.get();
+  if (!(R0 && mixed)) {
+    if (mixed) {
+      convert_mv(ctx, Y, w.Yf.get());
+      Yr = w.Yf.get();
+    }
+    d_axpby(ctx, s.alpha1_init, Yr, 0.0, Yr, RN.get());  // ResidualNew = alpha1 * Y
+    fill_mv(ctx, R.get(), 0.0);
   }
-  d_axpby(ctx, s.alpha1_init, Yr, 0.0, Yr, RN.get());  // ResidualNew = alpha1 * Y
-  fill_mv(ctx, R.get(), 0.0);
   const uint64_t n = X->count();
   // the d-1 recurrence steps: pointers and table offsets are fixed for a given
   // degree, the scalars come from device tables -> one graph for every pass
