@@ -210,12 +210,28 @@ __global__ void k_assemble_vec(const T *__restrict__ Yc, uint32_t m, uint64_t n_
     const uint32_t p0 = slot_ptr[i], e = slot_ptr[i + 1];
     if (!(is_row && is_row[i]) && p0 < e) {
       // the first slot starts the sum (no add to zero: for FP64 blocks the
-      // adds run on GB300's narrow FP64 pipe)
-      acc = *reinterpret_cast<const V *>(Yc + (uint64_t)slot[p0] * m + v);
-      for (uint32_t p = p0 + 1; p < e; ++p) {
-        const V y = *reinterpret_cast<const V *>(Yc + (uint64_t)slot[p] * m + v);
+      // adds run on GB300's narrow FP64 pipe); slots in batches of four: the
+      // indices, then the rows (four loads in flight), then the adds in slot order
+      bool first = true;
+      for (uint32_t p = p0; p < e; p += 4) {
+        uint32_t sl[4];
+        V y[4];
 #pragma unroll
-        for (int w = 0; w < W; ++w) acc.x[w] = acc.x[w] + y.x[w];
+        for (int u = 0; u < 4; ++u) sl[u] = p + u < e ? slot[p + u] : 0u;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (p + u < e) y[u] = *reinterpret_cast<const V *>(Yc + (uint64_t)sl[u] * m + v);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (p + u < e) {
+            if (first) {
+              acc = y[u];
+              first = false;
+            } else {
+#pragma unroll
+              for (int w = 0; w < W; ++w) acc.x[w] = acc.x[w] + y[u].x[w];
+            }
+          }
       }
     }
     *reinterpret_cast<V *>(Y + i * m + v) = acc;

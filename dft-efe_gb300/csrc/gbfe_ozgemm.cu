@@ -223,35 +223,29 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
       for (uint32_t c = c0; c < c1 && ok; ++c, ++nchunk) {
         for (uint32_t st = 0; st < STAGES_PER_CHUNK; ++st, ++q) {
           const uint32_t s = q % OG_STAGES;
+          const uint64_t k0 = (uint64_t)c * CHUNK + st * KC;
+          // A: 16 K values of row ar (two core rows); B: 8 K values of row bj
+          // (one core row) -- loaded before the wait for the ring stage
+          double va[16], vb[8];
+#pragma unroll
+          for (int kk = 0; kk < 16; ++kk) {
+            const uint64_t k = k0 + ah * 16 + kk;
+            va[kk] = (arow && k < a.N) ? __ldg(Asrc + k * am) : 0.0;
+          }
+#pragma unroll
+          for (int kk = 0; kk < 8; ++kk) {
+            const uint64_t k = k0 + bq * 8 + kk;
+            vb[kk] = (brow && k < a.N) ? __ldg(a.B + k * a.mb + J) : 0.0;
+          }
           if (q >= OG_STAGES) {
             ok = __all_sync(0xffffffffu, wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 43));
             if (!ok) break;
           }
           uint8_t *At = smem + s * OG_STAGE;
           uint8_t *Bt = At + oz::S * A_PART;
-          const uint64_t k0 = (uint64_t)c * CHUNK + st * KC;
-          // A: 16 K values of row ar (two core rows)
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const uint32_t kb = ah * 2 + h;
-            double v[8];
-#pragma unroll
-            for (int kk = 0; kk < 8; ++kk) {
-              const uint64_t k = k0 + kb * 8 + kk;
-              v[kk] = (arow && k < a.N) ? __ldg(Asrc + k * am) : 0.0;
-            }
-            store_core_rows(At, A_PART, (ar / 8) * SBO + kb * LBO + (ar % 8) * 16, v, ae);
-          }
-          // B: 8 K values of row bj (one core row)
-          {
-            double v[8];
-#pragma unroll
-            for (int kk = 0; kk < 8; ++kk) {
-              const uint64_t k = k0 + bq * 8 + kk;
-              v[kk] = (brow && k < a.N) ? __ldg(a.B + k * a.mb + J) : 0.0;
-            }
-            store_core_rows(Bt, B_PART, (bj / 8) * SBO + bq * LBO + (bj % 8) * 16, v, be);
-          }
+          store_core_rows(At, A_PART, (ar / 8) * SBO + (ah * 2) * LBO + (ar % 8) * 16, va, ae);
+          store_core_rows(At, A_PART, (ar / 8) * SBO + (ah * 2 + 1) * LBO + (ar % 8) * 16, va + 8, ae);
+          store_core_rows(Bt, B_PART, (bj / 8) * SBO + bq * LBO + (bj % 8) * 16, vb, be);
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           __syncwarp();
           if (lane == 0) mbar_arrive(&br.full[s]);
@@ -423,13 +417,15 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
       decode(it, op, rt, ct);
       const uint64_t row = (uint64_t)rt * 128 + ar;
       const bool rin = row < a.N;
-      const double *src = rin ? a.Y[op] + row * a.m : nullptr;
-      const double *src2 = (rin && a.Y2[op]) ? a.Y2[op] + row * a.m : nullptr;
+      const double *src = a.Y[op] + row * a.m;
+      const double *src2 = a.Y2[op] ? a.Y2[op] + row * a.m : src;
       const uint32_t K = a.Y2[op] ? 2 * a.m : a.m;
       const int re = rin ? a.rexp[(uint64_t)op * a.N + row] : 0;
       const uint32_t nk = a.kchunks[op];
       for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
         const uint32_t s = q % OG_STAGES;
+        // (loading these rows before the stage wait, or a chunk ahead,
+        // measured slower for this kernel)
         if (q >= OG_STAGES) {
           ok = __all_sync(0xffffffffu, wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 55));
           if (!ok) break;
@@ -437,14 +433,14 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
         uint8_t *At = smem + s * OG_STAGE;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const uint32_t kb = ah * 2 + h;
+          // 8 K values of row ar: one core row
           double v[8];
 #pragma unroll
           for (int kk = 0; kk < 8; ++kk) {
-            const uint32_t k = kc * KC + kb * 8 + kk;
+            const uint32_t k = kc * KC + (ah * 2 + h) * 8 + kk;
             v[kk] = (rin && k < K) ? __ldg(k < a.m ? src + k : src2 + (k - a.m)) : 0.0;
           }
-          store_core_rows(At, A_PART, (ar / 8) * SBO + kb * LBO + (ar % 8) * 16, v, re);
+          store_core_rows(At, A_PART, (ar / 8) * SBO + (ah * 2 + h) * LBO + (ar % 8) * 16, v, re);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
