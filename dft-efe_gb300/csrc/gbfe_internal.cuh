@@ -454,7 +454,7 @@ void host_sandwich(int n, const double *L, double *A);
 // FP64-accurate sliced tensor-core products of the subspace stages (gbfe_ozgemm.cu)
 bool oz_gemm_supported(gbfe_ctx *ctx, uint32_t m);
 void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, const double *B, uint32_t mb,
-             uint64_t N, double *const *S);
+             uint64_t N, double *const *S, const int *bexp = nullptr);
 // rows_ready: oz_rotate_rows already ran for these Y since they last changed
 void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const double *const *Y, double *const *out,
                uint32_t nops, uint64_t N, bool rows_ready = false);

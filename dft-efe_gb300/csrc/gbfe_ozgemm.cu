@@ -566,9 +566,10 @@ bool oz_gemm_supported(gbfe_ctx *ctx, uint32_t m) {
   return ctx->cc_major >= 10 && m > 0 && m <= (uint32_t)oz::K_EXACT;
 }
 
-// S_o (ma x mb, column-major) = A_o^T B for o < na (na <= 2); A_o: N x ma, B: N x mb, row-major blocks
+// S_o (ma x mb, column-major) = A_o^T B for o < na (na <= 2); A_o: N x ma, B: N x mb, row-major blocks.
+// bexp: the per-column exponents of B computed beforehand (nullptr: here)
 void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, const double *B, uint32_t mb,
-             uint64_t N, double *const *S) {
+             uint64_t N, double *const *S, const int *bexp) {
   GBFE_REQUIRE(na >= 1 && na <= 2 && ma > 0 && mb > 0, "oz_gram: bad shape");
   set_attrs_once();
   const uint32_t rows = na * ma;
@@ -589,10 +590,15 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
                                                                   ctx->oz_ipart.p);
   k_oz_colmax_final<<<(rows + 31) / 32, oz::COLMAX_FINAL_THREADS, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, rows,
                                                                                     ctx->oz_exp.p);
-  k_oz_colmax_partial<<<nb, oz::COLMAX_THREADS, 0, ctx->stream>>>(B, B, 1, mb, N, ctx->oz_ipart.p);
-  k_oz_colmax_final<<<(mb + 31) / 32, oz::COLMAX_FINAL_THREADS, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, mb,
-                                                                                  ctx->oz_exp.p + rows);
-  count_launch(ctx, 4);
+  count_launch(ctx, 2);
+  if (bexp) {
+    GBFE_CUDA(cudaMemcpyAsync(ctx->oz_exp.p + rows, bexp, sizeof(int) * mb, cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    k_oz_colmax_partial<<<nb, oz::COLMAX_THREADS, 0, ctx->stream>>>(B, B, 1, mb, N, ctx->oz_ipart.p);
+    k_oz_colmax_final<<<(mb + 31) / 32, oz::COLMAX_FINAL_THREADS, 0, ctx->stream>>>(ctx->oz_ipart.p, nb, mb,
+                                                                                    ctx->oz_exp.p + rows);
+    count_launch(ctx, 2);
+  }
   ctx->oz_part.ensure((size_t)items * TILE);
   GramArgs args{A[0], na > 1 ? A[1] : A[0], na, ma, B, mb, N, ctx->oz_exp.p, ctx->oz_exp.p + rows, row_tiles,
                 col_tiles, splits, chunks, cps, ctx->oz_part.p, ctx->status.p};

@@ -796,7 +796,9 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
     // S = (MY|HY)^T Y: the transposes of Y^T MY and Y^T HY (both symmetric)
     const double *As[2] = {st.MY->d.p, st.HY->d.p};
     double *Ss[2] = {st.SM.p, st.SH.p};
-    oz_gram(ctx, As, 2, (uint32_t)m, st.Y->d.p, (uint32_t)m, (uint64_t)N, Ss);
+    // the sliced apply of A on Y left Y's column exponents with A
+    const int *yexp = (A->oz_aoff.p && A->oz_xexp.p && A->oz_xexp.n >= (size_t)m) ? A->oz_xexp.p : nullptr;
+    oz_gram(ctx, As, 2, (uint32_t)m, st.Y->d.p, (uint32_t)m, (uint64_t)N, Ss, yexp);
   } else {
     ProfScope prof(ctx, "gram_f64_dgemm", 4.0 * (double)N * m * m, 24.0 * (double)N * m);
     gram(ctx, st.Y.get(), st.MY.get(), st.SM.p);
