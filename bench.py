@@ -104,7 +104,6 @@ class ClockSampler:
 
     def __enter__(self):
         try:
-            self.f = open(self.path, "w") if self.path else subprocess.DEVNULL
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                                           "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
                                          text=True)
@@ -346,7 +345,7 @@ def run_gpu(args, cfg_name, rank, world):
     ctx.set_profiling(False)
     launches0 = ctx.kernel_launches()
     lat, errs, passes, ok, eigs, rcs, ress = [], [], [], 0, [], [], []
-    clocks = ClockSampler(ROOT / "gpurun_out" / "bench_clocks.csv" if (ROOT / "gpurun_out").is_dir() else None)
+    clocks = ClockSampler(Path(args.clocks_csv) if args.clocks_csv else None)
     with clocks:  # sampler runs across the timed region, started and stopped outside it
         time.sleep(0.5)
         barrier()
@@ -437,7 +436,7 @@ def run_gpu(args, cfg_name, rank, world):
                 h2d=prob.n_dofs * m * 8, d2h=prob.n_dofs * m * 8 + 2 * m * 8)
 
 
-# ----------------------------------------------------------------------------- batched Poisson (configs[3])
+# ----------------------------------------------------------------------------- batched Poisson (64 instances)
 def _cpu_poisson_worker(args):
     """Oracle CGLinearSolver restatement on one Poisson instance (FP64, one thread)."""
     i, seed = args
@@ -480,7 +479,7 @@ def run_poisson(args):
     ctx.synchronize()
     l0 = ctx.kernel_launches()
     lat = []
-    clocks = ClockSampler(ROOT / "gpurun_out" / "bench_clocks_poisson.csv" if (ROOT / "gpurun_out").is_dir() else None)
+    clocks = ClockSampler(Path(args.clocks_csv) if args.clocks_csv else None)
     with clocks:
         time.sleep(0.3)
         ctx.synchronize()
@@ -553,7 +552,7 @@ def run_poisson(args):
     print(json.dumps(line))
 
 
-# ----------------------------------------------------------------------------- serving stream (configs[4])
+# ----------------------------------------------------------------------------- serving stream (KS and Poisson requests)
 def run_serving(args):
     import gbfe.enrichment as E
     import gbfe.mesh as M
@@ -688,6 +687,7 @@ def main():
                     help="FP64 solves; the first also pays one-time library loads and is not counted when more follow")
     ap.add_argument("--cpu-procs", type=int, default=0, help="oracle processes for the CPU baseline (0: all cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--clocks-csv", default="", help="also write the nvidia-smi samples of the timed region here")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gbfe" else args.warmup
 
