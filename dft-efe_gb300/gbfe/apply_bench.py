@@ -35,6 +35,8 @@ def main() -> None:
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--filter", type=int, default=0,
                     help="time the mixed residual Chebyshev filter of this degree instead of one apply")
+    ap.add_argument("--passes", type=int, default=0,
+                    help="time this many fused mixed ChFSI passes (degree 16, sliced FP64 stages) instead")
     args = ap.parse_args()
     w = WORKLOADS[args.config]
     m = args.m or w["m"]
@@ -49,6 +51,8 @@ def main() -> None:
     basis = api.FEBasisManager.from_problem(ctx, prob)
     if args.filter:
         return filter_bench(args, prob, ctx, basis, m)
+    if args.passes:
+        return passes_bench(args, prob, ctx, basis, m)
     mixed = args.precision not in ("f64", "f64_tensor")
     H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=mixed, fp64_tensor=args.precision == "f64_tensor")
     if args.precision == "f64_tensor":
@@ -110,6 +114,35 @@ def filter_bench(args, prob, ctx, basis, m) -> None:
     ctx.check_status()
     print(json.dumps({"config": args.config, "filter_degree": args.filter, "m": m, "n_dofs": prob.n_dofs,
                       "filter_ms": (time.perf_counter() - t0) / args.reps * 1e3}))
+
+
+def passes_bench(args, prob, ctx, basis, m) -> None:
+    """A fixed number of fused mixed ChFSI passes (the bench's solve, cut
+    short): mixed filter of degree 16, sliced FP64 applies, Gram products and
+    the rotation with the residual."""
+    H = api.KohnShamOperatorContextFE(basis, prob.H, mixed=True, fp64_tensor=True)
+    Mo = api.CFEOverlapOperatorContext(basis, prob.M, mixed=True, fp64_tensor=True)
+    if "enr_block_inv" in prob.extra:
+        Mi = api.OrthoEFEOverlapInverseOpContextGLL(basis, prob.m_gll_diag, prob.extra["enr_begin"],
+                                                    prob.extra["enr_block_inv"])
+    else:
+        Mi = api.CFEOverlapInverseOpContextGLL(basis, prob.m_gll_diag)
+    b = api.lanczos_bounds(H, Mo, Mi, 20, 7)
+    bounds = (b[0], b[0] + 0.1 * (b[1] - b[0]), b[1] + b[2] / 10)
+    X0 = M.random_block(prob.n_dofs, m, 1)
+    solver = api.KohnShamEigenSolver(max(1, 3 * m // 4), 16, args.passes, 1e-6, mixed=True, bounds=bounds,
+                                     fixed_passes=True, fp64_tensor=True)
+    ts = []
+    for _ in range(max(1, args.reps)):
+        X = api.MultiVector(basis, m, init=X0)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        solver.solve(H, X, Mo, Mi)
+        ctx.synchronize()
+        ts.append(time.perf_counter() - t0)
+    ctx.check_status()
+    print(json.dumps({"config": args.config, "passes": args.passes, "m": m, "n_dofs": prob.n_dofs,
+                      "ms_per_pass": min(ts) / args.passes * 1e3}))
 
 
 if __name__ == "__main__":
