@@ -788,6 +788,7 @@ int gbfe_ctx_destroy(gbfe_ctx *ctx) {
   if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
   if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
   if (ctx->host_ev) cudaEventDestroy(ctx->host_ev);
+  for (cudaGraphExec_t g : ctx->fw_exec_pool) cudaGraphExecDestroy(g);
   if (ctx->cusolver) cusolverDnDestroy(ctx->cusolver);
   if (ctx->cublas) cublasDestroy(ctx->cublas);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);

@@ -166,6 +166,9 @@ struct gbfe_ctx {
   cudaStream_t side_stream = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   cudaEvent_t host_ev = nullptr;  // the host waits on this one, not on the stream, when work follows a download
+  // instantiated filter-recurrence graphs no solve holds: the next capture of
+  // the same shape updates one in place instead of instantiating anew
+  std::vector<cudaGraphExec_t> fw_exec_pool;
   int split_groups = 1;      // 1: independent size groups of a cell product run concurrently
   cublasHandle_t cublas = nullptr;
   cusolverDnHandle_t cusolver = nullptr;

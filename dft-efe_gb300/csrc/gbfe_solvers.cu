@@ -448,6 +448,7 @@ struct FilterWork {
   DBuf<double> tab, coef;
   PinnedSlot pin_tab, pin_coef;
   cudaGraphExec_t exec = nullptr;
+  gbfe_ctx *owner = nullptr;  // the context whose pool takes exec back
   std::vector<GraphProf> prof;
   gbfe_ctx *prof_ctx = nullptr;  // replay whose event timings are not read yet
   uint64_t per_replay = 0;
@@ -474,7 +475,14 @@ struct FilterWork {
   }
   void drop_graph() {
     flush_prof();
-    if (exec) cudaGraphExecDestroy(exec);
+    // back to the context's pool once no replay of it is in flight (every
+    // replay is on the context stream); the pool keeps a few
+    if (exec) {
+      if (owner && owner->fw_exec_pool.size() < 4 && cudaStreamSynchronize(owner->stream) == cudaSuccess)
+        owner->fw_exec_pool.push_back(exec);
+      else
+        cudaGraphExecDestroy(exec);
+    }
     exec = nullptr;
     for (auto &g : prof) {
       cudaEventDestroy(g.e0);
@@ -599,7 +607,25 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
       if (e == cudaSuccess) e = e2;
     }
     ctx->capture_prof = nullptr;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&w.exec, graph, 0);
+    if (e == cudaSuccess) {
+      // a pooled graph of the same topology takes the new node parameters
+      // (every pointer and table of this capture); else a new instantiation
+      bool updated = false;
+      while (!updated && !ctx->fw_exec_pool.empty()) {
+        cudaGraphExec_t cand = ctx->fw_exec_pool.back();
+        ctx->fw_exec_pool.pop_back();
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(cand, graph, &info) == cudaSuccess) {
+          w.exec = cand;
+          updated = true;
+        } else {
+          (void)cudaGetLastError();
+          cudaGraphExecDestroy(cand);
+        }
+      }
+      if (!updated) e = cudaGraphInstantiate(&w.exec, graph, 0);
+      w.owner = ctx;
+    }
     if (graph) cudaGraphDestroy(graph);
     w.per_replay = ctx->launches - l0;
     ctx->launches = l0;

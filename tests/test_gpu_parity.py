@@ -364,6 +364,14 @@ def test_mixed_ks_solve_eigenvalues(gpu_ctx, small_problem):
     gpu_ctx.check_status()
     assert rc64 == 0 and rc32 == 0
     assert np.abs(e32[:nw] - e64[:nw]).max() <= 1e-6
+    # the same solve again: its filter graph is the previous solve's, updated
+    # in place with this solve's buffers -- the same bits
+    Xa = X.numpy().copy()
+    X.copy_from(X0)
+    rc2, e2, r2, n2 = api.KohnShamEigenSolver(nw, 12, 60, 1e-8, mixed=True, bounds=bounds).solve(H, X, Mo, Mi)
+    gpu_ctx.check_status()
+    assert rc2 == 0 and n2 == n32
+    assert np.array_equal(e2, e32) and np.array_equal(r2, r32) and np.array_equal(X.numpy(), Xa)
 
 
 def test_graph_replayed_filter_matches_eager(gpu_ctx, small_problem):
