@@ -50,22 +50,28 @@ class HostPool {
     static HostPool pool;
     return pool;
   }
-  // f(part) for part = 0 .. parts-1, parts <= HOST_THREADS; the caller runs part 0
+  // f(part) for part = 0 .. parts-1, parts <= HOST_THREADS.  The caller runs
+  // part 0 and then, like the workers, claims parts from a counter tagged with
+  // the job's generation: a part no worker has started (one that is asleep or
+  // was preempted) is run by the caller instead of waited for.
   void run(int parts, const std::function<void(int)> &f) {
     if (parts <= 1 || workers_.empty()) {
       for (int t = 0; t < parts; ++t) f(t);
       return;
     }
     std::lock_guard<std::mutex> serial(run_mu_);  // one job at a time
+    uint64_t g;
     {
       std::lock_guard<std::mutex> lk(mu_);
       job_ = &f;
       parts_ = parts;
-      pending_.store(parts - 1, std::memory_order_relaxed);
-      gen_.fetch_add(1, std::memory_order_release);
+      pending_.store(parts, std::memory_order_relaxed);
+      g = gen_.load(std::memory_order_relaxed) + 1;
+      next_.store(g << 32, std::memory_order_relaxed);
+      gen_.store(g, std::memory_order_release);
     }
     cv_.notify_all();
-    f(0);
+    claim_and_run(g, parts, f);
     while (pending_.load(std::memory_order_acquire) != 0) std::this_thread::yield();
   }
   void arm(bool on) {
@@ -112,8 +118,19 @@ class HostPool {
       const std::function<void(int)> *job = job_;
       const int parts = parts_;
       lk.unlock();
-      if (part < parts) (*job)(part);
-      if (part < parts) pending_.fetch_sub(1, std::memory_order_acq_rel);
+      claim_and_run(seen, parts, *job);
+    }
+  }
+  // run unclaimed parts of job generation g until none is left; a claim is a
+  // compare-and-swap on (generation << 32 | next part), so a thread holding a
+  // finished job's pointer can never claim a part of the next job
+  void claim_and_run(uint64_t g, int parts, const std::function<void(int)> &f) {
+    for (;;) {
+      uint64_t cur = next_.load(std::memory_order_acquire);
+      if ((cur >> 32) != g || (int)(cur & 0xffffffffu) >= parts) return;
+      if (!next_.compare_exchange_weak(cur, cur + 1, std::memory_order_acq_rel)) continue;
+      f((int)(cur & 0xffffffffu));
+      pending_.fetch_sub(1, std::memory_order_acq_rel);
     }
   }
   std::vector<std::thread> workers_;
@@ -121,6 +138,7 @@ class HostPool {
   std::condition_variable cv_;
   std::atomic<uint64_t> gen_{0};
   std::atomic<int> pending_{0};
+  std::atomic<uint64_t> next_{0};
   std::atomic<bool> armed_{false};
   const std::function<void(int)> *job_ = nullptr;
   int parts_ = 0;

@@ -107,3 +107,17 @@ def test_host_cholesky_and_solves(eig, n):
 def test_host_cholesky_reports_the_failing_minor(eig):
     A = np.asfortranarray(np.diag([1.0, 2.0, -1.0, 4.0]))
     assert eig.lib.chol(4, A.ctypes.data) == 3
+
+
+def test_host_block_is_deterministic_under_threads(eig):
+    """The pool splits a job by problem size only and any thread may run any
+    part: repeated decompositions and solves of the same 64 x 64 block (the
+    size that uses the pool) give the same bits every time."""
+    rng = np.random.default_rng(11)
+    n = 64
+    Q = rng.standard_normal((n, n))
+    A = Q + Q.T + n * np.eye(n)
+    ref = eig(A)
+    for _ in range(25):
+        rc, w, v = eig(A)
+        assert rc == ref[0] and np.array_equal(w, ref[1]) and np.array_equal(v, ref[2])
