@@ -282,23 +282,40 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
   }
 }
 
-// S_o[i + ma j] = 2^(aexp + bexp + 2) * sum over splits (fixed order)
-__global__ void k_oz_gram_final(const double *__restrict__ part, uint32_t na, uint32_t ma, uint32_t mb,
-                                uint32_t col_tiles, uint32_t splits, const int *__restrict__ aexp,
-                                const int *__restrict__ bexp, double *S0, double *S1) {
+// S_o[i + ma j] = 2^(aexp + bexp + 2) * sum over splits, in a fixed order:
+// a block takes 32 consecutive entries (coalesced partial reads) with
+// FINAL_GROUPS warps, warp g summing splits g, g + FINAL_GROUPS, ... in
+// ascending order; then the group sums are added in group order
+constexpr int FINAL_GROUPS = 8;
+__global__ void __launch_bounds__(32 * FINAL_GROUPS) k_oz_gram_final(const double *__restrict__ part, uint32_t na,
+                                                                   uint32_t ma, uint32_t mb, uint32_t col_tiles,
+                                                                   uint32_t splits, const int *__restrict__ aexp,
+                                                                   const int *__restrict__ bexp, double *S0,
+                                                                   double *S1) {
+  __shared__ double red[FINAL_GROUPS][32];
   const uint64_t total = (uint64_t)na * ma * mb;
-  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
-       t += (uint64_t)gridDim.x * blockDim.x) {
+  const uint32_t lane = threadIdx.x % 32, g = threadIdx.x / 32;
+  for (uint64_t base = (uint64_t)blockIdx.x * 32; base < total; base += (uint64_t)gridDim.x * 32) {
+    const uint64_t t = base + lane;
     const uint32_t R = (uint32_t)(t % (na * ma));
     const uint32_t j = (uint32_t)(t / (na * ma));
-    const uint32_t rt = R / 128, r = R % 128, ct = j / OG_N, cj = j % OG_N;
-    const double *p = part + ((uint64_t)(rt * col_tiles + ct) * splits) * TILE + (uint64_t)cj * 128 + r;
     double s = 0.0;
-#pragma unroll 8
-    for (uint32_t sp = 0; sp < splits; ++sp) s += __ldg(p + (uint64_t)sp * TILE);
-    const double v = s * oz::pow2(aexp[R] + bexp[j] + 2);
-    const uint32_t i = R % ma;
-    (R < ma ? S0 : S1)[i + (uint64_t)ma * j] = v;
+    if (t < total) {
+      const uint32_t rt = R / 128, r = R % 128, ct = j / OG_N, cj = j % OG_N;
+      const double *p = part + ((uint64_t)(rt * col_tiles + ct) * splits) * TILE + (uint64_t)cj * 128 + r;
+#pragma unroll 4
+      for (uint32_t sp = g; sp < splits; sp += FINAL_GROUPS) s += __ldg(p + (uint64_t)sp * TILE);
+    }
+    red[g][lane] = s;
+    __syncthreads();
+    if (g == 0 && t < total) {
+      double v = red[0][lane];
+#pragma unroll
+      for (int k = 1; k < FINAL_GROUPS; ++k) v += red[k][lane];
+      const uint32_t i = R % ma;
+      (R < ma ? S0 : S1)[i + (uint64_t)ma * j] = v * oz::pow2(aexp[R] + bexp[j] + 2);
+    }
+    __syncthreads();
   }
 }
 
@@ -522,30 +539,43 @@ __device__ __forceinline__ double factor_at(const double *__restrict__ T, const 
 }
 
 // slices of the factor as the B operand (rows = output columns j, K = input
-// index i) with per-column exponents
-__global__ void k_oz_build_t(const double *__restrict__ T, const double *__restrict__ neg_scale, uint32_t m,
-                             uint32_t mo, uint32_t kchunks, int *__restrict__ texp, __nv_bfloat16 *__restrict__ out) {
-  const uint32_t ct = blockIdx.x;  // one block per 64-column tile
+// index i) with per-column exponents.  Block (column tile, K chunk): the four
+// thread quarters take every fourth row of the column maxima (the whole K
+// range, so every chunk's block finds the same exponents), then the block
+// cuts its chunk; the first chunk's block stores the exponents.
+__global__ void __launch_bounds__(256) k_oz_build_t(const double *__restrict__ T, const double *__restrict__ neg_scale,
+                                                    uint32_t m, uint32_t mo, uint32_t kchunks, int *__restrict__ texp,
+                                                    __nv_bfloat16 *__restrict__ out) {
+  __shared__ double cmax[4][OG_N];
+  __shared__ int cexp[OG_N];
+  const uint32_t ct = blockIdx.x, kc = blockIdx.y;
   const uint32_t K = neg_scale ? 2 * m : m;
-  for (uint32_t jr = threadIdx.x; jr < OG_N; jr += blockDim.x) {
+  {
+    const uint32_t jr = threadIdx.x % OG_N, qt = threadIdx.x / OG_N;
     const uint32_t j = ct * OG_N + jr;
     double mx = 0.0;
     if (j < mo)
-      for (uint32_t i = 0; i < K; ++i) mx = fmax(mx, fabs(factor_at(T, neg_scale, m, i, j)));
-    if (j < mo) texp[j] = oz::exponent_of(mx);
+      for (uint32_t i = qt; i < K; i += 4) mx = fmax(mx, fabs(factor_at(T, neg_scale, m, i, j)));
+    cmax[qt][jr] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x < OG_N) {
+    const uint32_t jr = threadIdx.x, j = ct * OG_N + jr;
+    const double mx = fmax(fmax(cmax[0][jr], cmax[1][jr]), fmax(cmax[2][jr], cmax[3][jr]));
+    cexp[jr] = oz::exponent_of(mx);
+    if (kc == 0 && j < mo) texp[j] = cexp[jr];
   }
   __syncthreads();
   const uint32_t per_slice = OG_N * KC;
-  for (uint32_t idx = threadIdx.x; idx < kchunks * per_slice; idx += blockDim.x) {
-    const uint32_t kc = idx / per_slice, rem = idx % per_slice;
+  __nv_bfloat16 *base = out + ((uint64_t)(ct * kchunks + kc) * oz::S) * per_slice;
+  for (uint32_t rem = threadIdx.x; rem < per_slice; rem += blockDim.x) {
     const uint32_t jr = rem / KC, kk = rem % KC;
     const uint32_t j = ct * OG_N + jr, i = kc * KC + kk;
     int d[oz::S] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (j < mo && i < K) oz::digits(factor_at(T, neg_scale, m, i, j), texp[j], d);
+    if (j < mo && i < K) oz::digits(factor_at(T, neg_scale, m, i, j), cexp[jr], d);
     const uint32_t pos = (jr / 8) * (KC / 8) * 64 + (kk / 8) * 64 + (jr % 8) * 8 + (kk % 8);
-    __nv_bfloat16 *base = out + ((uint64_t)(ct * kchunks + kc) * oz::S) * per_slice;
 #pragma unroll
-    for (int s = 0; s < oz::S; ++s) base[(uint64_t)s * per_slice + pos] = __int2bfloat16_rn(d[s]);
+    for (int s2 = 0; s2 < oz::S; ++s2) base[(uint64_t)s2 * per_slice + pos] = __int2bfloat16_rn(d[s2]);
   }
 }
 
@@ -609,7 +639,8 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
     check_launch(ctx, "oz_gram");
   }
   const uint64_t total = (uint64_t)rows * mb;
-  k_oz_gram_final<<<grid_for(total, 64), 64, 0, ctx->stream>>>(ctx->oz_part.p, na, ma, mb, col_tiles, splits,
+  k_oz_gram_final<<<(unsigned)std::min<uint64_t>((total + 31) / 32, (uint64_t)ctx->sm_count * 8), 32 * FINAL_GROUPS, 0,
+                    ctx->stream>>>(ctx->oz_part.p, na, ma, mb, col_tiles, splits,
                                                                ctx->oz_exp.p, ctx->oz_exp.p + rows, S[0],
                                                                na > 1 ? S[1] : S[0]);
   check_launch(ctx, "oz_gram_final");
@@ -638,7 +669,8 @@ void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const do
   ctx->oz_exp.ensure(mo);
   ctx->oz_tdig.ensure((size_t)col_tiles * kchunks * oz::S * OG_N * KC);
   if (!rows_ready) oz_rotate_rows(ctx, Y, m, nops, N, false);
-  k_oz_build_t<<<col_tiles, 256, 0, ctx->stream>>>(T, nullptr, m, mo, kchunks, ctx->oz_exp.p, ctx->oz_tdig.p);
+  k_oz_build_t<<<dim3(col_tiles, kchunks), 256, 0, ctx->stream>>>(T, nullptr, m, mo, kchunks, ctx->oz_exp.p,
+                                                                   ctx->oz_tdig.p);
   count_launch(ctx, 1);
   RotArgs args{};
   for (uint32_t o = 0; o < nops; ++o) {
@@ -681,8 +713,9 @@ void oz_rotate_residual(gbfe_ctx *ctx, const double *T, const double *eps, uint3
   ctx->oz_tdig.ensure(fac0 + (size_t)col_tiles * k1 * oz::S * OG_N * KC);
   const double *in[3] = {Y, HY, MY};
   if (!rows_ready) oz_rotate_rows(ctx, in, m, 3, N, true);
-  k_oz_build_t<<<col_tiles, 256, 0, ctx->stream>>>(T, nullptr, m, m, k0, ctx->oz_exp.p, ctx->oz_tdig.p);
-  k_oz_build_t<<<col_tiles, 256, 0, ctx->stream>>>(T, eps, m, m, k1, ctx->oz_exp.p + m, ctx->oz_tdig.p + fac0);
+  k_oz_build_t<<<dim3(col_tiles, k0), 256, 0, ctx->stream>>>(T, nullptr, m, m, k0, ctx->oz_exp.p, ctx->oz_tdig.p);
+  k_oz_build_t<<<dim3(col_tiles, k1), 256, 0, ctx->stream>>>(T, eps, m, m, k1, ctx->oz_exp.p + m,
+                                                             ctx->oz_tdig.p + fac0);
   count_launch(ctx, 2);
   RotArgs args{};
   args.Y[0] = Y;
