@@ -149,12 +149,28 @@ __global__ void k_coldot_partial(const T *__restrict__ x, const T *__restrict__ 
   }
 }
 
-__global__ void k_coldot_final(const double *__restrict__ partial, uint32_t nb, uint32_t m, double *__restrict__ out,
-                               int take_sqrt) {
-  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
+// stage 2: a block takes 32 columns with eight warps, warp g summing the
+// partials of blocks g, g + 8, ... in ascending order; the eight sums are
+// then added in warp order (a fixed order: deterministic)
+__global__ void __launch_bounds__(256) k_coldot_final(const double *__restrict__ partial, uint32_t nb, uint32_t m,
+                                                      double *__restrict__ out, int take_sqrt) {
+  __shared__ double red[8][32];
+  const uint32_t lane = threadIdx.x % 32, g = threadIdx.x / 32;
+  for (uint32_t j0 = blockIdx.x * 32; j0 < m; j0 += gridDim.x * 32) {
+    const uint32_t j = j0 + lane;
     double s = 0.0;
-    for (uint32_t b = 0; b < nb; ++b) s += partial[(uint64_t)b * m + j];
-    out[j] = take_sqrt ? sqrt(s) : s;
+    if (j < m)
+#pragma unroll 4
+      for (uint32_t b = g; b < nb; b += 8) s += partial[(uint64_t)b * m + j];
+    red[g][lane] = s;
+    __syncthreads();
+    if (g == 0 && j < m) {
+      double v = red[0][lane];
+#pragma unroll
+      for (int k = 1; k < 8; ++k) v += red[k][lane];
+      out[j] = take_sqrt ? sqrt(v) : v;
+    }
+    __syncthreads();
   }
 }
 
@@ -230,7 +246,7 @@ void d_coldots(gbfe_ctx *ctx, const gbfe_mv *x, const gbfe_mv *y, double *out_d,
   else
     k_coldot_partial<float><<<nb, 256, 256 * sizeof(double), ctx->stream>>>(x->f.p, y->f.p, rows, m, ctx->red.p);
   check_launch(ctx, "coldot_partial");
-  k_coldot_final<<<(m + 255) / 256, 256, 0, ctx->stream>>>(ctx->red.p, nb, m, out_d, take_sqrt ? 1 : 0);
+  k_coldot_final<<<(m + 31) / 32, 256, 0, ctx->stream>>>(ctx->red.p, nb, m, out_d, take_sqrt ? 1 : 0);
   check_launch(ctx, "coldot_final");
 }
 
