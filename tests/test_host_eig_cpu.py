@@ -26,7 +26,8 @@ def eig(tmp_path_factory):
                     '{ return gbfe::host_sym_eig(n, a, w); }\n'
                     'extern "C" int chol(int n, double *a) { return gbfe::host_cholesky(n, a); }\n'
                     'extern "C" void sandwich(int n, const double *L, double *A) { gbfe::host_sandwich(n, L, A); }\n'
-                    'extern "C" void trsm_lt(int n, const double *L, double *B) { gbfe::host_trsm_lower_t(n, L, B); }\n')
+                    'extern "C" void trsm_lt(int n, const double *L, double *B) { gbfe::host_trsm_lower_t(n, L, B); }\n'
+                    'extern "C" void arm(int on) { gbfe::host_pool_arm(on != 0); }\n')
     lib = d / "libeig.so"
     subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", str(wrap), "-o", str(lib)], check=True)
     L = C.CDLL(str(lib))
@@ -36,6 +37,7 @@ def eig(tmp_path_factory):
     L.chol.restype = C.c_int
     L.sandwich.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
     L.trsm_lt.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+    L.arm.argtypes = [C.c_int]
 
     def run(A):
         n = A.shape[0]
@@ -121,3 +123,25 @@ def test_host_block_is_deterministic_under_threads(eig):
     for _ in range(25):
         rc, w, v = eig(A)
         assert rc == ref[0] and np.array_equal(w, ref[1]) and np.array_equal(v, ref[2])
+
+
+def test_host_pool_armed_and_sleeping_give_the_same_bits(eig):
+    """The pool's workers spin while armed and sleep otherwise; jobs run the
+    same either way (and arming without a job, or twice, is harmless)."""
+    rng = np.random.default_rng(12)
+    n = 64
+    Q = rng.standard_normal((n, n))
+    A = Q + Q.T
+    ref = eig(A)
+    L = eig.lib
+    L.arm(1)
+    L.arm(1)
+    try:
+        for _ in range(5):
+            rc, w, v = eig(A)
+            assert rc == ref[0] and np.array_equal(w, ref[1]) and np.array_equal(v, ref[2])
+    finally:
+        L.arm(0)
+    L.arm(0)
+    rc, w, v = eig(A)
+    assert np.array_equal(w, ref[1]) and np.array_equal(v, ref[2])
