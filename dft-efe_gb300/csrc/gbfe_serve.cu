@@ -65,6 +65,10 @@ struct Request {
 
 struct Slot {
   gbfe_ctx *ctx = nullptr;
+  // Poisson requests run on this stream of the highest priority: when a
+  // KS solve's kernel ends, the block scheduler starts the short requests'
+  // pending blocks first, so they are not queued behind whole KS passes
+  cudaStream_t hi = nullptr;
   Request *req = nullptr;
   std::thread th;
 };
@@ -242,7 +246,13 @@ void worker(gbfe_server *sv, size_t slot_index) {
       if (sv->stop && !slot.req) return;
       r = slot.req;
     }
+    const bool urgent = r->kind != 0 && slot.hi;
+    if (urgent) gbfe_ctx_set_stream(slot.ctx, slot.hi);
     run_request(sv, slot.ctx, r);
+    if (urgent) {
+      gbfe_ctx_synchronize(slot.ctx);  // nothing of this request left on the priority stream
+      gbfe_ctx_set_stream(slot.ctx, nullptr);
+    }
     {
       std::lock_guard<std::mutex> lk(sv->mu);
       r->t_done = now_s();
@@ -304,9 +314,18 @@ int gbfe_server_create(int device, uint32_t slots, uint64_t hbm_budget_bytes, gb
   for (auto &s : sv->slots) {
     const int rc = gbfe_ctx_create(device, &s.ctx);
     if (rc != GBFE_OK) {
-      for (auto &t : sv->slots) gbfe_ctx_destroy(t.ctx);
+      for (auto &t : sv->slots) {
+        gbfe_ctx_destroy(t.ctx);
+        if (t.hi) cudaStreamDestroy(t.hi);
+      }
       delete sv;
       return rc;
+    }
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&s.hi, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+      (void)cudaGetLastError();
+      s.hi = nullptr;  // every request on the context's own stream
     }
   }
   for (size_t i = 0; i < sv->slots.size(); ++i) sv->slots[i].th = std::thread(worker, sv, i);
@@ -328,7 +347,10 @@ int gbfe_server_destroy(gbfe_server *sv) {
   }
   for (auto &s : sv->slots)
     if (s.th.joinable()) s.th.join();
-  for (auto &s : sv->slots) gbfe_ctx_destroy(s.ctx);
+  for (auto &s : sv->slots) {
+    gbfe_ctx_destroy(s.ctx);
+    if (s.hi) cudaStreamDestroy(s.hi);
+  }
   delete sv;
   return GBFE_OK;
 }
