@@ -14,6 +14,7 @@
 // No float atomics anywhere: every output element has exactly one writer and a
 // fixed summation order, so results are bitwise reproducible run to run.
 #include "gbfe_internal.cuh"
+#include "gbfe_tc_ptx.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -27,6 +28,18 @@ namespace {
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
+// Check of the bounded-wait path of the tensor-core kernels: one thread waits
+// on an mbarrier that nothing arrives on, with the same wait routine and a
+// caller-chosen time limit.  The wait gives up, writes GBFE_ERR_TIMEOUT into
+// the status word, and the kernel returns; no copy or MMA is in flight, so
+// the context stays usable.
+__global__ void k_wait_unset_barrier(int *status, uint64_t max_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) tc::mbar_wait_limited(&bar, 0, status, GBFE_ERR_TIMEOUT, tc::WAIT_LIMIT, max_ns);
+}
+
 template <class T>
 __global__ void k_p2c(T *__restrict__ x, uint32_t m, uint32_t n_rows, const uint32_t *__restrict__ row_ids,
                       const uint32_t *__restrict__ row_sizes, const uint32_t *__restrict__ col_ids,
@@ -444,11 +457,10 @@ static void cell_apply_f64(const gbfe_op *op, gbfe_mv *X, double *Yc) {
   const uint64_t target = (uint64_t)ctx->sm_count * 12;
   while (base * jsplit < target && jsplit * 8 < me->nd_min) jsplit *= 2;
   const size_t smem = sizeof(double) * (size_t)me->nd_max * mt;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_once;
+  attr_once.run(ctx->device, [&] {
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
-    attr_set = true;
-  }
+  });
   dim3 grid(me->n_cells, vt, jsplit);
   ProfScope prof(ctx, "cell_apply_f64", 2.0 * m * (double)me->total_mat,
                  8.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat));
@@ -829,6 +841,15 @@ int gbfe_ctx_check_status(gbfe_ctx *ctx) {
   });
   if (rc != GBFE_OK) return rc;
   return st ? GBFE_ERR_TIMEOUT : GBFE_OK;
+}
+
+int gbfe_ctx_check_wait_timeout(gbfe_ctx *ctx, double limit_s) {
+  if (!ctx || !(limit_s >= 0.0 && limit_s <= 1.0)) return GBFE_ERR_ARG;
+  return gbfe_guard(ctx, [&] {
+    k_wait_unset_barrier<<<1, 32, 0, ctx->stream>>>(ctx->status.p, (uint64_t)(limit_s * 1e9));
+    check_launch(ctx, "wait_unset_barrier");
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
 }
 
 int gbfe_ctx_set_split_groups(gbfe_ctx *ctx, int on) {
@@ -1449,8 +1470,10 @@ int gbfe_apply(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
 namespace {
 constexpr uint64_t kNoAllocScratchDoubles = 8ull << 20;  // 64 MiB per GPU, held until exit
 static __device__ __align__(256) double g_noalloc_cell_scratch[kNoAllocScratchDoubles];
-constexpr int kMaxDevices = 64;
-double *g_noalloc_ptr[kMaxDevices] = {nullptr};  // device address per device (set on first use)
+// device address of the array per device, looked up on the first call there;
+// atomic because server slot threads may make their first calls concurrently
+// (every thread that looks it up stores the same address)
+std::atomic<double *> g_noalloc_ptr[kMaxDevices];
 }  // namespace
 
 extern "C" int gbfe_apply_f64_noalloc(const gbfe_op *op, double *X_dev, double *Y_dev, uint32_t m) {
@@ -1470,15 +1493,16 @@ extern "C" int gbfe_apply_f64_noalloc(const gbfe_op *op, double *X_dev, double *
     GBFE_CUDA(cudaGetDevice(&dev));
     GBFE_REQUIRE(dev == ctx->device, "apply_f64_noalloc: the context's device must be current");
     GBFE_REQUIRE(dev >= 0 && dev < kMaxDevices, "apply_f64_noalloc: device index out of range");
-    if (!g_noalloc_ptr[dev]) {
+    double *Yc = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+    if (!Yc) {
       // once per device, with that device current: the symbol's host-side name
       // is not a device address, so fetch the real one
       void *p = nullptr;
       GBFE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_cell_scratch));
-      g_noalloc_ptr[dev] = (double *)p;
+      Yc = (double *)p;
+      g_noalloc_ptr[dev].store(Yc, std::memory_order_release);
     }
     GBFE_REQUIRE(!op->nl, "apply_f64_noalloc: operators with a nonlocal part need gbfe_apply");
-    double *Yc = g_noalloc_ptr[dev];
     const uint32_t Nn = (uint32_t)me->n_dofs;
     (void)Nn;
     // constraints on X (the same kernels gbfe_apply launches)

@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <exception>
 #include <functional>
 #include <mutex>
 #include <thread>
@@ -72,7 +73,16 @@ class HostPool {
     }
     cv_.notify_all();
     claim_and_run(g, parts, f);
+    // every part has been claimed; wait for the ones still running on workers
+    // (they hold a reference to f, so f must stay alive until then), then
+    // rethrow the first exception any part raised
     while (pending_.load(std::memory_order_acquire) != 0) std::this_thread::yield();
+    std::exception_ptr err;
+    {
+      std::lock_guard<std::mutex> lk(err_mu_);
+      std::swap(err, err_);
+    }
+    if (err) std::rethrow_exception(err);
   }
   void arm(bool on) {
     if (workers_.empty()) return;
@@ -129,12 +139,20 @@ class HostPool {
       uint64_t cur = next_.load(std::memory_order_acquire);
       if ((cur >> 32) != g || (int)(cur & 0xffffffffu) >= parts) return;
       if (!next_.compare_exchange_weak(cur, cur + 1, std::memory_order_acq_rel)) continue;
-      f((int)(cur & 0xffffffffu));
+      // a part that throws still counts as done: the exception is kept for
+      // run() to rethrow in the calling thread (never escapes a worker)
+      try {
+        f((int)(cur & 0xffffffffu));
+      } catch (...) {
+        std::lock_guard<std::mutex> lk(err_mu_);
+        if (!err_) err_ = std::current_exception();
+      }
       pending_.fetch_sub(1, std::memory_order_acq_rel);
     }
   }
   std::vector<std::thread> workers_;
-  std::mutex mu_, run_mu_;
+  std::mutex mu_, run_mu_, err_mu_;
+  std::exception_ptr err_;  // first exception of the current job
   std::condition_variable cv_;
   std::atomic<uint64_t> gen_{0};
   std::atomic<int> pending_{0};

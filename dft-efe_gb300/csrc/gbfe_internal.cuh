@@ -70,6 +70,30 @@ struct Error : std::runtime_error {
     if (!(cond)) throw ::gbfe::Error(GBFE_ERR_ARG, msg);                                     \
   } while (0)
 
+// Devices a process may drive (the per-device flags and addresses below).
+constexpr int kMaxDevices = 64;
+
+// cudaFuncSetAttribute (the dynamic shared-memory opt-in of a kernel) is a
+// property of a device's context, not of the process: a call site keeps one
+// flag per device, so a context created later on another device sets the
+// attribute there too.  The flags are atomic because server slot threads
+// launch concurrently; two threads that both see "not done" both set the same
+// value, which is harmless.  Not a stream operation, so it stays out of graph
+// captures once it has run.
+struct PerDeviceOnce {
+  std::atomic<bool> done[kMaxDevices];
+  template <class F>
+  void run(int dev, F &&f) {
+    if (dev < 0 || dev >= kMaxDevices) {
+      f();
+      return;
+    }
+    if (done[dev].load(std::memory_order_acquire)) return;
+    f();
+    done[dev].store(true, std::memory_order_release);
+  }
+};
+
 // owning device buffer
 template <class T>
 struct DBuf {

@@ -98,11 +98,10 @@ void apply_cell_mixed(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
   uint32_t jsplit = 1;
   const uint64_t target = (uint64_t)ctx->sm_count * 12;
   while (base * jsplit < target && jsplit * 8 < me->nd_min) jsplit *= 2;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_once;
+  attr_once.run(ctx->device, [&] {
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
-    attr_set = true;
-  }
+  });
   const size_t smem = sizeof(float) * (size_t)me->nd_max * mt;
   dim3 grid(me->n_cells, vt, jsplit);
   const DBuf<float> *m32 = &op->mats_f32;

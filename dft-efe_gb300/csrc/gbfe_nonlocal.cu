@@ -103,13 +103,12 @@ __global__ void __launch_bounds__(NL_THREADS)
 }
 
 template <class T>
-void set_smem_attr_once() {
-  static bool done = false;
-  if (!done) {
+void set_smem_attr_once(int device) {
+  static PerDeviceOnce once;
+  once.run(device, [] {
     GBFE_CUDA(cudaFuncSetAttribute(k_nl_project<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)NL_SMEM));
     GBFE_CUDA(cudaFuncSetAttribute(k_nl_add<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)NL_SMEM));
-    done = true;
-  }
+  });
 }
 
 // vectors per CTA: the gathered tile (nd x mt or np x mt) must fit NL_SMEM
@@ -125,7 +124,7 @@ template <class T>
 void project_t(const gbfe_nl *nl, const T *X, uint32_t m, T *CX, T *W, const T *cm, const T *V) {
   gbfe_mesh *me = nl->mesh;
   gbfe_ctx *ctx = me->ctx;
-  set_smem_attr_once<T>();
+  set_smem_attr_once<T>(ctx->device);
   const uint32_t mt = nl_tile(nl, m, sizeof(T));
   const dim3 grid(nl->n_cells_nl, (m + mt - 1) / mt);
   {
@@ -143,7 +142,7 @@ template <class T>
 void add_t(const gbfe_nl *nl, uint32_t m, T *Yc, const T *cm, const T *W) {
   gbfe_mesh *me = nl->mesh;
   gbfe_ctx *ctx = me->ctx;
-  set_smem_attr_once<T>();
+  set_smem_attr_once<T>(ctx->device);
   const uint32_t mt = nl_tile(nl, m, sizeof(T));
   const dim3 grid(nl->n_cells_nl, (m + mt - 1) / mt);
   ProfScope prof(ctx, "nonlocal_add", 2.0 * m * (double)nl->cmat.n, (double)sizeof(T) * nl->cmat.n);

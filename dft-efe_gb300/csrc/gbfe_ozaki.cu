@@ -384,11 +384,10 @@ void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc, const int *x
   if (!xexp) xexp = oz_column_exponents(op, X);
   const uint32_t vt = (m + OZ_N - 1) / OZ_N;
   const uint32_t smem = OZ_SMEM;
-  static bool attr_set = false;  // once: not a stream operation, so it stays out of graph captures
-  if (!attr_set) {
+  static PerDeviceOnce attr_once;
+  attr_once.run(ctx->device, [&] {
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+  });
   for (uint32_t mts = 1; mts <= 2; ++mts) {
     uint32_t b0 = UINT32_MAX, b1 = 0;
     for (uint32_t b = 0; b < me->bin_nd.size(); ++b)

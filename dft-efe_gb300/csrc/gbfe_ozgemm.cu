@@ -579,13 +579,12 @@ __global__ void __launch_bounds__(256) k_oz_build_t(const double *__restrict__ T
   }
 }
 
-void set_attrs_once() {
-  static bool done = false;  // not a stream operation: stays out of graph captures
-  if (!done) {
+void set_attrs_once(int device) {
+  static PerDeviceOnce once;
+  once.run(device, [] {
     GBFE_CUDA(cudaFuncSetAttribute(k_oz_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OG_SMEM));
     GBFE_CUDA(cudaFuncSetAttribute(k_oz_rot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OG_SMEM));
-    done = true;
-  }
+  });
 }
 
 }  // namespace
@@ -601,7 +600,7 @@ bool oz_gemm_supported(gbfe_ctx *ctx, uint32_t m) {
 void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, const double *B, uint32_t mb,
              uint64_t N, double *const *S, const int *bexp) {
   GBFE_REQUIRE(na >= 1 && na <= 2 && ma > 0 && mb > 0, "oz_gram: bad shape");
-  set_attrs_once();
+  set_attrs_once(ctx->device);
   const uint32_t rows = na * ma;
   const uint32_t row_tiles = (rows + 127) / 128, col_tiles = (mb + OG_N - 1) / OG_N;
   const uint32_t chunks = (uint32_t)std::max<uint64_t>(1, (N + CHUNK - 1) / CHUNK);
@@ -663,7 +662,7 @@ void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t 
 void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const double *const *Y, double *const *out,
                uint32_t nops, uint64_t N, bool rows_ready) {
   GBFE_REQUIRE(nops >= 1 && nops <= 3 && m > 0 && m <= (uint32_t)oz::K_EXACT && mo > 0, "oz_rotate: bad shape");
-  set_attrs_once();
+  set_attrs_once(ctx->device);
   const uint32_t kchunks = (m + KC - 1) / KC, col_tiles = (mo + OG_N - 1) / OG_N;
   const uint32_t row_tiles = (uint32_t)((N + 127) / 128);
   ctx->oz_exp.ensure(mo);
@@ -705,7 +704,7 @@ bool oz_rotate_residual_supported(gbfe_ctx *ctx, uint32_t m) { return oz_gemm_su
 void oz_rotate_residual(gbfe_ctx *ctx, const double *T, const double *eps, uint32_t m, const double *Y,
                         const double *HY, const double *MY, double *X, double *R, uint64_t N, bool rows_ready) {
   GBFE_REQUIRE(m > 0 && oz_rotate_residual_supported(ctx, m), "oz_rotate_residual: bad shape");
-  set_attrs_once();
+  set_attrs_once(ctx->device);
   const uint32_t k0 = (m + KC - 1) / KC, k1 = (2 * m + KC - 1) / KC, col_tiles = (m + OG_N - 1) / OG_N;
   const uint32_t row_tiles = (uint32_t)((N + 127) / 128);
   const size_t fac0 = (size_t)col_tiles * k0 * oz::S * OG_N * KC;

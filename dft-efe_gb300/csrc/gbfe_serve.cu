@@ -42,7 +42,7 @@ struct Request {
   std::vector<double> cvals, inh;
   uint64_t n_dofs = 0;
   // KS
-  std::vector<double> H, M, minv, X0, blk;
+  std::vector<double> H, M, minv, X0, blk, lanczos_start;
   uint64_t blk_begin = 0, blk_n = 0;
   gbfe_ks_params ks{};
   uint32_t m = 0;
@@ -373,6 +373,13 @@ int gbfe_server_submit_ks(gbfe_server *sv, const gbfe_mesh_desc *mesh, const dou
   r->X0 = copy_arr(X0, r->n_dofs * (uint64_t)m);
   r->m = m;
   r->ks = *params;
+  // a start vector is copied like the other arrays (the caller may free it)
+  if (params->use_lanczos && params->lanczos_start) {
+    r->lanczos_start = copy_arr(params->lanczos_start, r->n_dofs);
+    r->ks.lanczos_start = r->lanczos_start.data();
+  } else {
+    r->ks.lanczos_start = nullptr;
+  }
   r->footprint = ks_footprint(*r);
   return submit_common(sv, std::move(r), id_out);
 }

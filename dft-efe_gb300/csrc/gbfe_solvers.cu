@@ -716,18 +716,26 @@ void host_sym_eigvals(std::vector<double> a, int k, std::vector<double> &w) {
   std::sort(w.begin(), w.end());
 }
 
+// start: the initial vector (n_dofs values, host or device memory), or nullptr
+// for a seeded uniform [0, 1) vector (the reference draws std::rand() /
+// RAND_MAX per entry, LanczosExtremeEigenSolver.t.cpp:40-52)
 void lanczos_impl(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, uint32_t steps, uint64_t seed,
-                  double *out3) {
+                  double *out3, const double *start = nullptr) {
   gbfe_mesh *me = A->mesh;
   gbfe_ctx *ctx = me->ctx;
   const uint64_t N = me->n_dofs;
   auto x0 = make_mv(me, 1, GBFE_F64), temp = make_mv(me, 1, GBFE_F64), v = make_mv(me, 1, GBFE_F64);
   auto q = make_mv(me, 1, GBFE_F64), qPrev = make_mv(me, 1, GBFE_F64);
-  std::vector<double> h(N);
-  std::mt19937_64 g(seed);
-  std::uniform_real_distribution<double> U(0.0, 1.0);
-  for (auto &x : h) x = U(g);
-  GBFE_CUDA(cudaMemcpyAsync(x0->d.p, h.data(), N * 8, cudaMemcpyHostToDevice, ctx->stream));
+  if (start) {
+    GBFE_CUDA(cudaMemcpyAsync(x0->d.p, start, N * 8, cudaMemcpyDefault, ctx->stream));
+  } else {
+    std::vector<double> h(N);
+    std::mt19937_64 g(seed);
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    for (auto &x : h) x = U(g);
+    GBFE_CUDA(cudaMemcpyAsync(x0->d.p, h.data(), N * 8, cudaMemcpyHostToDevice, ctx->stream));
+    GBFE_CUDA(cudaStreamSynchronize(ctx->stream));  // h is freed on return
+  }
   double alpha = 0.0, beta = 0.0;
   apply_op(B, x0.get(), temp.get());
   host_coldots(ctx, x0.get(), temp.get(), &alpha, false);
@@ -1194,6 +1202,15 @@ int gbfe_lanczos_bounds(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
   });
 }
 
+int gbfe_lanczos_bounds_from(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, uint32_t steps,
+                             const double *start, double *out3) {
+  if (!A || !B || !BInv || !start || !out3) return GBFE_ERR_ARG;
+  return gbfe_guard(A->mesh->ctx, [&] {
+    GBFE_REQUIRE(steps >= 2, "lanczos: need at least 2 steps");
+    lanczos_impl(A, B, BInv, steps, 0, out3, start);
+  });
+}
+
 int gbfe_ks_eigen_solve(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv *X,
                         const gbfe_ks_params *prm, double *eigenvalues, double *residuals, uint32_t *passes_out) {
   if (!A || !B || !BInv || !X || !prm || !eigenvalues || !residuals) return GBFE_ERR_ARG;
@@ -1206,7 +1223,8 @@ int gbfe_ks_eigen_solve(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
     double wl = prm->wanted_lower, wu = prm->wanted_upper, uu = prm->unwanted_upper;
     if (prm->use_lanczos) {
       double b3[3];
-      lanczos_impl(A, B, BInv, prm->lanczos_steps ? prm->lanczos_steps : 20, prm->lanczos_seed, b3);
+      lanczos_impl(A, B, BInv, prm->lanczos_steps ? prm->lanczos_steps : 20, prm->lanczos_seed, b3,
+                   prm->lanczos_start);
       const double res = b3[2] / 10.0;  // KohnShamEigenSolver.t.cpp:270-273
       wl = b3[0];
       uu = b3[1] + res;

@@ -671,12 +671,11 @@ static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, f
       std::max<uint32_t>(1, std::min<uint32_t>(std::min<uint32_t>((228 * 1024) / (smem + 1024), 512 / cols), occ));
   const uint32_t items = ncell * vt;
   const uint32_t grid = std::min<uint32_t>(items, per_sm * (uint32_t)ctx->sm_count);
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_once;
+  attr_once.run(ctx->device, [&] {
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr_set = true;
-  }
+  });
   // float4 gather when every row of X (and of xsub) starts on a 16-byte boundary
   uint32_t wpc = 0;
   if (m % 4 == 0 && ((uintptr_t)X->f.p % 16) == 0 && ((uintptr_t)xsub % 16) == 0 && ctx->tc_gather4) {

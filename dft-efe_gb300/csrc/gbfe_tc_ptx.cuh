@@ -48,13 +48,14 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
   return t;
 }
 
-// bounded wait on the given phase parity (WAIT_LIMIT polls and WAIT_NS of
-// wall time, whichever ends first); false on timeout, and then, when status is
+// bounded wait on the given phase parity (max_polls polls and max_ns of wall
+// time, whichever ends first); false on timeout, and then, when status is
 // given, the error code goes into the device status word
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code) {
+__device__ __forceinline__ bool mbar_wait_limited(uint64_t *bar, uint32_t parity, int *status, int code,
+                                                  uint32_t max_polls, uint64_t max_ns) {
   const uint32_t a = smem_u32(bar);
   uint64_t t0 = 0;
-  for (uint32_t it = 0; it < WAIT_LIMIT; ++it) {
+  for (uint32_t it = 0; it < max_polls; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -66,12 +67,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *s
       const uint64_t t = globaltimer_ns();
       if (!t0)
         t0 = t;
-      else if (t - t0 > WAIT_NS)
+      else if (t - t0 > max_ns)
         break;
     }
   }
   if (status) atomicCAS(status, 0, code);
   return false;
+}
+
+// the waits of the tensor-core kernels: WAIT_LIMIT polls or WAIT_NS
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code) {
+  return mbar_wait_limited(bar, parity, status, code, WAIT_LIMIT, WAIT_NS);
 }
 
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {

@@ -28,7 +28,7 @@ class KSParams(C.Structure):
         ("degree", u32), ("max_passes", u32), ("n_wanted", u32), ("filter_precision", i32),
         ("residual_tol", f64), ("wanted_lower", f64), ("wanted_upper", f64), ("unwanted_upper", f64),
         ("use_lanczos", i32), ("lanczos_steps", u32), ("lanczos_seed", u64), ("fixed_passes", i32),
-        ("fp64_apply", i32), ("faithful_passes", i32),
+        ("fp64_apply", i32), ("faithful_passes", i32), ("lanczos_start", p),
     ]
 
 
@@ -52,6 +52,7 @@ SIGNATURES = {
     "gbfe_ctx_synchronize": (i32, [p]),
     "gbfe_ctx_kernel_launches": (i32, [p, C.POINTER(u64)]),
     "gbfe_ctx_check_status": (i32, [p]),
+    "gbfe_ctx_check_wait_timeout": (i32, [p, f64]),
     "gbfe_ctx_set_tensor_cores": (i32, [p, i32]),
     "gbfe_ctx_set_split_groups": (i32, [p, i32]),
     "gbfe_ctx_set_profiling": (i32, [p, i32]),
@@ -104,6 +105,7 @@ SIGNATURES = {
     "gbfe_chfsi_pass": (i32, [p, p, p, p, p, u32, f64, f64, f64, i32]),
     "gbfe_ks_eigen_solve": (i32, [p, p, p, p, C.POINTER(KSParams), p, p, C.POINTER(u32)]),
     "gbfe_lanczos_bounds": (i32, [p, p, p, u32, u64, p]),
+    "gbfe_lanczos_bounds_from": (i32, [p, p, p, u32, p, p]),
     "gbfe_cg_solve": (i32, [p, p, p, p, u32, f64, f64, f64, C.POINTER(u32), p]),
     "gbfe_pcg_solve_batched": (i32, [p, p, p, p, u32, p, u32, f64, f64, f64, u32, p, p, p]),
     "gbfe_server_create": (i32, [i32, u32, u64, C.POINTER(p)]),

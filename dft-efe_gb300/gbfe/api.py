@@ -488,16 +488,29 @@ class ChebyshevFilteredEigenSolver:
         return ev
 
 
-def lanczos_bounds(A, B, BInv, steps: int = 20, seed: int = 7) -> np.ndarray:
+def lanczos_bounds(A, B, BInv, steps: int = 20, seed: int = 7, start=None) -> np.ndarray:
+    """[smallest, largest Ritz value, last beta] of B^-1 A after `steps` Lanczos steps, from `start` (a one-column
+    MultiVector or a host array of n_dofs values) or a seeded uniform start vector."""
     out = np.empty(3)
-    check(A.ctx.lib.gbfe_lanczos_bounds(A.h, B.h, BInv.h, int(steps), int(seed), _ptr(out)), A.ctx.h, "lanczos")
+    if start is None:
+        check(A.ctx.lib.gbfe_lanczos_bounds(A.h, B.h, BInv.h, int(steps), int(seed), _ptr(out)), A.ctx.h, "lanczos")
+        return out
+    if isinstance(start, MultiVector):
+        ptr = C.c_void_p(start.device_ptr())
+    else:
+        start = np.ascontiguousarray(start, dtype=np.float64).ravel()
+        ptr = _ptr(start)
+    check(A.ctx.lib.gbfe_lanczos_bounds_from(A.h, B.h, BInv.h, int(steps), ptr, _ptr(out)), A.ctx.h, "lanczos")
     return out
 
 
 class KohnShamEigenSolver:
     def __init__(self, n_wanted: int, degree: int, max_passes: int, residual_tol: float = 1e-6, mixed: bool = False,
                  bounds: Optional[Sequence[float]] = None, lanczos_steps: int = 20, lanczos_seed: int = 7,
-                 fixed_passes: bool = False, faithful_passes: bool = False, fp64_tensor: bool = False):
+                 fixed_passes: bool = False, faithful_passes: bool = False, fp64_tensor: bool = False,
+                 lanczos_start=None):
+        """lanczos_start (with bounds=None): the Lanczos start vector, a MultiVector with one column (device
+        resident) or a host array of n_dofs values; None draws a seeded uniform vector (lanczos_seed)."""
         self.p = KSParams()
         self.p.degree, self.p.max_passes, self.p.n_wanted = int(degree), int(max_passes), int(n_wanted)
         self.p.filter_precision = GBFE_F32 if mixed else GBFE_F64
@@ -511,6 +524,16 @@ class KohnShamEigenSolver:
         self.p.fixed_passes = 1 if fixed_passes else 0
         self.p.faithful_passes = 1 if faithful_passes else 0
         self.p.fp64_apply = int(fp64_tensor)  # True / 1: sliced products everywhere; 2: cell products only
+        self._start = None
+        if lanczos_start is not None:
+            if isinstance(lanczos_start, MultiVector):
+                if lanczos_start.m != 1 or lanczos_start.dtype != np.float64:
+                    raise ValueError("lanczos_start must be one FP64 column")
+                self._start = lanczos_start
+                self.p.lanczos_start = lanczos_start.device_ptr()
+            else:
+                self._start = np.ascontiguousarray(lanczos_start, dtype=np.float64).ravel()
+                self.p.lanczos_start = self._start.ctypes.data
 
     def solve(self, H, X: MultiVector, M, MInv, eigenvalues: Optional[np.ndarray] = None):
         ev = np.zeros(X.m) if eigenvalues is None else np.ascontiguousarray(eigenvalues, dtype=np.float64).copy()

@@ -341,6 +341,13 @@ def config3(seed: int = 12348, **kw) -> FEProblem:
     return ks_box(24, 5, 40.0, 64, 4.0, 0.5, seed, atom_layout="jittered_cubic", **kw)
 
 
+def lanczos_start_vector(n_dofs: int, seed: int) -> np.ndarray:
+    """Seeded uniform [0, 1) Lanczos start vector (the reference draws
+    std::rand() / RAND_MAX per entry, LanczosExtremeEigenSolver.t.cpp:40-52,
+    from an unseeded generator; a seeded one makes runs repeatable)."""
+    return np.random.Generator(np.random.MT19937(seed)).random(n_dofs)
+
+
 def random_block(n_dofs: int, m: int, seed: int, dtype=np.float64) -> np.ndarray:
     """Seeded N(0,1) initial block, row-major [N][m] (vector index fastest)."""
     return np.random.default_rng(seed).standard_normal((n_dofs, m)).astype(dtype)

@@ -72,6 +72,13 @@ int gbfe_ctx_synchronize(gbfe_ctx *ctx);
 /* Reads and clears the device status word that the tensor-core kernels set
  * when one of their bounded waits gives up: GBFE_OK or GBFE_ERR_TIMEOUT. */
 int gbfe_ctx_check_status(gbfe_ctx *ctx);
+/* Check of that failure path (no counterpart in the reference): launches one
+ * thread that waits, through the same bounded-wait routine, on a barrier that
+ * nothing completes, giving up after limit_s seconds (0 to 1).  Afterwards
+ * gbfe_ctx_check_status returns GBFE_ERR_TIMEOUT once and the context stays
+ * usable.  Nothing else is in flight in that kernel, so no GPU fault is
+ * involved. */
+int gbfe_ctx_check_wait_timeout(gbfe_ctx *ctx, double limit_s);
 /* Cell product of the FP32 apply: 2 (default) the persistent warp-specialised
  * split-BF16 tcgen05 kernel (16-byte row gathers when m % 4 == 0); 3 the same
  * kernel with one 4-byte element per gather load; 1 the one-CTA-per-cell
@@ -341,6 +348,10 @@ typedef struct {
                                    fresh H X, M X: six FP64 applies per pass).
                                    0: H X and M X are carried through the
                                    m x m rotations (two FP64 applies per pass). */
+  const double *lanczos_start;  /* with use_lanczos: the Lanczos start vector
+                                   (n_dofs values, host or device memory; read
+                                   once per solve), or NULL for a seeded
+                                   uniform [0, 1) vector (lanczos_seed)       */
 } gbfe_ks_params;
 
 /* ChebyshevFilteredEigenSolver::solve (ChebyshevFilteredEigenSolver.t.cpp:
@@ -361,6 +372,11 @@ int gbfe_ks_eigen_solve(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
  * largest Ritz value, out[2] = last beta (residual). */
 int gbfe_lanczos_bounds(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
                         uint32_t steps, uint64_t seed, double *out3);
+/* The same from a given start vector (n_dofs values, host or device memory):
+ * the initialGuess constructor argument of LanczosExtremeEigenSolver
+ * (LanczosExtremeEigenSolver.t.cpp:94-112). */
+int gbfe_lanczos_bounds_from(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv,
+                             uint32_t steps, const double *start, double *out3);
 
 /* ---- CG -------------------------------------------------------------------
  * CGLinearSolver::solve (linearAlgebra/CGLinearSolver.t.cpp:68-313) with

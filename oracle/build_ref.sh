@@ -4,16 +4,26 @@
 # against scipy's bundled LP64 OpenBLAS.  Test infrastructure only: it makes
 # the golden vectors in tests/golden/.  Outputs go to oracle/_ref/ only.
 #
-#   REF  : reference source tree (default /root/reference)
+#   DFTEFE_REFERENCE (or REF): reference source tree (default /root/reference)
+#   --source      print the reference's src/ directory and exit (status 3 when
+#                 it is absent); tests use it to find the reference headers
+#   --if-present  exit 0 without building when the sources are absent
 #   The one reference-side defect that stops the serial build -- a stray ';'
 #   at utils/MPIWrapper.cpp:334 in the non-MPI branch -- is patched into a
 #   copy under oracle/_ref/patched/ at build time.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${REF:-/root/reference}"
+REF="${DFTEFE_REFERENCE:-${REF:-/root/reference}}"
 OUT="$HERE/_ref"
 SRC="$REF/src"
-if [ ! -d "$SRC" ]; then echo "reference sources not found at $SRC" >&2; exit 1; fi
+if [ "${1:-}" = "--source" ]; then
+  if [ -d "$SRC" ]; then echo "$SRC"; exit 0; fi
+  exit 3
+fi
+if [ ! -d "$SRC" ]; then
+  if [ "${1:-}" = "--if-present" ]; then echo "reference sources not found at $SRC: reference build skipped"; exit 0; fi
+  echo "reference sources not found at $SRC" >&2; exit 1
+fi
 mkdir -p "$OUT/patched" "$OUT/obj"
 
 BLASDIR="$(python3 -c 'import scipy, os; print(os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs"))')"

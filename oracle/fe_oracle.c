@@ -38,6 +38,10 @@
  *   orc_chebyshev_filter
  *                linearAlgebra/ChebyshevFilter.t.cpp:39-135
  *   orc_cg       linearAlgebra/CGLinearSolver.t.cpp:68-313
+ *   orc_sweep    one column-scaled sweep z = a x + b coef[j] y, the loop form
+ *                of the filter's axpby / axpbyBlocked updates above
+ *                (linearAlgebra/BlasLapackKernels.cpp:477-502); timed by the
+ *                CPU baseline's per-operation sample
  *
  * The per-cell product goes through a caller-supplied Fortran dgemm (the
  * reference calls dgemm_ through blasWrapper::gemm); with none supplied a
@@ -419,4 +423,14 @@ int orc_cg(const orc_op *A, const orc_op *PC, const double *b, double *x_inout, 
   if (rnorm_out) memcpy(rnorm_out, rn, sizeof(double) * k);
   free(x); free(xc); free(r); free(w); free(z); free(p); free(bn); free(rn); free(zr); free(pw); free(zrn); free(conv);
   return err;
+}
+
+/* z[i][j] = a x[i][j] + b coef[j] y[i][j] over n = N m entries (row-major, m
+   columns): the cost of one of the filter's vector updates. */
+void orc_sweep(uint64_t n, uint32_t m, double a, const double *x, double b, const double *coef, const double *y,
+               double *z) {
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint32_t j = (uint32_t)(i % m);
+    z[i] = a * x[i] + b * coef[j] * y[i];
+  }
 }

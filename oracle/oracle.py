@@ -95,6 +95,8 @@ def load(use_blas: bool = True):
         lib.orc_chebyshev_filter.argtypes = [P, P, P, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, P]
         lib.orc_cg.argtypes = [P, P, P, P, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
                                C.POINTER(C.c_uint32), P]
+        lib.orc_sweep.argtypes = [C.c_uint64, C.c_uint32, C.c_double, P, C.c_double, P, P, P]
+        lib.orc_sweep.restype = None
         _lib = lib
     _lib.orc_set_dgemm(C.c_void_p(_dgemm_pointer()) if use_blas else None)
     return _lib
@@ -259,9 +261,17 @@ class OracleSystem:
             raise RuntimeError(f"oracle Cholesky-GS failed ({st})")
         return self.rayleigh_ritz(A, Xo)
 
-    def lanczos_bounds(self, A, B, BInv, steps=20, seed=7):
-        rng = np.random.Generator(np.random.MT19937(seed))
-        x0 = rng.random((self.n_dofs, 1))
+    def sweep(self, a, x, b, coef, y, z):
+        """z = a x + b coef[j] y (one vector update of the filter's kind, in C)."""
+        self.lib.orc_sweep(x.size, x.shape[1], float(a), _p(x), float(b), _p(np.ascontiguousarray(coef)), _p(y), _p(z))
+
+    def lanczos_bounds(self, A, B, BInv, steps=20, seed=7, start=None):
+        """start: the initial vector (n_dofs values); None draws MT19937(seed) uniform [0, 1)."""
+        if start is None:
+            rng = np.random.Generator(np.random.MT19937(seed))
+            x0 = rng.random((self.n_dofs, 1))
+        else:
+            x0 = np.ascontiguousarray(start, dtype=np.float64).reshape(self.n_dofs, 1).copy()
         temp = self.apply(B, x0)
         alpha = np.sqrt(float((x0 * temp).sum()))
         q = x0 / alpha
@@ -288,11 +298,11 @@ class OracleSystem:
         return np.array([w[0], w[-1], bv[-1]])
 
     def ks_eigen_solve(self, A, B, BInv, X0, degree, max_passes, n_wanted, tol, bounds=None, eig0=None,
-                       fixed_passes=False, lanczos_steps=20, lanczos_seed=7):
+                       fixed_passes=False, lanczos_steps=20, lanczos_seed=7, lanczos_start=None):
         X = np.ascontiguousarray(X0, dtype=np.float64).copy()
         m = X.shape[1]
         if bounds is None:
-            b = self.lanczos_bounds(A, B, BInv, lanczos_steps, lanczos_seed)
+            b = self.lanczos_bounds(A, B, BInv, lanczos_steps, lanczos_seed, start=lanczos_start)
             res = b[2] / 10.0
             wl, uu = b[0], b[1] + res
             wu = (b[1] + res - b[0]) * (m * 200.0 / self.n_dofs) + b[0]

@@ -45,14 +45,15 @@ def test_operator_context_adapter_compiles_against_reference_headers(tmp_path):
     the reference's own OperatorContext / MultiVector headers, instantiated
     for HOST and DEVICE memory spaces.  Skipped where the reference sources are
     not present."""
-    import os
     import shutil
     import subprocess
 
     import pytest
 
-    ref = Path(os.environ.get("DFTEFE_REFERENCE", "/root/reference")) / "src"
-    if not ref.is_dir() or not shutil.which("g++"):
+    found = subprocess.run(["bash", str(ROOT / "oracle" / "build_ref.sh"), "--source"], capture_output=True,
+                           text=True)
+    ref = Path(found.stdout.strip()) if found.returncode == 0 else None
+    if ref is None or not ref.is_dir() or not shutil.which("g++"):
         pytest.skip("reference sources not available")
     src = tmp_path / "adapter.cpp"
     src.write_text(

@@ -6,12 +6,17 @@ latency-critical loop that must not pay the device-wide synchronisation a
 cudaMalloc can trigger.  Its cell-wise intermediate lives in a fixed
 64 MiB library array instead of a buffer grown per operator.
 
-This file is collected last.  The test calls the entry point through the C ABI
-twice in a row on caller-owned device buffers and checks both results against
-gbfe_apply (relative max-norm <= 1e-12, the FP64 apply tolerance), and checks
-that an oversize request is rejected.  It must pass alone in a fresh process
-and after the rest of the suite.
+This file is collected last.  The tests call the entry point through the C ABI
+twice in a row on caller-owned device buffers and check both results against
+gbfe_apply (relative max-norm <= 1e-12, the FP64 apply tolerance): once on a
+mesh with homogeneous Dirichlet rows only, once on the reference-built
+hanging-node fixture (constraint rows with parents and inhomogeneities, an odd
+number of vectors), where the result is also checked against the reference's
+own output.  An oversize request must be rejected.  The file must pass alone
+in a fresh process and after the rest of the suite.
 """
+from pathlib import Path
+
 import ctypes as C
 
 import numpy as np
@@ -45,6 +50,37 @@ def test_noalloc_apply_matches_apply_twice(gpu_ctx):
         gpu_ctx.synchronize()
         assert rel_maxnorm(Yd.numpy(), Ya.numpy()) <= 1e-12
         assert rel_maxnorm(Xd.numpy(), Xa.numpy()) == 0.0
+
+
+def test_noalloc_apply_hanging_constraints_twice(gpu_ctx):
+    """Parent-to-child distribution and the parent-weighted assembly (the
+    constraint branch Dirichlet-only meshes never reach), with m = 3 and m = 5
+    (odd widths: the scalar paths of the kernels)."""
+    from gbfe import api
+
+    z = np.load(Path(__file__).resolve().parent / "golden" / "case_hanging_p2.npz")
+    cons = M.Constraints(z["cons_rows"], z["cons_sizes"], z["cons_cols"], z["cons_acc"], z["cons_vals"],
+                         z["cons_inh"])
+    assert cons.row_sizes.max() > 0 and np.abs(cons.inhomogeneities).max() > 0
+    basis = api.FEBasisManager(gpu_ctx, z["nd"], z["ids"], int(z["n_dofs"]), cons)
+    H = api.KohnShamOperatorContextFE(basis, z["H"])
+    lib = gpu_ctx.lib
+    for call, X0 in enumerate((z["X"], M.random_block(int(z["n_dofs"]), 5, 901))):
+        m = X0.shape[1]
+        Xa = api.MultiVector(basis, m, init=X0)
+        Ya = api.MultiVector(basis, m)
+        H.apply(Xa, Ya)
+        Xd = api.MultiVector(basis, m, init=X0)
+        Yd = api.MultiVector(basis, m)
+        Yd.setValue(np.nan)
+        rc = lib.gbfe_apply_f64_noalloc(H.h, C.c_void_p(Xd.device_ptr()), C.c_void_p(Yd.device_ptr()), m)
+        assert rc == 0, rc
+        gpu_ctx.synchronize()
+        assert rel_maxnorm(Yd.numpy(), Ya.numpy()) <= 1e-12
+        assert rel_maxnorm(Xd.numpy(), Xa.numpy()) == 0.0
+        if call == 0:  # the reference's own output on this fixture
+            assert rel_maxnorm(Yd.numpy(), z["Y_H"]) <= 1e-12
+            assert rel_maxnorm(Xd.numpy(), z["X_after"]) <= 1e-15
 
 
 def test_noalloc_apply_rejects_oversize(gpu_ctx):
