@@ -222,6 +222,7 @@ struct gbfe_ctx {
   size_t vec_top = 0;
   gbfe::DBuf<double> oz_part;       // per-item Gram partials
   gbfe::DBuf<__nv_bfloat16> oz_tdig;  // slices of the rotation factor
+  gbfe::DBuf<uint8_t> oz_dig;         // digit tiles of the Gram / rotation operands (each value cut once)
 };
 
 struct gbfe_mesh {

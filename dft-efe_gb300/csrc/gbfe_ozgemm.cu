@@ -7,21 +7,30 @@
 // RayleighRitzEigenSolver.t.cpp:233-301):
 //   * Gram matrices  S_o = A_o^T B      (A_o, B: N x m blocks, K = N long)
 //   * rotations      out_o = Y_o T     (Y_o: N x m, T: m x m, K = m short)
-// GB300's FP64 pipe caps both near 1.1 TFLOP/s.  Here:
-//   k_oz_gram: work item = (128 rows of the stacked A_o columns, 64 columns of
-//     B, a range of 512-row K chunks).  Eight producer warps read FP64 rows
-//     (coalesced across columns), cut them into 8 balanced digit slices with
-//     per-column exponents and store canonical K-major tiles; one thread
-//     issues 36 tcgen05.mma per 16-row K step into 8 level accumulators (all
-//     512 TMEM columns).  After every 512 rows (the exact FP32 range) the
-//     producers drain TMEM into FP64 registers.  Each item writes its partial;
+// GB300's FP64 pipe caps both near 1.1 TFLOP/s.  Here each FP64 operand is
+// cut into its 8 digit slices ONCE, by an HBM-bound slicing pass
+// (k_oz_slice_cols: per-column exponents, Gram operands; k_oz_slice_rows:
+// per-row exponents, rotation inputs) that writes the digits straight in the
+// MMA operand layout (canonical K-major tiles, 8 slices of 128 x KC or 64 x KC
+// BF16 per K stage).  The product kernels then only move tiles and multiply:
+//   k_oz_gram: work item = (128 stacked A columns, 64 columns of B, a range of
+//     512-row K chunks).  One warp bulk-copies the A and B digit tiles of each
+//     K stage, one thread issues 36 tcgen05.mma per 16-row K step into 8 level
+//     accumulators (all 512 TMEM columns); after every 512 rows (the exact
+//     FP32 range) eight warps drain TMEM into FP64 registers.  Items are
+//     ordered K range first, so the items sharing a K range (and so the same
+//     digit tiles) run at the same time and read them from L2; their count is
+//     a multiple of the SM count.  Each item writes its partial;
 //     k_oz_gram_final sums the partials in a fixed order (deterministic).
 //   * k_oz_rot: work item = (operand, 128 rows, 64 output columns); the m x m
-//     factor is sliced once per call (k_oz_build_t) and lands by bulk copies;
-//     Y rows are sliced by the producers with per-row exponents; one TMEM pass
-//     covers K = m <= 512.  An operand may be two row blocks side by side
-//     (K = 2m) with its own factor: the residual HY T - MY T diag(eps) of the
-//     rotated block is [HY | MY] [T; -T diag(eps)], one product.
+//     factor is sliced once per call (k_oz_build_t); the row digit tiles and
+//     the factor tiles land by bulk copies; one TMEM pass covers K = m <= 512;
+//     eight warps run the epilogue.  An operand may be two row blocks side by
+//     side (K = 2m) with its own factor: the residual HY T - MY T diag(eps) of
+//     the rotated block is [HY | MY] [T; -T diag(eps)], one product.
+// Slicing each value once instead of once per 64-column output tile is what
+// keeps the tensor pipe fed at m = 512: the digit cut is ~60 integer
+// instructions per value.
 // Every wait is bounded (error status, no hang); TMEM is freed on every exit.
 #include "gbfe_internal.cuh"
 #include "gbfe_oz.cuh"
@@ -63,6 +72,95 @@ __device__ __forceinline__ void store_core_rows(uint8_t *tile, uint32_t part, ui
     *(uint4 *)(tile + s * part + pos) = make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
 }
 
+// 8 consecutive values Y[row][k0 .. k0+8) of a row of the N x K operand made
+// of the rows of Y (columns 0 .. m-1) and, for K = 2m, Y2 side by side; zero
+// past the ends.  Two 16-byte loads per pair of values when the 8 values lie
+// in one block and are 16-byte aligned.
+__device__ __forceinline__ void load_row8(const double *__restrict__ Y, const double *__restrict__ Y2, uint32_t m,
+                                          uint32_t K, uint64_t row, uint64_t N, uint32_t k0, double *v) {
+  if (row >= N) {
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) v[kk] = 0.0;
+    return;
+  }
+  if (k0 + 8 <= K && (k0 + 8 <= m || k0 >= m)) {
+    const double *src = k0 < m ? Y + row * m + k0 : Y2 + row * m + (k0 - m);
+    if (((uintptr_t)src & 15u) == 0) {
+#pragma unroll
+      for (int kk = 0; kk < 8; kk += 2) {
+        const double2 t = __ldg((const double2 *)(src + kk));
+        v[kk] = t.x;
+        v[kk + 1] = t.y;
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk) {
+    const uint32_t k = k0 + kk;
+    v[kk] = k < K ? __ldg(k < m ? Y + row * m + k : Y2 + row * m + (k - m)) : 0.0;
+  }
+}
+
+// Digit tiles of the rows of an N x K operand (see load_row8) with per-row
+// exponents rexp: tile (row tile rt, K stage kc) = 8 slices of 128 x KC BF16
+// in the canonical K-major layout, tiles in (rt, kc) order, rows past N and K
+// values past K zero.  Thread (row r, K group g of 8 values): four threads
+// read a row's 256 contiguous bytes; for each slice, the eight rows of a
+// warp with the same g write one 128-byte core matrix.
+__global__ void __launch_bounds__(256) k_oz_slice_rows(const double *__restrict__ Y, const double *__restrict__ Y2,
+                                                       uint32_t m, uint32_t K, uint64_t N,
+                                                       const int *__restrict__ rexp, uint32_t kchunks,
+                                                       uint64_t ntiles, uint8_t *__restrict__ out) {
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint64_t rt = tile / kchunks;
+    const uint32_t kc = (uint32_t)(tile % kchunks);
+    uint8_t *dst = out + tile * (oz::S * A_PART);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t r = h * 64 + threadIdx.x / 4, g = threadIdx.x % 4;
+      const uint64_t row = rt * 128 + r;
+      double v[8];
+      load_row8(Y, Y2, m, K, row, N, kc * KC + g * 8, v);
+      store_core_rows(dst, A_PART, (r / 8) * SBO + g * LBO + (r % 8) * 16, v, row < N ? rexp[row] : 0);
+    }
+  }
+}
+
+// Digit tiles of the columns of up to two stacked N x ma row-major blocks
+// (column c < ma of A0, else column c - ma of A1; cols columns in all) with
+// per-column exponents cexp: tile (column tile ct of W columns, K stage kc
+// of KC rows) = 8 slices of W x KC BF16, K-major (a core row holds 8
+// consecutive rows of one column), tiles in (ct, kc) order, zero past N
+// and past cols.  A warp's 32 consecutive columns read 256 contiguous
+// bytes per row and write four 128-byte core matrices per slice.
+template <int W>
+__global__ void __launch_bounds__(256) k_oz_slice_cols(const double *__restrict__ A0, const double *__restrict__ A1,
+                                                       uint32_t ma, uint32_t cols, uint64_t N,
+                                                       const int *__restrict__ cexp, uint32_t kchunks,
+                                                       uint64_t ntiles, uint8_t *__restrict__ out) {
+  constexpr uint32_t PART = W * KC * 2;
+  static_assert((W * 4) % 256 == 0, "whole passes of 256 threads");
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint32_t ct = (uint32_t)(tile / kchunks), kc = (uint32_t)(tile % kchunks);
+    uint8_t *dst = out + tile * (oz::S * PART);
+#pragma unroll
+    for (int h = 0; h < W * 4 / 256; ++h) {
+      const uint32_t p = threadIdx.x + 256 * h, c = p % W, g = p / W;
+      const uint32_t col = ct * W + c;
+      const bool cin = col < cols;
+      const double *src = cin ? (col < ma ? A0 + col : A1 + (col - ma)) : nullptr;
+      double v[8];
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        const uint64_t k = (uint64_t)kc * KC + g * 8 + kk;
+        v[kk] = (cin && k < N) ? __ldg(src + k * ma) : 0.0;
+      }
+      store_core_rows(dst, PART, (c / 8) * SBO + g * LBO + (c % 8) * 16, v, cin ? cexp[col] : 0);
+    }
+  }
+}
+
 // The 36 digit-pair products of one 16-row K step as 12 MMAs: slice s of A
 // against the stacked B slices t0..t1 (contiguous in shared memory, so one
 // descriptor with N = 64 (t1 - t0 + 1) <= 256 covers them) lands in the
@@ -95,7 +193,8 @@ struct Barriers {
 };
 
 // after the stages the epilogue scratch (OG_EPI), then the barrier block:
-// full[S], full_b[S], empty[S], tfull, tempty, spare, the TMEM address and the
+// full[S] (unused), full_b[S] (the stage's bulk copies landed), empty[S] (its
+// MMAs finished reading it), tfull, tempty, spare, the TMEM address and the
 // abort flag
 __device__ __forceinline__ Barriers carve(uint8_t *smem) {
   Barriers b;
@@ -113,17 +212,26 @@ __device__ __forceinline__ Barriers carve(uint8_t *smem) {
 
 // ---------------------------------------------------------------- Gram
 struct GramArgs {
-  const double *A0, *A1;  // stacked operands: rows R < ma from A0, then A1
-  uint32_t na, ma;
-  const double *B;
-  uint32_t mb;
-  uint64_t N;
-  const int *aexp;  // [na * ma]
-  const int *bexp;  // [mb]
-  uint32_t row_tiles, col_tiles, splits, chunks, chunks_per_split;
+  const uint8_t *adig;  // A digit tiles [row_tiles][kstages][S][A_PART] (k_oz_slice_cols<128>)
+  const uint8_t *bdig;  // B digit tiles [col_tiles][kstages][S][B_PART] (k_oz_slice_cols<64>)
+  uint32_t kstages;     // K stages of KC rows per column tile (chunks * STAGES_PER_CHUNK)
+  uint32_t row_tiles, col_tiles, splits, chunks;
   double *part;  // [items][OG_N][128] unscaled partial sums
   int *status;
 };
+
+// item it: K range (split) it / tiles, then the (row tile, column tile) pair,
+// column tile fastest; split sp covers chunks [sp chunks / splits, (sp + 1)
+// chunks / splits)
+__device__ __forceinline__ void gram_item(const GramArgs &a, uint32_t it, uint32_t &rt, uint32_t &ct, uint32_t &c0,
+                                          uint32_t &c1) {
+  const uint32_t tiles = a.row_tiles * a.col_tiles;
+  const uint32_t sp = it / tiles, tile = it % tiles;
+  rt = tile / a.col_tiles;
+  ct = tile % a.col_tiles;
+  c0 = (uint32_t)(((uint64_t)sp * a.chunks) / a.splits);
+  c1 = (uint32_t)(((uint64_t)(sp + 1) * a.chunks) / a.splits);
+}
 
 __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -133,7 +241,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
   const uint32_t n_items = a.row_tiles * a.col_tiles * a.splits;
   if (tid == 0) {
     for (int s = 0; s < OG_STAGES; ++s) {
-      mbar_init(&br.full[s], PW);
+      mbar_init(&br.full_b[s], 1);
       mbar_init(&br.empty[s], 1);
     }
     mbar_init(br.tfull, 1);
@@ -158,20 +266,43 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
     *br.abort_flag = 1;
     return false;
   };
-  auto chunk_range = [&](uint32_t it, uint32_t &c0, uint32_t &c1) {
-    const uint32_t sp = it % a.splits;
-    c0 = sp * a.chunks_per_split;
-    c1 = min(a.chunks, c0 + a.chunks_per_split);
-  };
 
-  if (warp == PW + 1) {
+  if (warp == PW) {
+    // ---------------- bulk copies of the A and B digit tiles of each K stage
+    if (lane == 0) {
+      uint32_t q = 0;
+      bool ok = true;
+      for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
+        uint32_t rt, ct, c0, c1;
+        gram_item(a, it, rt, ct, c0, c1);
+        for (uint32_t kc = c0 * STAGES_PER_CHUNK; kc < c1 * STAGES_PER_CHUNK; ++kc, ++q) {
+          const uint32_t s = q % OG_STAGES;
+          if (q >= OG_STAGES && !wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 40)) {
+            ok = false;
+            break;
+          }
+          uint8_t *At = smem + s * OG_STAGE;
+          uint8_t *Bt = At + oz::S * A_PART;
+          mbar_arrive_expect_tx(&br.full_b[s], oz::S * (A_PART + B_PART));
+          const uint8_t *asrc = a.adig + ((uint64_t)rt * a.kstages + kc) * (oz::S * A_PART);
+          const uint8_t *bsrc = a.bdig + ((uint64_t)ct * a.kstages + kc) * (oz::S * B_PART);
+          for (int sl = 0; sl < oz::S; ++sl) {
+            bulk_g2s(At + sl * A_PART, asrc + sl * A_PART, A_PART, &br.full_b[s]);
+            bulk_g2s(Bt + sl * B_PART, bsrc + sl * B_PART, B_PART, &br.full_b[s]);
+          }
+        }
+      }
+      drain_copies(br.full_b, q, OG_STAGES);
+    }
+    __syncwarp();
+  } else if (warp == PW + 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
       uint32_t q = 0, nchunk = 0;
       bool ok = true;
       for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
-        uint32_t c0, c1;
-        chunk_range(it, c0, c1);
+        uint32_t rt, ct, c0, c1;
+        gram_item(a, it, rt, ct, c0, c1);
         for (uint32_t c = c0; c < c1 && ok; ++c, ++nchunk) {
           if (nchunk >= 1 && !wait(br.tempty, (nchunk - 1) & 1, 41)) {
             ok = false;
@@ -180,7 +311,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           for (uint32_t st = 0; st < STAGES_PER_CHUNK; ++st, ++q) {
             const uint32_t s = q % OG_STAGES;
-            if (!wait(&br.full[s], (q / OG_STAGES) & 1, 42)) {
+            if (!wait(&br.full_b[s], (q / OG_STAGES) & 1, 42)) {
               ok = false;
               break;
             }
@@ -197,61 +328,17 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
     }
     __syncwarp();
   } else if (warp < PW) {
-    // ---------------- producers: FP64 rows -> digit tiles; drains
-    const uint32_t ar = tid % 128, ah = tid / 128;  // A: row of the tile, half of the K chunk
-    const uint32_t bj = tid % OG_N, bq = tid / OG_N;  // B: row (column of B), quarter of the K chunk
+    // ---------------- drains: after every 512-row chunk, TMEM -> FP64 registers
     const uint32_t quad = warp % 4, colh = warp / 4;
-    uint32_t q = 0, nchunk = 0;
+    uint32_t nchunk = 0;
     bool ok = true;
     for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
-      const uint32_t tile = it / a.splits;
-      const uint32_t rt = tile / a.col_tiles, ct = tile % a.col_tiles;
-      uint32_t c0, c1;
-      chunk_range(it, c0, c1);
-      // this thread's A row and B row
-      const uint32_t R = rt * 128 + ar;
-      const bool arow = R < a.na * a.ma;
-      const double *Asrc = arow ? ((R < a.ma ? a.A0 : a.A1) + (R % a.ma)) : nullptr;
-      const uint32_t am = a.ma;
-      const int ae = arow ? a.aexp[R] : 0;
-      const uint32_t J = ct * OG_N + bj;
-      const bool brow = J < a.mb;
-      const int be = brow ? a.bexp[J] : 0;
+      uint32_t rt, ct, c0, c1;
+      gram_item(a, it, rt, ct, c0, c1);
       double acc[32];
 #pragma unroll
       for (int i = 0; i < 32; ++i) acc[i] = 0.0;
-      for (uint32_t c = c0; c < c1 && ok; ++c, ++nchunk) {
-        for (uint32_t st = 0; st < STAGES_PER_CHUNK; ++st, ++q) {
-          const uint32_t s = q % OG_STAGES;
-          const uint64_t k0 = (uint64_t)c * CHUNK + st * KC;
-          // A: 16 K values of row ar (two core rows); B: 8 K values of row bj
-          // (one core row) -- loaded before the wait for the ring stage
-          double va[16], vb[8];
-#pragma unroll
-          for (int kk = 0; kk < 16; ++kk) {
-            const uint64_t k = k0 + ah * 16 + kk;
-            va[kk] = (arow && k < a.N) ? __ldg(Asrc + k * am) : 0.0;
-          }
-#pragma unroll
-          for (int kk = 0; kk < 8; ++kk) {
-            const uint64_t k = k0 + bq * 8 + kk;
-            vb[kk] = (brow && k < a.N) ? __ldg(a.B + k * a.mb + J) : 0.0;
-          }
-          if (q >= OG_STAGES) {
-            ok = __all_sync(0xffffffffu, wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 43));
-            if (!ok) break;
-          }
-          uint8_t *At = smem + s * OG_STAGE;
-          uint8_t *Bt = At + oz::S * A_PART;
-          store_core_rows(At, A_PART, (ar / 8) * SBO + (ah * 2) * LBO + (ar % 8) * 16, va, ae);
-          store_core_rows(At, A_PART, (ar / 8) * SBO + (ah * 2 + 1) * LBO + (ar % 8) * 16, va + 8, ae);
-          store_core_rows(Bt, B_PART, (bj / 8) * SBO + bq * LBO + (bj % 8) * 16, vb, be);
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&br.full[s]);
-        }
-        if (!ok) break;
-        // drain this chunk's level sums into the FP64 accumulators
+      for (uint32_t c = c0; c < c1; ++c, ++nchunk) {
         ok = __all_sync(0xffffffffu, wait(br.tfull, nchunk & 1, 44));
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -288,8 +375,9 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_gram(const GramArgs a) {
 // ascending order; then the group sums are added in group order
 constexpr int FINAL_GROUPS = 8;
 __global__ void __launch_bounds__(32 * FINAL_GROUPS) k_oz_gram_final(const double *__restrict__ part, uint32_t na,
-                                                                   uint32_t ma, uint32_t mb, uint32_t col_tiles,
-                                                                   uint32_t splits, const int *__restrict__ aexp,
+                                                                   uint32_t ma, uint32_t mb, uint32_t row_tiles,
+                                                                   uint32_t col_tiles, uint32_t splits,
+                                                                   const int *__restrict__ aexp,
                                                                    const int *__restrict__ bexp, double *S0,
                                                                    double *S1) {
   __shared__ double red[FINAL_GROUPS][32];
@@ -302,9 +390,11 @@ __global__ void __launch_bounds__(32 * FINAL_GROUPS) k_oz_gram_final(const doubl
     double s = 0.0;
     if (t < total) {
       const uint32_t rt = R / 128, r = R % 128, ct = j / OG_N, cj = j % OG_N;
-      const double *p = part + ((uint64_t)(rt * col_tiles + ct) * splits) * TILE + (uint64_t)cj * 128 + r;
+      // item of (split sp, tile) is sp * tiles + tile (k_oz_gram's order)
+      const uint64_t tiles = (uint64_t)row_tiles * col_tiles;
+      const double *p = part + (uint64_t)(rt * col_tiles + ct) * TILE + (uint64_t)cj * 128 + r;
 #pragma unroll 4
-      for (uint32_t sp = g; sp < splits; sp += FINAL_GROUPS) s += __ldg(p + (uint64_t)sp * TILE);
+      for (uint32_t sp = g; sp < splits; sp += FINAL_GROUPS) s += __ldg(p + (uint64_t)sp * tiles * TILE);
     }
     red[g][lane] = s;
     __syncthreads();
@@ -321,13 +411,12 @@ __global__ void __launch_bounds__(32 * FINAL_GROUPS) k_oz_gram_final(const doubl
 
 // ---------------------------------------------------------------- rotation
 struct RotArgs {
-  const double *Y[3];
-  const double *Y2[3];  // second K half of operand o (N x m, K = 2m), or nullptr (K = m)
+  const uint8_t *adig[3];        // row digit tiles of operand o: [row tile][K stage][S][A_PART] (k_oz_slice_rows)
   double *out[3];
   const __nv_bfloat16 *Tdig[3];  // factor of operand o: [col tile][K chunk][slice][OG_N x KC]
   const int *texp[3];            // its per-column exponents [mo]
-  uint32_t kchunks[3];           // its K chunks
-  uint32_t nops, m, mo;          // m: row width of each input block, mo output columns
+  uint32_t kchunks[3];           // its K stages
+  uint32_t nops, mo;             // mo output columns
   uint64_t N;
   const int *rexp;  // [nops][N] row exponents (over both halves of a K = 2m operand)
   uint32_t row_tiles, col_tiles;
@@ -343,7 +432,6 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
   const uint32_t n_items = a.nops * a.row_tiles * a.col_tiles;
   if (tid == 0) {
     for (int s = 0; s < OG_STAGES; ++s) {
-      mbar_init(&br.full[s], PW);
       mbar_init(&full_b[s], 1);
       mbar_init(&br.empty[s], 1);
     }
@@ -369,6 +457,8 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
     *br.abort_flag = 1;
     return false;
   };
+  // item it: (operand, row tile, column tile), column tile fastest, so the
+  // CTAs reading the same row digit tiles run side by side (L2 reuse)
   auto decode = [&](uint32_t it, uint32_t &op, uint32_t &rt, uint32_t &ct) {
     ct = it % a.col_tiles;
     const uint32_t r = it / a.col_tiles;
@@ -377,21 +467,31 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
   };
 
   if (warp == PW) {
-    // ---------------- bulk copies of the sliced factor
+    // ---------------- bulk copies: row digit tiles and factor tiles
     if (lane == 0) {
       uint32_t q = 0;
       for (uint32_t it = blockIdx.x; it < n_items && !*br.abort_flag; it += gridDim.x) {
         uint32_t op, rt, ct;
         decode(it, op, rt, ct);
         const uint32_t nk = a.kchunks[op];
+        bool ok = true;
         for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
           const uint32_t s = q % OG_STAGES;
-          if (q >= OG_STAGES && !wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 51)) break;
-          uint8_t *Bt = smem + s * OG_STAGE + oz::S * A_PART;
-          mbar_arrive_expect_tx(&full_b[s], oz::S * B_PART);
-          const __nv_bfloat16 *src = a.Tdig[op] + ((uint64_t)(ct * nk + kc) * oz::S) * (OG_N * KC);
-          for (int sl = 0; sl < oz::S; ++sl) bulk_g2s(Bt + sl * B_PART, src + (uint64_t)sl * OG_N * KC, B_PART, &full_b[s]);
+          if (q >= OG_STAGES && !wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 51)) {
+            ok = false;
+            break;
+          }
+          uint8_t *At = smem + s * OG_STAGE;
+          uint8_t *Bt = At + oz::S * A_PART;
+          mbar_arrive_expect_tx(&full_b[s], oz::S * (A_PART + B_PART));
+          const uint8_t *asrc = a.adig[op] + ((uint64_t)rt * nk + kc) * (oz::S * A_PART);
+          const __nv_bfloat16 *bsrc = a.Tdig[op] + ((uint64_t)(ct * nk + kc) * oz::S) * (OG_N * KC);
+          for (int sl = 0; sl < oz::S; ++sl) {
+            bulk_g2s(At + sl * A_PART, asrc + sl * A_PART, A_PART, &full_b[s]);
+            bulk_g2s(Bt + sl * B_PART, bsrc + (uint64_t)sl * OG_N * KC, B_PART, &full_b[s]);
+          }
         }
+        if (!ok) break;
       }
       drain_copies(full_b, q, OG_STAGES);
     }
@@ -407,7 +507,7 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
         const uint32_t nk = a.kchunks[it / (a.row_tiles * a.col_tiles)];
         for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
           const uint32_t s = q % OG_STAGES;
-          if (!wait(&br.full[s], (q / OG_STAGES) & 1, 53) || !wait(&full_b[s], (q / OG_STAGES) & 1, 54)) {
+          if (!wait(&full_b[s], (q / OG_STAGES) & 1, 54)) {
             ok = false;
             break;
           }
@@ -424,46 +524,13 @@ __global__ void __launch_bounds__(OG_THREADS, 1) k_oz_rot(const RotArgs a) {
     }
     __syncwarp();
   } else {
-    // ---------------- producers: Y rows -> digit tiles (per-row exponents); epilogue
-    const uint32_t ar = tid % 128, ah = tid / 128;
+    // ---------------- epilogue: levels -> FP64, scaled, whole-row-segment stores
     const uint32_t quad = warp % 4, colh = warp / 4;
-    uint32_t q = 0, li = 0;
+    uint32_t li = 0;
     bool ok = true;
     for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
       uint32_t op, rt, ct;
       decode(it, op, rt, ct);
-      const uint64_t row = (uint64_t)rt * 128 + ar;
-      const bool rin = row < a.N;
-      const double *src = a.Y[op] + row * a.m;
-      const double *src2 = a.Y2[op] ? a.Y2[op] + row * a.m : src;
-      const uint32_t K = a.Y2[op] ? 2 * a.m : a.m;
-      const int re = rin ? a.rexp[(uint64_t)op * a.N + row] : 0;
-      const uint32_t nk = a.kchunks[op];
-      for (uint32_t kc = 0; kc < nk; ++kc, ++q) {
-        const uint32_t s = q % OG_STAGES;
-        // (loading these rows before the stage wait, or a chunk ahead,
-        // measured slower for this kernel)
-        if (q >= OG_STAGES) {
-          ok = __all_sync(0xffffffffu, wait(&br.empty[s], ((q / OG_STAGES) - 1) & 1, 55));
-          if (!ok) break;
-        }
-        uint8_t *At = smem + s * OG_STAGE;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          // 8 K values of row ar: one core row
-          double v[8];
-#pragma unroll
-          for (int kk = 0; kk < 8; ++kk) {
-            const uint32_t k = kc * KC + (ah * 2 + h) * 8 + kk;
-            v[kk] = (rin && k < K) ? __ldg(k < a.m ? src + k : src2 + (k - a.m)) : 0.0;
-          }
-          store_core_rows(At, A_PART, (ar / 8) * SBO + (ah * 2 + h) * LBO + (ar % 8) * 16, v, re);
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&br.full[s]);
-      }
-      if (!ok) break;
       ok = __all_sync(0xffffffffu, wait(br.tfull, li & 1, 56));
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -595,6 +662,17 @@ bool oz_gemm_supported(gbfe_ctx *ctx, uint32_t m) {
   return ctx->cc_major >= 10 && m > 0 && m <= (uint32_t)oz::K_EXACT;
 }
 
+// Item count of the Gram product: splits of the K range per (row tile, col
+// tile) pair such that tiles x splits is a multiple of the SM count (every
+// SM gets the same number of items), with at least one 512-row chunk per
+// split where the K range allows it
+static uint32_t gram_splits(uint32_t tiles, uint32_t chunks, uint32_t sms) {
+  const uint32_t lo = std::max<uint32_t>(1, (sms + tiles - 1) / tiles);
+  for (uint32_t sp = lo; sp <= std::min<uint32_t>(chunks, 8 * lo); ++sp)
+    if (((uint64_t)tiles * sp) % sms == 0) return sp;
+  return std::min(lo, std::max<uint32_t>(1, chunks));
+}
+
 // S_o (ma x mb, column-major) = A_o^T B for o < na (na <= 2); A_o: N x ma, B: N x mb, row-major blocks.
 // bexp: the per-column exponents of B computed beforehand (nullptr: here)
 void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, const double *B, uint32_t mb,
@@ -604,12 +682,9 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
   const uint32_t rows = na * ma;
   const uint32_t row_tiles = (rows + 127) / 128, col_tiles = (mb + OG_N - 1) / OG_N;
   const uint32_t chunks = (uint32_t)std::max<uint64_t>(1, (N + CHUNK - 1) / CHUNK);
+  const uint32_t kstages = chunks * STAGES_PER_CHUNK;
   const uint32_t tiles = row_tiles * col_tiles;
-  // about one item per SM: every item is a few 512-row chunks, partials stay few
-  const uint32_t want = std::max<uint32_t>(1, ((uint32_t)ctx->sm_count + tiles - 1) / tiles);
-  const uint32_t splits_req = std::min(chunks, want);
-  const uint32_t cps = (chunks + splits_req - 1) / splits_req;
-  const uint32_t splits = (chunks + cps - 1) / cps;
+  const uint32_t splits = gram_splits(tiles, chunks, (uint32_t)ctx->sm_count);
   const uint32_t items = tiles * splits;
   // exponents
   const unsigned nb = (unsigned)std::min<uint64_t>(8 * (uint64_t)ctx->sm_count, std::max<uint64_t>(1, N));
@@ -628,9 +703,24 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
                                                                                     ctx->oz_exp.p + rows);
     count_launch(ctx, 2);
   }
+  // the digit tiles of both operands, each value cut once
+  const uint64_t a_bytes = (uint64_t)row_tiles * kstages * oz::S * A_PART;
+  const uint64_t b_bytes = (uint64_t)col_tiles * kstages * oz::S * B_PART;
+  ctx->oz_dig.ensure(a_bytes + b_bytes);
+  uint8_t *adig = ctx->oz_dig.p, *bdig = ctx->oz_dig.p + a_bytes;
+  {
+    ProfScope prof(ctx, "slice_f64_oz", 0.0, 8.0 * (double)N * (rows + mb) + (double)(a_bytes + b_bytes));
+    const uint64_t ta = (uint64_t)row_tiles * kstages, tb = (uint64_t)col_tiles * kstages;
+    const unsigned gs = (unsigned)(ctx->sm_count * 8);
+    k_oz_slice_cols<128><<<(unsigned)std::min<uint64_t>(ta, gs), 256, 0, ctx->stream>>>(
+        A[0], na > 1 ? A[1] : A[0], ma, rows, N, ctx->oz_exp.p, kstages, ta, adig);
+    k_oz_slice_cols<64><<<(unsigned)std::min<uint64_t>(tb, gs), 256, 0, ctx->stream>>>(
+        B, B, mb, mb, N, ctx->oz_exp.p + rows, kstages, tb, bdig);
+    check_launch(ctx, "oz_slice_cols");
+    count_launch(ctx, 1);
+  }
   ctx->oz_part.ensure((size_t)items * TILE);
-  GramArgs args{A[0], na > 1 ? A[1] : A[0], na, ma, B, mb, N, ctx->oz_exp.p, ctx->oz_exp.p + rows, row_tiles,
-                col_tiles, splits, chunks, cps, ctx->oz_part.p, ctx->status.p};
+  GramArgs args{adig, bdig, kstages, row_tiles, col_tiles, splits, chunks, ctx->oz_part.p, ctx->status.p};
   const uint32_t grid = std::min<uint32_t>(items, (uint32_t)ctx->sm_count);
   {
     ProfScope prof(ctx, "gram_f64_oz", 2.0 * (double)N * rows * mb, 8.0 * (double)N * (rows + mb));
@@ -639,17 +729,20 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
   }
   const uint64_t total = (uint64_t)rows * mb;
   k_oz_gram_final<<<(unsigned)std::min<uint64_t>((total + 31) / 32, (uint64_t)ctx->sm_count * 8), 32 * FINAL_GROUPS, 0,
-                    ctx->stream>>>(ctx->oz_part.p, na, ma, mb, col_tiles, splits,
-                                                               ctx->oz_exp.p, ctx->oz_exp.p + rows, S[0],
-                                                               na > 1 ? S[1] : S[0]);
+                    ctx->stream>>>(ctx->oz_part.p, na, ma, mb, row_tiles, col_tiles, splits, ctx->oz_exp.p,
+                                   ctx->oz_exp.p + rows, S[0], na > 1 ? S[1] : S[0]);
   check_launch(ctx, "oz_gram_final");
 }
 
-// out_o (N x mo, row-major) = Y_o (N x m, row-major) T (m x mo, column-major) for o < nops (<= 3)
-// per-row exponents of the rotation inputs (they depend on Y alone, so a
-// caller can issue this before T is known)
-// (pair12: two operands, Y[0] and the rows of Y[1], Y[2] side by side, as
-// oz_rotate_residual takes them)
+// Row exponents and row digit tiles of the rotation inputs (they depend on Y
+// alone, so a caller can issue this before T is known).  Operand o < nops is
+// Y[o] (K = m); with pair12 there are two operands, Y[0] (K = m) and the rows
+// of Y[1], Y[2] side by side (K = 2m), as oz_rotate_residual takes them.
+// Operand o's tiles start at byte rot_dig_offset(o) of ctx->oz_dig.
+static uint64_t rot_tiles_bytes(uint64_t N, uint32_t K) {
+  return ((N + 127) / 128) * (uint64_t)((K + KC - 1) / KC) * oz::S * A_PART;
+}
+
 void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N, bool pair12) {
   if (pair12) nops = 2;
   ctx->oz_rexp.ensure((size_t)nops * N);
@@ -657,6 +750,21 @@ void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t 
                 ctx->stream>>>(Y[0], nops > 1 ? Y[1] : Y[0], (nops > 2 || pair12) ? Y[2] : Y[0], nops, m, N, pair12,
                                ctx->oz_rexp.p);
   count_launch(ctx, 1);
+  uint64_t total = 0;
+  for (uint32_t o = 0; o < nops; ++o) total += rot_tiles_bytes(N, (pair12 && o == 1) ? 2 * m : m);
+  ctx->oz_dig.ensure(total);
+  ProfScope prof(ctx, "slice_f64_oz", 0.0, (double)N * m * 8.0 * (pair12 ? 3 : nops) + (double)total);
+  uint64_t off = 0;
+  for (uint32_t o = 0; o < nops; ++o) {
+    const bool two = pair12 && o == 1;
+    const uint32_t K = two ? 2 * m : m, kchunks = (K + KC - 1) / KC;
+    const uint64_t ntiles = ((N + 127) / 128) * (uint64_t)kchunks;
+    k_oz_slice_rows<<<(unsigned)std::min<uint64_t>(ntiles, (uint64_t)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+        Y[o], two ? Y[2] : Y[o], m, K, N, ctx->oz_rexp.p + (uint64_t)o * N, kchunks, ntiles, ctx->oz_dig.p + off);
+    off += rot_tiles_bytes(N, K);
+  }
+  check_launch(ctx, "oz_slice_rows");
+  count_launch(ctx, nops - 1);
 }
 
 void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const double *const *Y, double *const *out,
@@ -673,14 +781,13 @@ void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const do
   count_launch(ctx, 1);
   RotArgs args{};
   for (uint32_t o = 0; o < nops; ++o) {
-    args.Y[o] = Y[o];
+    args.adig[o] = ctx->oz_dig.p + (uint64_t)o * rot_tiles_bytes(N, m);
     args.out[o] = out[o];
     args.Tdig[o] = ctx->oz_tdig.p;
     args.texp[o] = ctx->oz_exp.p;
     args.kchunks[o] = kchunks;
   }
   args.nops = nops;
-  args.m = m;
   args.mo = mo;
   args.N = N;
   args.rexp = ctx->oz_rexp.p;
@@ -717,9 +824,8 @@ void oz_rotate_residual(gbfe_ctx *ctx, const double *T, const double *eps, uint3
                                                              ctx->oz_tdig.p + fac0);
   count_launch(ctx, 2);
   RotArgs args{};
-  args.Y[0] = Y;
-  args.Y[1] = HY;
-  args.Y2[1] = MY;
+  args.adig[0] = ctx->oz_dig.p;
+  args.adig[1] = ctx->oz_dig.p + rot_tiles_bytes(N, m);
   args.out[0] = X;
   args.out[1] = R;
   args.Tdig[0] = ctx->oz_tdig.p;
@@ -729,7 +835,6 @@ void oz_rotate_residual(gbfe_ctx *ctx, const double *T, const double *eps, uint3
   args.kchunks[0] = k0;
   args.kchunks[1] = k1;
   args.nops = 2;
-  args.m = m;
   args.mo = m;
   args.N = N;
   args.rexp = ctx->oz_rexp.p;
