@@ -154,7 +154,8 @@ struct GraphProf {
 struct TcTune {
   uint32_t N = 0, stages = 0;
   float ms = 0.f;
-  uint32_t occ = 2;  // resident CTAs per SM the kernel is compiled for (2 or 3)
+  uint32_t occ = 2;   // resident CTAs per SM the kernel is compiled for (2 or 3)
+  uint32_t nbuf = 0;  // TMEM accumulator buffers: 0 two where they fit, 1 one (more CTAs per SM)
 };
 
 // Pinned host staging for small host-to-device copies issued inside a solve:

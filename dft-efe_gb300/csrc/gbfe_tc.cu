@@ -638,7 +638,7 @@ static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, f
                            uint32_t ncell, uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0,
                            uint32_t stages_req = 0, const __nv_bfloat16 *tiles = nullptr, const float *xsub = nullptr,
                            uint32_t sub_begin = 0, uint32_t sub_n = 0, uint32_t occ_req = 0,
-                           cudaStream_t stream = nullptr) {
+                           cudaStream_t stream = nullptr, uint32_t nbuf_req = 0) {
   gbfe_mesh *me = op->mesh;
   const uint32_t m = X->m;
   if (!stream) stream = ctx->stream;
@@ -648,6 +648,7 @@ static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, f
       N_req = it->second.N;
       stages_req = it->second.stages;
       occ_req = it->second.occ;
+      nbuf_req = it->second.nbuf;
     }
   }
   const uint32_t occ = occ_req >= 3 ? 3u : 2u;
@@ -662,7 +663,10 @@ static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, f
   while (stages > 2 && stages * stage_bytes + reserve > 227 * 1024) --stages;
   GBFE_REQUIRE(stages * stage_bytes + reserve <= 227 * 1024, "tensor-core tile does not fit in shared memory");
   const uint32_t smem = stages * stage_bytes + reserve;
-  const uint32_t nbuf = (2 * mtiles * N <= 512) ? 2 : 1;
+  // two TMEM accumulators (the epilogue of one item overlaps the MMAs of the
+  // next) where they fit, unless one was asked for (half the columns: room
+  // for another CTA on the SM)
+  const uint32_t nbuf = (2 * mtiles * N <= 512 && nbuf_req != 1) ? 2 : 1;
   uint32_t cols = 32;
   while (cols < nbuf * mtiles * N) cols *= 2;
   // CTAs per SM: shared memory (228 KB per SM, 1 KB of it reserved per CTA),
@@ -817,14 +821,17 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
     for (uint32_t N : {16u, 32u, 64u, 128u, 256u}) {
       if (N > std::max<uint32_t>(16, (m + 15) / 16 * 16) && N != 16) continue;
       for (uint32_t st : {2u, 3u, 4u})
-      for (uint32_t occ : {2u, 3u}) {
+      for (uint32_t occ : {2u, 3u})
+      for (uint32_t nb : {0u, 1u}) {
+        if (nb == 1 && 2 * mtiles * N > 512) continue;  // one buffer already
         // warm; a shape that cannot hold 3 CTAs per SM runs as the 2-CTA one: not timed twice
-        const uint32_t used =
-            launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st, nullptr, nullptr, 0, 0, occ);
+        const uint32_t used = launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st, nullptr,
+                                         nullptr, 0, 0, occ, ctx->stream, nb);
         if (occ > 2 && used < occ) continue;
         GBFE_CUDA(cudaEventRecord(e0, ctx->stream));
         for (int r = 0; r < 3; ++r)
-          launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st, nullptr, nullptr, 0, 0, occ);
+          launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st, nullptr, nullptr, 0, 0, occ,
+                     ctx->stream, nb);
         GBFE_CUDA(cudaEventRecord(e1, ctx->stream));
         GBFE_CUDA(cudaEventSynchronize(e1));
         int st_word = 0;
@@ -841,13 +848,14 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
           best.N = N;
           best.stages = st;
           best.occ = occ;
+          best.nbuf = nb;
         }
       }
     }
     ctx->tc_tune[std::make_tuple(nd_max, mtiles, m)] = best;
     log.push_back("tc2 " + std::to_string(nd_max) + " " + std::to_string(mtiles) + " " + std::to_string(m) + " " +
                   std::to_string(best.N) + " " + std::to_string(best.stages) + " " + std::to_string(best.occ) + " " +
-                  std::to_string(best.ms));
+                  std::to_string(best.ms) + " " + std::to_string(best.nbuf));
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -23,6 +23,10 @@ WORKLOADS = {
     "cfg2c": dict(n=12, p=4, L=24.0, atoms=8, Z=6.0, rc=0.4, layout="uniform_inner_half", nq=None, m=64,
                   seed=12347),
     "cfg3": dict(n=24, p=5, L=40.0, atoms=64, Z=4.0, rc=0.5, layout="jittered_cubic", nq=None, m=512, seed=12348),
+    # the same cells (degree 5, 216 dofs) and block width on an 8^3 mesh: a
+    # case small enough for a full profiler capture (X 141 MB, tiles 95 MB)
+    "cfg3s": dict(n=8, p=5, L=40.0 / 3.0, atoms=8, Z=4.0, rc=0.5, layout="jittered_cubic", nq=None, m=512,
+                  seed=12348),
     "cfg2": dict(enriched=True, m=64),  # gbfe.enrichment.config2(): 12^3 cells of degree 4 + 40 enrichment dofs
 }
 
@@ -35,6 +39,7 @@ def main() -> None:
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--filter", type=int, default=0,
                     help="time the mixed residual Chebyshev filter of this degree instead of one apply")
+    ap.add_argument("--tune", action="store_true", help="autotune the split-BF16 launch shape first (as bench.py)")
     ap.add_argument("--passes", type=int, default=0,
                     help="time this many fused mixed ChFSI passes (degree 16, sliced FP64 stages) instead")
     args = ap.parse_args()
@@ -64,6 +69,7 @@ def main() -> None:
         ctx.set_tensor_cores(0)
     elif args.precision == "mixed_v1":
         ctx.set_tensor_cores(1)
+    tuned = api.autotune(H, m) if (args.tune and args.precision == "mixed") else None
     for _ in range(3):
         H.apply(X, Y)
     ctx.synchronize()
@@ -85,7 +91,7 @@ def main() -> None:
         "config": args.config, "precision": args.precision, "m": m, "n_dofs": prob.n_dofs, "cells": prob.n_cells,
         "nd": int(prob.nd_per_cell.max()), "cell_kernel_ms": k_ms, "apply_wall_ms": wall * 1e3,
         "cell_kernel_tflops": flops / (k_ms * 1e-3) / 1e12, "cell_kernel_gbs": bytes_ / (k_ms * 1e-3) / 1e9,
-        "algorithmic_gflop": flops / 1e9, "algorithmic_mb": bytes_ / 1e6,
+        "algorithmic_gflop": flops / 1e9, "algorithmic_mb": bytes_ / 1e6, "tuned": tuned,
     }))
 
 

@@ -48,6 +48,24 @@ else
   rm -f "$NLOUT"
 fi
 
+# The apply() member of basis::OrthoEFEOverlapInverseOpContextGLL (the direct
+# branch: GLL diagonal on every dof, dense inverse enrichment block on the
+# enrichment ids), cut from the reference's .t.cpp and wrapped in its
+# namespaces.  The constructors need deal.II basis data and are left out: the
+# harness declaration ref_harness/shadow/basis/OrthoEFEOverlapInverseOpContextGLL.h
+# takes the diagonal and the block instead.
+EFESRC="$SRC/basis/OrthoEFEOverlapInverseOpContextGLL.t.cpp"
+EFEOUT="$OUT/patched/OrthoEFEOverlapInverseOpContextGLL.apply.t.cpp"
+if sed -n '1173p' "$EFESRC" | grep -q 'template <typename ValueTypeOperator,' &&
+   sed -n '1182p' "$EFESRC" | grep -q 'dim>::apply(' && sed -n '1305p' "$EFESRC" | grep -q '^    }$' &&
+   sed -n '1306p' "$EFESRC" | grep -q 'namespace basis'; then
+  { echo 'namespace dftefe { namespace basis {'; sed -n '1173,1305p' "$EFESRC"; echo '} }'; } > "$EFEOUT.tmp"
+  if ! cmp -s "$EFEOUT.tmp" "$EFEOUT"; then mv "$EFEOUT.tmp" "$EFEOUT"; else rm -f "$EFEOUT.tmp"; fi
+else
+  echo "OrthoEFEOverlapInverseOpContextGLL.t.cpp layout differs from the expected one; OrthoEFE inverse left out" >&2
+  rm -f "$EFEOUT"
+fi
+
 CXXFLAGS="-std=c++17 -O2 -DNDEBUG -w -I$HERE/ref_harness/shadow -I$SRC"
 SOURCES=(
   utils/Exceptions.cpp utils/MemoryTransfer.cpp utils/MPITypes.cpp utils/MPIRequestersNBX.cpp

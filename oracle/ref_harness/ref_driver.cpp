@@ -11,6 +11,8 @@
 //   linearAlgebra::ChebyshevFilter (ChebyshevFilter.t.cpp:39-135)
 //   linearAlgebra::CGLinearSolver::solve (CGLinearSolver.t.cpp:68-313)
 //   linearAlgebra::PreconditionerJacobi (PreconditionerJacobi.t.cpp)
+//   basis::OrthoEFEOverlapInverseOpContextGLL::apply, direct branch
+//       (OrthoEFEOverlapInverseOpContextGLL.t.cpp:1173-1305)
 //   basis::AtomCenterNonLocalOpContextFE apply-side members
 //       (AtomCenterNonLocalOpContextFE.t.cpp:36-265, :714-1045), standalone
 //       and fused into the KS apply through an ONCV component
@@ -26,9 +28,12 @@
 //            cons_acc.u32, cons_vals.f64, cons_inh.f64, X.f64, eig.f64, b.f64
 //            optional nonlocal part: nl_meta.txt (n_proj), nl_np.u32,
 //            nl_pids.u32, nl_c.f64, nl_v.f64
+//            optional enrichment block: efe_meta.txt (first enrichment id,
+//            count), efe_blk.f64 (inverse enrichment overlap, column-major)
 //   outputs: Y_H.f64, X_after.f64, Y_M.f64, Y_Minv.f64, Y_rfilter.f64,
 //            Y_filter.f64, x_cg.f64, cg.txt; with the nonlocal inputs also
-//            Y_nl.f64 (standalone) and Y_Hnl.f64 (H + nonlocal, fused)
+//            Y_nl.f64 (standalone) and Y_Hnl.f64 (H + nonlocal, fused); with
+//            the enrichment block Y_Minv_efe.f64
 #include <fstream>
 #include <ksdft/KohnShamOperatorContextFE.h>
 #include <basis/ConstraintsInternal.h>
@@ -36,6 +41,7 @@
 #include <linearAlgebra/CGLinearSolver.h>
 #include <linearAlgebra/PreconditionerJacobi.h>
 #include <linearAlgebra/LinearSolverFunction.h>
+#include <basis/OrthoEFEOverlapInverseOpContextGLL.h>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -221,6 +227,24 @@ int main(int argc, char **argv) {
     opMinv.apply(X, Y, true, false);
     write_bin(d + "Y_Minv.f64", Y.data(), (size_t)N * m);
   }
+#ifdef GBFE_REF_HAS_ORTHO_EFE_INVERSE
+  {  // OrthoEFE inverse overlap (enriched meshes: the enrichment ids are the last ones)
+    std::ifstream em(d + "efe_meta.txt");
+    size_type enrBegin = 0, nEnr = 0;
+    if (em >> enrBegin >> nEnr) {
+      basis.ownedRanges = {{0, enrBegin}, {enrBegin, enrBegin + nEnr}};
+      basis::EFEGlobalRanges gr;
+      gr.ranges = basis.ownedRanges;
+      auto blk = read_bin<double>(d + "efe_blk.f64");
+      using EfeInv = basis::OrthoEFEOverlapInverseOpContextGLL<double, double, HOST, 3>;
+      EfeInv opEfe(basis, gr, minv, nEnr, blk, ctx);
+      MV X(basis.pattern, ctx, m, 0.0), Y(basis.pattern, ctx, m, 0.0);
+      load_mv(X, X0);
+      opEfe.apply(X, Y, true, false);
+      write_bin(d + "Y_Minv_efe.f64", Y.data(), (size_t)N * m);
+    }
+  }
+#endif
 #ifdef GBFE_REF_HAS_NONLOCAL
   {  // nonlocal part: standalone and fused into the KS apply
     std::ifstream nm(d + "nl_meta.txt");

@@ -20,11 +20,14 @@ struct FEBasisManager {
   utils::MemoryStorage<size_type, memorySpace> cellIds;
   std::shared_ptr<const utils::mpi::MPIPatternP2P<memorySpace>> pattern;
   const ConstraintsLocal<ValueTypeBasisCoeff, memorySpace> *constraints = nullptr;
+  // locally owned (classical, enrichment) id ranges, as an EFE basis reports them
+  std::vector<std::pair<global_size_type, global_size_type>> ownedRanges;
   size_type nLocallyOwnedCells() const { return nCells; }
   size_type nLocallyOwnedCellDofs(size_type c) const { return cellDofs[c]; }
   const size_type *locallyOwnedCellLocalDofIdsBegin() const { return cellIds.data(); }
   std::shared_ptr<const utils::mpi::MPIPatternP2P<memorySpace>> getMPIPatternP2P() const { return pattern; }
   const ConstraintsLocal<ValueTypeBasisCoeff, memorySpace> &getConstraints() const { return *constraints; }
+  std::vector<std::pair<global_size_type, global_size_type>> getLocallyOwnedRanges() const { return ownedRanges; }
   const BasisDofHandler &getBasisDofHandler() const;
 };
 }  // namespace basis

@@ -12,6 +12,9 @@ and the reference outputs:
   x_cg, cg_ok    Jacobi-preconditioned CGLinearSolver on K
   Y_nl, Y_Hnl    (nonlocal cases) AtomCenterNonLocalOpContextFE::apply alone,
                  and the KS apply of H with the nonlocal part fused in
+  Y_Minv_efe     (enriched cases) OrthoEFEOverlapInverseOpContextGLL::apply:
+                 GLL diagonal inverse plus the dense inverse enrichment block
+                 (inputs enr_begin, enr_blk)
 
 Run (in a checkout where the reference sources exist):
     bash oracle/build_ref.sh && python tests/golden/make_golden.py [case names]
@@ -34,7 +37,7 @@ HERE = Path(__file__).resolve().parent
 
 
 def run_case(name, nd, ids, N, cons, H, Mm, K, minv, jacdiag, X, eig, b, degree, wl, wu, uu,
-             max_iter=3000, abs_tol=1e-14, rel_tol=1e-11, div_tol=1e8, nl=None):
+             max_iter=3000, abs_tol=1e-14, rel_tol=1e-11, div_tol=1e8, nl=None, efe=None):
     m = X.shape[1]
     nrhs = b.shape[1]
     with tempfile.TemporaryDirectory() as d:
@@ -58,6 +61,11 @@ def run_case(name, nd, ids, N, cons, H, Mm, K, minv, jacdiag, X, eig, b, degree,
                 np.ascontiguousarray(arr, dtype=dt).tofile(d / fname)
             extra = dict(nl_n_proj=np.array(nl.n_proj), nl_np=nl.proj_per_cell, nl_pids=nl.proj_ids,
                          nl_c=nl.cell_c, nl_v=nl.coupling)
+        if efe is not None:
+            enr_begin, blk = efe  # blk: the inverse enrichment overlap block, row-major
+            (d / "efe_meta.txt").write_text(f"{enr_begin} {blk.shape[0]}\n")
+            np.ascontiguousarray(blk.T, dtype=np.float64).tofile(d / "efe_blk.f64")  # column-major
+            extra.update(enr_begin=np.array(enr_begin), enr_blk=blk)
         subprocess.run([str(DRIVER), str(d)], check=True)
         rd = lambda f, shape: np.fromfile(d / f, dtype=np.float64).reshape(shape)  # noqa: E731
         out = dict(Y_H=rd("Y_H.f64", (N, m)), X_after=rd("X_after.f64", (N, m)), Y_M=rd("Y_M.f64", (N, m)),
@@ -68,6 +76,10 @@ def run_case(name, nd, ids, N, cons, H, Mm, K, minv, jacdiag, X, eig, b, degree,
             if not (d / "Y_nl.f64").exists():
                 sys.exit("ref_driver was built without the nonlocal part (see oracle/build_ref.sh)")
             out.update(Y_nl=rd("Y_nl.f64", (N, m)), Y_Hnl=rd("Y_Hnl.f64", (N, m)))
+        if efe is not None:
+            if not (d / "Y_Minv_efe.f64").exists():
+                sys.exit("ref_driver was built without the OrthoEFE inverse (see oracle/build_ref.sh)")
+            out.update(Y_Minv_efe=rd("Y_Minv_efe.f64", (N, m)))
     np.savez_compressed(HERE / f"{name}.npz", nd=nd.astype(np.uint32), ids=ids.astype(np.uint32), n_dofs=np.array(N),
                         cons_rows=cons.row_ids, cons_sizes=cons.row_sizes, cons_cols=cons.col_ids,
                         cons_acc=cons.row_acc, cons_vals=cons.col_values, cons_inh=cons.inhomogeneities,
@@ -111,6 +123,24 @@ def fe_case(name, n, p, L, atoms, seed, m, degree, hanging=False, nonlocal_part=
                                                 prob.constraints), X, eig, b, degree, wl, wu, uu, nl=nl)
 
 
+def enriched_case(name, n, p, L, atoms, seed, m, degree):
+    """Orthogonalised enrichment (gbfe/enrichment.py): uneven cells, the
+    enrichment ids after the classical ones, the OrthoEFE inverse overlap."""
+    from gbfe import enrichment
+
+    prob = enrichment.enriched_problem(n, p, L, atoms, 4.0, 0.5, seed)
+    rng = np.random.default_rng(seed + 1)
+    X = rng.standard_normal((prob.n_dofs, m))
+    eig = np.sort(rng.uniform(-3.0, 0.5, m))
+    b = rng.standard_normal((prob.n_dofs, 2))
+    b[prob.constraints.row_ids] = 0.0
+    wl, wu, uu = -4.0, 1.0, 40.0 * p * p / (L / n) ** 2
+    run_case(name, prob.nd_per_cell, prob.cell_dof_ids, prob.n_dofs, prob.constraints, prob.H, prob.M, prob.K,
+             1.0 / prob.m_gll_diag, jacobi_diag(prob.nd_per_cell, prob.cell_dof_ids, prob.K, prob.n_dofs,
+                                                prob.constraints), X, eig, b, degree, wl, wu, uu,
+             efe=(int(prob.extra["enr_begin"]), prob.extra["enr_block_inv"]))
+
+
 def variable_case(name, seed):
     """Uneven cell sizes (as enriched cells have) with SPD cell matrices."""
     rng = np.random.default_rng(seed)
@@ -150,6 +180,7 @@ if __name__ == "__main__":
         "case_nonlocal_p3": lambda n: fe_case(n, 2, 3, 8.0, 2, 105, 5, 6, nonlocal_part=True),
         "case_nonlocal_hanging_p2": lambda n: fe_case(n, 3, 2, 6.0, 2, 106, 4, 5, hanging=True,
                                                       nonlocal_part=True),
+        "case_enriched_p2": lambda n: enriched_case(n, 3, 2, 8.0, 2, 107, 5, 6),
     }
     for name in (sys.argv[1:] or list(cases)):
         cases[name](name)

@@ -140,3 +140,37 @@ def test_gpu_nonlocal_matches_reference(gpu_ctx, path):
     X.copy_from(z["X"])
     H.apply(X, Y)
     assert rel_maxnorm(Y.numpy(), z["Y_Hnl"]) <= 1e-12
+
+
+ENRICHED = [p for p in GOLDEN if "enriched" in p.stem]
+
+
+def test_enriched_fixtures_present():
+    assert len(ENRICHED) >= 1
+
+
+@pytest.mark.parametrize("path", ENRICHED, ids=[p.stem for p in ENRICHED])
+def test_oracle_ortho_efe_inverse_matches_reference(path):
+    """OrthoEFEOverlapInverseOpContextGLL::apply (direct branch) as the
+    reference computes it: GLL diagonal inverse on every dof, the enrichment
+    rows replaced by the dense inverse block times X's enrichment rows."""
+    z = load(path)
+    s = O.OracleSystem(z["nd"], z["ids"], int(z["n_dofs"]), z["cons"])
+    op = s.diag_block_op(z["minv"], int(z["enr_begin"]), z["enr_blk"])
+    assert rel_maxnorm(s.apply(op, z["X"].copy()), z["Y_Minv_efe"]) <= 1e-14
+    # the block changes the enrichment rows
+    assert rel_maxnorm(z["Y_Minv_efe"], z["Y_Minv"]) > 1e-3
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", ENRICHED, ids=[p.stem for p in ENRICHED])
+def test_gpu_ortho_efe_inverse_matches_reference(gpu_ctx, path):
+    from gbfe import api
+
+    z = load(path)
+    basis = api.FEBasisManager(gpu_ctx, z["nd"], z["ids"], int(z["n_dofs"]), z["cons"])
+    Mi = api.OrthoEFEOverlapInverseOpContextGLL(basis, 1.0 / z["minv"], int(z["enr_begin"]), z["enr_blk"])
+    m = z["X"].shape[1]
+    X, Y = api.MultiVector(basis, m, init=z["X"]), api.MultiVector(basis, m)
+    Mi.apply(X, Y)
+    assert rel_maxnorm(Y.numpy(), z["Y_Minv_efe"]) <= 1e-14
