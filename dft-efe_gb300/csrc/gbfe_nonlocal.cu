@@ -258,6 +258,8 @@ int gbfe_nonlocal_upload(gbfe_mesh *mesh, uint32_t n_proj, const uint32_t *proj_
 }
 
 int gbfe_nonlocal_destroy(gbfe_nl *nl) {
+  if (!nl) return GBFE_OK;
+  cudaStreamSynchronize(nl->mesh->ctx->stream);  // no launch of the context still reads its arrays
   delete nl;
   return GBFE_OK;
 }

@@ -65,6 +65,9 @@ struct Request {
 
 struct Slot {
   gbfe_ctx *ctx = nullptr;
+  // Poisson requests admitted together (same iteration limit and
+  // tolerances) run as one batched solve; empty for a single request
+  std::vector<Request *> batch;
   // Poisson requests run on this stream of the highest priority: when a
   // KS solve's kernel ends, the block scheduler starts the short requests'
   // pending blocks first, so they are not queued behind whole KS passes
@@ -87,6 +90,8 @@ struct gbfe_server {
   bool stop = false;
   int inject_alloc_failures = 0;  // host-side fault injection: fail the next N uploads
   uint64_t admitted = 0, completed = 0, rejected = 0;
+  uint64_t poisson_batches = 0, poisson_batched = 0;  // batched solves, and the requests they carried
+  uint32_t max_poisson_batch = 32;
 };
 
 namespace {
@@ -194,6 +199,102 @@ void run_request(gbfe_server *sv, gbfe_ctx *ctx, Request *r) {
   gbfe_mesh_destroy(me);
 }
 
+// Poisson requests of one batch as a single block-diagonal solve: the meshes,
+// constraints, indexed Laplace matrices, Jacobi diagonals and right-hand
+// sides are concatenated (dof, constraint-column and matrix indices shifted),
+// and gbfe_pcg_solve_batched advances every instance in the same kernels.
+// Its per-instance scalars and fixed per-instance reductions make each
+// instance's arithmetic the same as in a solve of its own, so results do not
+// depend on the batch.  A batch is not cancellable once it runs.
+void run_poisson_batch(gbfe_server *sv, gbfe_ctx *ctx, const std::vector<Request *> &batch) {
+  int rc = GBFE_OK;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->inject_alloc_failures > 0) {
+      --sv->inject_alloc_failures;
+      rc = GBFE_ERR_ALLOC;
+    }
+  }
+  if (rc != GBFE_OK) {
+    for (Request *r : batch) {
+      r->status = rc;
+      r->message = "injected allocation failure";
+    }
+    return;
+  }
+  std::vector<uint32_t> nd, ids, rows, rsz, cols, racc, c2m;
+  std::vector<double> cvals, inh, K, diag, b;
+  std::vector<uint64_t> off{0};
+  uint64_t dofs = 0;
+  uint32_t mats = 0, nnz = 0;
+  for (const Request *r : batch) {
+    nd.insert(nd.end(), r->nd.begin(), r->nd.end());
+    for (uint32_t g : r->ids) ids.push_back((uint32_t)(g + dofs));
+    for (uint32_t g : r->rows) rows.push_back((uint32_t)(g + dofs));
+    rsz.insert(rsz.end(), r->rsz.begin(), r->rsz.end());
+    for (uint32_t g : r->cols) cols.push_back((uint32_t)(g + dofs));
+    for (uint32_t a : r->racc) racc.push_back(a + nnz);
+    cvals.insert(cvals.end(), r->cvals.begin(), r->cvals.end());
+    inh.insert(inh.end(), r->inh.begin(), r->inh.end());
+    K.insert(K.end(), r->K.begin(), r->K.end());
+    for (uint32_t u : r->cell_to_mat) c2m.push_back(u + mats);
+    diag.insert(diag.end(), r->diag.begin(), r->diag.end());
+    b.insert(b.end(), r->b.begin(), r->b.end());
+    dofs += r->n_dofs;
+    off.push_back(dofs);
+    mats += r->n_mats;
+    nnz += (uint32_t)r->cols.size();
+  }
+  const Request *r0 = batch.front();
+  const uint32_t n = (uint32_t)batch.size();
+  std::vector<uint32_t> iters(n, 0);
+  std::vector<int> st(n, GBFE_OK);
+  std::vector<double> rn(n, 0.0), x(dofs, 0.0);
+  gbfe_mesh *me = nullptr;
+  gbfe_cons *cons = nullptr;
+  gbfe_op *A = nullptr, *PC = nullptr;
+  gbfe_mv *bv = nullptr, *X = nullptr;
+  do {
+    if ((rc = gbfe_mesh_upload(ctx, (uint32_t)nd.size(), nd.data(), ids.data(), dofs, &me))) break;
+    if ((rc = gbfe_constraints_upload(me, (uint32_t)rows.size(), rows.data(), rsz.data(), cols.data(), racc.data(),
+                                      cvals.data(), inh.data(), &cons)))
+      break;
+    if ((rc = gbfe_cellmat_upload_indexed(me, cons, mats, K.data(), c2m.data(), GBFE_PREC_FP64, &A))) break;
+    if ((rc = gbfe_jacobi_upload(me, diag.data(), &PC))) break;
+    if ((rc = gbfe_mv_create(me, 1, GBFE_F64, &bv))) break;
+    if ((rc = gbfe_mv_copy_in(bv, b.data()))) break;
+    if ((rc = gbfe_mv_create(me, 1, GBFE_F64, &X))) break;
+    rc = gbfe_pcg_solve_batched(A, PC, bv, X, n, off.data(), r0->max_iter, r0->abs_tol, r0->rel_tol, r0->div_tol,
+                                16, iters.data(), st.data(), rn.data());
+    if (rc == GBFE_OK) rc = gbfe_mv_copy_out(X, x.data());
+  } while (false);
+  char msg[512] = {0};
+  if (rc != GBFE_OK) gbfe_last_error(ctx, msg, sizeof msg);
+  for (uint32_t i = 0; i < n; ++i) {
+    Request *r = batch[i];
+    if (rc != GBFE_OK) {
+      r->status = rc;
+      r->message = msg;
+      continue;
+    }
+    r->status = st[i];
+    r->iters = iters[i];
+    r->x.assign(x.begin() + (ptrdiff_t)off[i], x.begin() + (ptrdiff_t)off[i + 1]);
+  }
+  gbfe_mv_destroy(X);
+  gbfe_mv_destroy(bv);
+  gbfe_op_destroy(A);
+  gbfe_op_destroy(PC);
+  gbfe_constraints_destroy(cons);
+  gbfe_mesh_destroy(me);
+}
+
+// two Poisson requests can share a batched solve
+bool same_cg_params(const Request *a, const Request *b) {
+  return a->kind == 1 && b->kind == 1 && a->max_iter == b->max_iter && a->abs_tol == b->abs_tol &&
+         a->rel_tol == b->rel_tol && a->div_tol == b->div_tol;
+}
+
 // admit waiting requests while a slot is free and the footprint fits (lock held)
 void admit_locked(gbfe_server *sv) {
   while (!sv->queue.empty()) {
@@ -230,7 +331,31 @@ void admit_locked(gbfe_server *sv) {
     r->state = RQ_RUNNING;
     r->t_admit = now_s();
     free_slot->req = r;
+    free_slot->batch.clear();
     ++sv->admitted;
+    if (r->kind == 1) {
+      // continuous batching: the compatible Poisson requests waiting behind it
+      // join the same solve while the budget allows
+      for (auto it = sv->queue.begin(); it != sv->queue.end() && free_slot->batch.size() + 1 < sv->max_poisson_batch;) {
+        Request *q = *it;
+        if (!q->cancel.load() && same_cg_params(r, q) && q->footprint <= sv->budget &&
+            sv->used + q->footprint <= sv->budget) {
+          if (free_slot->batch.empty()) free_slot->batch.push_back(r);
+          free_slot->batch.push_back(q);
+          sv->used += q->footprint;
+          q->state = RQ_RUNNING;
+          q->t_admit = r->t_admit;
+          ++sv->admitted;
+          it = sv->queue.erase(it);
+        } else {
+          ++it;
+        }
+      }
+      if (!free_slot->batch.empty()) {
+        ++sv->poisson_batches;
+        sv->poisson_batched += free_slot->batch.size();
+      }
+    }
     sv->cv_work.notify_all();
   }
 }
@@ -248,18 +373,30 @@ void worker(gbfe_server *sv, size_t slot_index) {
     }
     const bool urgent = r->kind != 0 && slot.hi;
     if (urgent) gbfe_ctx_set_stream(slot.ctx, slot.hi);
-    run_request(sv, slot.ctx, r);
+    std::vector<Request *> done;
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      done = slot.batch.empty() ? std::vector<Request *>{r} : slot.batch;
+    }
+    if (done.size() > 1)
+      run_poisson_batch(sv, slot.ctx, done);
+    else
+      run_request(sv, slot.ctx, r);
     if (urgent) {
       gbfe_ctx_synchronize(slot.ctx);  // nothing of this request left on the priority stream
       gbfe_ctx_set_stream(slot.ctx, nullptr);
     }
     {
       std::lock_guard<std::mutex> lk(sv->mu);
-      r->t_done = now_s();
-      r->state = RQ_DONE;
-      sv->used -= r->footprint;
+      const double t = now_s();
+      for (Request *q : done) {
+        q->t_done = t;
+        q->state = RQ_DONE;
+        sv->used -= q->footprint;
+        ++sv->completed;
+      }
       slot.req = nullptr;
-      ++sv->completed;
+      slot.batch.clear();
       admit_locked(sv);
       sv->cv_done.notify_all();
     }
@@ -473,6 +610,21 @@ int gbfe_server_stats(gbfe_server *sv, uint64_t *admitted, uint64_t *completed, 
   if (rejected) *rejected = sv->rejected;
   if (used_bytes) *used_bytes = sv->used;
   if (queued) *queued = (uint32_t)sv->queue.size();
+  return GBFE_OK;
+}
+
+int gbfe_server_batch_stats(gbfe_server *sv, uint64_t *poisson_batches, uint64_t *poisson_batched_requests) {
+  if (!sv) return GBFE_ERR_ARG;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (poisson_batches) *poisson_batches = sv->poisson_batches;
+  if (poisson_batched_requests) *poisson_batched_requests = sv->poisson_batched;
+  return GBFE_OK;
+}
+
+int gbfe_server_set_max_batch(gbfe_server *sv, uint32_t max_poisson_batch) {
+  if (!sv || max_poisson_batch == 0) return GBFE_ERR_ARG;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  sv->max_poisson_batch = max_poisson_batch;
   return GBFE_OK;
 }
 

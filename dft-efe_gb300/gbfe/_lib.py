@@ -120,6 +120,8 @@ SIGNATURES = {
     "gbfe_server_release": (i32, [p, u64]),
     "gbfe_server_stats": (i32, [p, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u32)]),
     "gbfe_server_inject_alloc_failures": (i32, [p, i32]),
+    "gbfe_server_batch_stats": (i32, [p, C.POINTER(u64), C.POINTER(u64)]),
+    "gbfe_server_set_max_batch": (i32, [p, u32]),
 }
 
 _lib = None

@@ -135,7 +135,14 @@ class Server:
         a, c, r, u = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
         q = C.c_uint32()
         self.lib.gbfe_server_stats(self.h, C.byref(a), C.byref(c), C.byref(r), C.byref(u), C.byref(q))
-        return dict(admitted=a.value, completed=c.value, rejected=r.value, used_bytes=u.value, queued=q.value)
+        nb, nr = C.c_uint64(), C.c_uint64()
+        self.lib.gbfe_server_batch_stats(self.h, C.byref(nb), C.byref(nr))
+        return dict(admitted=a.value, completed=c.value, rejected=r.value, used_bytes=u.value, queued=q.value,
+                    poisson_batches=nb.value, poisson_batched_requests=nr.value)
+
+    def set_max_batch(self, n: int) -> None:
+        """Largest batch of Poisson requests solved together (1: no batching)."""
+        self.lib.gbfe_server_set_max_batch(self.h, int(n))
 
     def close(self) -> None:
         if getattr(self, "h", None):

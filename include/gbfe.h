@@ -455,8 +455,18 @@ int gbfe_server_result(gbfe_server *server, uint64_t id, double *values, double 
 int gbfe_server_release(gbfe_server *server, uint64_t id);
 int gbfe_server_stats(gbfe_server *server, uint64_t *admitted, uint64_t *completed, uint64_t *rejected,
                       uint64_t *used_bytes, uint32_t *queued);
+/* Continuous batching of Poisson requests: when a Poisson request is admitted,
+ * the queued Poisson requests with the same iteration limit and tolerances
+ * join it (up to the batch limit, default 32, and the HBM budget) and all run
+ * as one batched solve (gbfe_pcg_solve_batched over the concatenated meshes).
+ * Each instance's arithmetic is that of a solve of its own, so results do not
+ * depend on the batch; a running batch is not cancellable.  Counters: batches
+ * of two or more requests, and the requests they carried. */
+int gbfe_server_batch_stats(gbfe_server *server, uint64_t *poisson_batches, uint64_t *poisson_batched_requests);
+/* Largest Poisson batch (1 turns batching off). */
+int gbfe_server_set_max_batch(gbfe_server *server, uint32_t max_poisson_batch);
 /* Fault injection for tests (host side): the next `count` admitted requests
- * fail their device upload with GBFE_ERR_ALLOC. */
+ * (a batch counts as one) fail their device upload with GBFE_ERR_ALLOC. */
 int gbfe_server_inject_alloc_failures(gbfe_server *server, int count);
 
 #ifdef __cplusplus

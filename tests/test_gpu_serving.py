@@ -32,13 +32,21 @@ def test_results_same_alone_and_in_the_mix(gpu_ctx, workload):
     from gbfe.serve import Server
 
     ks, pb = workload
-    # alone: one slot, requests strictly one after another
+    # alone: one slot, each request submitted after the previous one finished
+    # (so no Poisson batch forms)
+    from gbfe.serve import poisson_request_from_batch
+
     srv1 = Server(slots=1, hbm_budget_bytes=8 << 30)
     alone = []
-    for kind, rid, n in _submit_all(srv1, ks, pb):
-        info = srv1.wait(rid)
-        assert info.status == 0, info.message
-        alone.append(srv1.ks_result(rid, n)[0] if kind == "ks" else srv1.poisson_result(rid, n))
+    for j, prob in enumerate(ks):
+        X0 = M.random_block(prob.n_dofs, 8, 60 + j)
+        rid = srv1.submit_ks(prob, X0, 4, 10, 60, 1e-8, mixed=True)
+        assert srv1.wait(rid).status == 0
+        alone.append(srv1.ks_result(rid, 8)[0])
+        rid = srv1.submit_poisson(poisson_request_from_batch(pb, j))
+        assert srv1.wait(rid).status == 0
+        alone.append(srv1.poisson_result(rid, P.instance_view(pb, j)["N"]))
+    assert srv1.stats()["poisson_batches"] == 0
     srv1.close()
     # mixed: four slots, everything in flight together
     srv4 = Server(slots=4, hbm_budget_bytes=8 << 30)
@@ -53,6 +61,35 @@ def test_results_same_alone_and_in_the_mix(gpu_ctx, workload):
     assert st["completed"] == len(ids)
     for a, b in zip(alone, mixed):
         assert np.array_equal(a, b)  # private buffers + deterministic kernels: bitwise equal
+
+
+def test_poisson_requests_batched_bitwise_as_alone(gpu_ctx, workload):
+    """Poisson requests queued together run as one batched solve (continuous
+    batching); each result is bitwise the result of its solve alone."""
+    from gbfe.serve import Server, poisson_request_from_batch
+
+    _, pb = workload
+    srv = Server(slots=1, hbm_budget_bytes=8 << 30)
+    alone = []
+    for j in range(pb.n_inst):
+        rid = srv.submit_poisson(poisson_request_from_batch(pb, j))
+        assert srv.wait(rid).status == 0
+        alone.append(srv.poisson_result(rid, P.instance_view(pb, j)["N"]))
+    assert srv.stats()["poisson_batches"] == 0
+    # a KS request holds the slot while the Poisson requests queue behind it
+    ks = M.ks_box(3, 3, 6.0, 1, 4.0, 0.5, seed=71)
+    srv.submit_ks(ks, M.random_block(ks.n_dofs, 8, 72), 4, 10, 60, 1e-8, mixed=True)
+    rids = [srv.submit_poisson(poisson_request_from_batch(pb, j)) for j in range(pb.n_inst)]
+    batched = []
+    for j, rid in enumerate(rids):
+        info = srv.wait(rid)
+        assert info.status == 0, info.message
+        batched.append(srv.poisson_result(rid, P.instance_view(pb, j)["N"]))
+    st = srv.stats()
+    srv.close()
+    assert st["poisson_batches"] >= 1 and st["poisson_batched_requests"] >= 2
+    for a, b in zip(alone, batched):
+        assert np.array_equal(a, b)
 
 
 def test_admission_respects_budget_and_rejects_oversize(gpu_ctx, workload):
