@@ -469,6 +469,17 @@ static void cell_apply_f64(const gbfe_op *op, gbfe_mv *X, double *Yc) {
   check_launch(ctx, "cell_apply_f64");
 }
 
+// the FP64 cell product alone (no constraints, no assembly): the sliced
+// tensor-core product when the operator carries the slices and the FP64 mode
+// selects it, else the FP64 FMA kernel
+void cell_product_f64(const gbfe_op *op, gbfe_mv *X, double *Yc) {
+  GBFE_REQUIRE(X->mesh == op->mesh && X->dtype == GBFE_F64, "cell product: X must be FP64 on the operator's mesh");
+  if (op->mesh->ctx->fp64_tc && op->oz_aoff.p)
+    cell_apply_oz(op, X, Yc);
+  else
+    cell_apply_f64(op, X, Yc);
+}
+
 void apply_op(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y) {
   gbfe_mesh *me = op->mesh;
   gbfe_ctx *ctx = me->ctx;

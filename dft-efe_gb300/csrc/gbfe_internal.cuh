@@ -498,6 +498,9 @@ void build_oz_mats(gbfe_op *op);
 void cell_apply_oz(const gbfe_op *op, const gbfe_mv *X, double *Yc, const int *xexp = nullptr,
                    cudaStream_t stream = nullptr);
 const int *oz_column_exponents(const gbfe_op *op, const gbfe_mv *X);
+// Yc (cell-wise, sum nd_c x m) = the operator's FP64 cell products of X, no
+// constraints and no assembly (sliced tensor-core product in FP64 mode 1/2)
+void cell_product_f64(const gbfe_op *op, gbfe_mv *X, double *Yc);
 
 // vector kernels (solvers)
 void axpby(gbfe_ctx *ctx, size_t n, double a, const gbfe_mv *x, double b, const gbfe_mv *y, gbfe_mv *z);

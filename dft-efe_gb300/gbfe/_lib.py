@@ -85,6 +85,9 @@ SIGNATURES = {
     "gbfe_op_destroy": (i32, [p]),
     "gbfe_op_assemble_local": (i32, [p, u32, p, p, p, f64]),
     "gbfe_density": (i32, [p, p, u32, p, p]),
+    "gbfe_op_assemble_cells": (i32, [p, p, p, p, p, f64]),
+    "gbfe_density_cells": (i32, [p, p, p, p, p]),
+    "gbfe_density_op": (i32, [p, p, p, p]),
     "gbfe_mv_create": (i32, [p, u32, i32, C.POINTER(p)]),
     "gbfe_mv_wrap": (i32, [p, u32, i32, p, C.POINTER(p)]),
     "gbfe_mv_destroy": (i32, [p]),

@@ -345,6 +345,37 @@ def assemble_local(op: "OperatorContext", basis_values: np.ndarray, weights: np.
                                             float(alpha)), op.ctx.h, "assemble_local")
 
 
+def assemble_cells(op: "OperatorContext", nq_per_cell, basis_values: np.ndarray, weights: np.ndarray,
+                   fixed_mats: Optional[np.ndarray] = None, alpha: float = 1.0) -> None:
+    """A_c = alpha F_c + B_c^T diag(w_c) B_c for cells of any size and rule: B_c nq_c x nd_c row-major and
+    w_c (nq_c) per cell, cells concatenated."""
+    nq = np.ascontiguousarray(nq_per_cell, dtype=np.uint32)
+    B = np.ascontiguousarray(basis_values, dtype=np.float64)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    F = None if fixed_mats is None else np.ascontiguousarray(fixed_mats, dtype=np.float64)
+    check(op.ctx.lib.gbfe_op_assemble_cells(op.h, _ptr(nq), _ptr(B), _ptr(w), _ptr(F) if F is not None else None,
+                                            float(alpha)), op.ctx.h, "assemble_cells")
+
+
+def density_cells(Psi: "MultiVector", occupation, nq_per_cell, basis_values: np.ndarray) -> np.ndarray:
+    """rho at each cell's quadrature points (cells concatenated) for cells of any size and rule."""
+    nq = np.ascontiguousarray(nq_per_cell, dtype=np.uint32)
+    B = np.ascontiguousarray(basis_values, dtype=np.float64)
+    f = np.ascontiguousarray(occupation, dtype=np.float64)
+    out = np.empty(int(nq.astype(np.int64).sum()))
+    check(Psi.ctx.lib.gbfe_density_cells(Psi.h, _ptr(f), _ptr(nq), _ptr(B), _ptr(out)), Psi.ctx.h, "density_cells")
+    return out
+
+
+def density_op(basis_op: "OperatorContext", Psi: "MultiVector", occupation) -> np.ndarray:
+    """rho at nd_c points per cell with the interpolation run as the cell product of `basis_op` (a
+    CellMatrixOperatorContext built from each cell's basis values, use_constraints=False)."""
+    f = np.ascontiguousarray(occupation, dtype=np.float64)
+    out = np.empty(int(np.asarray(Psi.basis._nd, dtype=np.int64).sum()))
+    check(Psi.ctx.lib.gbfe_density_op(basis_op.h, Psi.h, _ptr(f), _ptr(out)), Psi.ctx.h, "density_op")
+    return out
+
+
 def density(Psi: "MultiVector", occupation, basis_values: np.ndarray) -> np.ndarray:
     """rho[c][q] = sum_i 2 f_i psi_i(x_cq)^2 (DensityCalculator::computeRho)."""
     B = np.ascontiguousarray(basis_values, dtype=np.float64)

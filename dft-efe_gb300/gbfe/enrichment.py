@@ -91,11 +91,16 @@ def enrichment_values(pts, center, l, mm, zeta, r0=3.0, d=3.0):
 
 
 def enriched_problem(n=12, p=4, L=24.0, n_atoms=8, Z=6.0, rc=0.4, seed=12347, specs=DEFAULT_SPECS, r0=3.0, d=3.0,
-                     nq_enr=None):
+                     nq_enr=None, keep_quadrature=False):
+    """keep_quadrature: also keep, per cell, the basis values at its
+    quadrature points (classical cells: the (p+1)^3 Gauss rule; enriched
+    cells: the finer rule over [N | phi~]) and the weights JxW V_loc, so that
+    H_c = 0.5 K_c + B_c^T diag(w_c) B_c (extra["quad_cells"])."""
     rng = np.random.default_rng(seed)
     atoms = rng.uniform(0.25 * L, 0.75 * L, size=(n_atoms, 3))
     charges = np.full(n_atoms, Z)
-    base = M.build_problem(n, p, L, atoms, charges, rc)
+    base = M.build_problem(n, p, L, atoms, charges, rc, keep_quadrature=keep_quadrature)
+    q_nq, q_B, q_w = [], [], []
     nq = p + 1
     nq_e = nq_enr or (p + 4)
     h = L / n
@@ -154,6 +159,10 @@ def enriched_problem(n=12, p=4, L=24.0, n_atoms=8, Z=6.0, rc=0.4, seed=12347, sp
             H_list.append(base.H[sl])
             M_list.append(base.M[sl])
             K_list.append(base.K[sl])
+            if keep_quadrature:
+                q_nq.append(base.extra["quad_B"].shape[0])
+                q_B.append(base.extra["quad_B"].ravel())
+                q_w.append(base.extra["quad_w"][c])
             continue
         pts = lo[c] + (qloc + 1.0) * jac
         vq = M.local_potential(pts, atoms, charges, rc)
@@ -175,6 +184,10 @@ def enriched_problem(n=12, p=4, L=24.0, n_atoms=8, Z=6.0, rc=0.4, seed=12347, sp
         Vc = Bx.T @ ((w3 * vq)[:, None] * Bx)
         Mc, Kc, Vc = [0.5 * (A + A.T) for A in (Mc, Kc, Vc)]
         Hc = 0.5 * Kc + Vc
+        if keep_quadrature:
+            q_nq.append(Bx.shape[0])
+            q_B.append(np.ascontiguousarray(Bx).ravel())
+            q_w.append(w3 * vq)
         ndc = nd0 + len(eids)
         nd_list.append(ndc)
         ids_list.append(np.concatenate([ids0[c], Ncl + np.array(eids, np.int64)]))
@@ -194,6 +207,8 @@ def enriched_problem(n=12, p=4, L=24.0, n_atoms=8, Z=6.0, rc=0.4, seed=12347, sp
     prob.extra.update(n_classical=Ncl, n_enrichment=nE, enr_begin=Ncl,
                       enr_block_inv=np.linalg.inv(0.5 * (Mee + Mee.T)),
                       enriched_cells=int(sum(1 for e in enr_of_cell if e)), seed=seed)
+    if keep_quadrature:
+        prob.extra["quad_cells"] = dict(nq=np.array(q_nq, np.uint32), B=np.concatenate(q_B), w=np.concatenate(q_w))
     return prob
 
 

@@ -120,7 +120,9 @@ int gbfe_op_attach_nonlocal(gbfe_op *op, const gbfe_nl *nl);
  * (vector tile, pipeline stages) shape on `op` (built with GBFE_PREC_MIXED)
  * with m vectors, per launch group of cell sizes, and keeps the fastest on the
  * context.  `report` receives one line per group ("tc2 nd_max tiles m N
- * stages ms").  With GBFE_AUTOTUNE_CACHE=<file> in the environment, new
+ * stages occupancy ms tmem_buffers"; tmem_buffers 1: one accumulator, which
+ * leaves TMEM for another CTA per SM; 0: two where they fit).  With
+ * GBFE_AUTOTUNE_CACHE=<file> in the environment, new
  * contexts load earlier lines from that file and tuning appends to it. */
 int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len);
 /* 1 (default): inside gbfe_ks_eigen_solve the d-1 steps of the Chebyshev
@@ -280,6 +282,28 @@ int gbfe_apply(const gbfe_op *op, gbfe_mv *X, gbfe_mv *Y);
  * rewritten by each call: calls whose work overlaps on the GPU (other streams,
  * other contexts) race and must be serialised by the caller. */
 int gbfe_apply_f64_noalloc(const gbfe_op *op, double *X_dev, double *Y_dev, uint32_t m);
+
+/* Cell matrices of cells of any size and quadrature rule (enriched cells carry
+ * extra basis functions and a finer rule): A_c = alpha F_c + B_c^T diag(w_c)
+ * B_c with B_c the cell's nq_c x nd_c basis values (row-major, cells
+ * concatenated) and w_c its nq_c weights (cells concatenated); the rest as
+ * gbfe_op_assemble_local (KohnShamOperatorContextFE.t.cpp:1253-1311). */
+int gbfe_op_assemble_cells(gbfe_op *op, const uint32_t *nq_per_cell, const double *basis_values,
+                           const double *weights, const double *fixed_mats, double alpha);
+/* Electron density for cells of any size and quadrature rule
+ * (DensityCalculator.t.cpp:37-100, 283-345): rho at the nq_c points of each
+ * cell (rho_host: sum nq_c values, cells concatenated), basis values as in
+ * gbfe_op_assemble_cells.  FP64. */
+int gbfe_density_cells(const gbfe_mv *Psi, const double *occupation, const uint32_t *nq_per_cell,
+                       const double *basis_values, double *rho_host);
+/* The same density with the interpolation psi_c = B_c Psi_c run as the cell
+ * product of `basis_op`: a cell operator on Psi's mesh, built without
+ * constraints from each cell's basis values B_c (nd_c points x nd_c
+ * functions, row-major, uploaded as the cell's "matrix" by
+ * gbfe_cellmat_upload), so rho has nd_c points per cell (rho_host: sum nd_c).
+ * With GBFE_PREC_FP64_TENSOR and FP64 mode 1 or 2 the product is the sliced
+ * FP64-accurate tensor-core kernel; else the FP64 FMA kernel. */
+int gbfe_density_op(const gbfe_op *basis_op, gbfe_mv *Psi, const double *occupation, double *rho_host);
 
 /* ---- Chebyshev filters -----------------------------------------------------
  * ResidualChebyshevFilterGEP (linearAlgebra/ChebyshevFilter.t.cpp:242-444).

@@ -19,6 +19,14 @@ Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
   - ``ks_eigen_solve``: the pass loop of KohnShamEigenSolver.t.cpp:319-487
     (without the Fermi-level step) and its bound heuristics :262-300;
   - ``lanczos_bounds``: LanczosExtremeEigenSolver.t.cpp:230-440.
+* Either side of the eigensolve (module functions, numpy FP64):
+  - ``assemble_cells``: KohnShamOperatorContextFE::reinit
+    (ksdft/KohnShamOperatorContextFE.t.cpp:1253-1311) with the kinetic part
+    (ksdft/KineticFE.t.cpp:90-97) passed as fixed matrices and the local
+    potential part int N_i V N_j (ksdft/ElectrostaticLocalFE.t.cpp:1625-1660);
+  - ``density_cells``: DensityCalculator's interpolation of psi to the
+    quadrature points and rho = sum_i 2 |psi_i|^2 f_i
+    (ksdft/DensityCalculator.t.cpp:37-100, 283-345).
 """
 from __future__ import annotations
 
@@ -324,3 +332,35 @@ class OracleSystem:
                 status = 0 if conv else 6
             wl, wu = eig[0], eig[m - 1]
         return status, eig, X, resid, passes
+
+
+def _cell_blocks(nd, nq_per_cell, basis_values):
+    off = 0
+    for k, q in zip(np.asarray(nd, np.int64), np.asarray(nq_per_cell, np.int64)):
+        yield k, q, basis_values[off: off + q * k].reshape(q, k)
+        off += q * k
+
+
+def assemble_cells(nd, nq_per_cell, basis_values, weights, fixed_mats=None, alpha=1.0):
+    """Cell matrices A_c = alpha F_c + B_c^T diag(w_c) B_c, column-major per
+    cell, cells concatenated (the layout of d_hamiltonianInAllCells)."""
+    out, moff, qoff = [], 0, 0
+    for k, q, Bc in _cell_blocks(nd, nq_per_cell, basis_values):
+        A = Bc.T @ (weights[qoff: qoff + q, None] * Bc)
+        if fixed_mats is not None:
+            A = A + alpha * fixed_mats[moff: moff + k * k].reshape(k, k).T
+        out.append(A.T.ravel())
+        moff += k * k
+        qoff += q
+    return np.concatenate(out)
+
+
+def density_cells(nd, ids, Psi, occupation, nq_per_cell, basis_values):
+    """rho at each cell's quadrature points, cells concatenated."""
+    out, doff = [], 0
+    occ = np.asarray(occupation, dtype=np.float64)
+    for k, q, Bc in _cell_blocks(nd, nq_per_cell, basis_values):
+        psi = Bc @ Psi[np.asarray(ids[doff: doff + k], np.int64)]  # nq_c x m
+        out.append((2.0 * psi * psi * occ[None, :]).sum(axis=1))
+        doff += k
+    return np.concatenate(out)

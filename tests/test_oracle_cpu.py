@@ -140,3 +140,16 @@ def test_nonlocal_matches_dense_projector_form(use_blas):
     # symmetric: the projected operator is Hermitian
     G = Xp.T @ Ynl
     assert np.abs(G - G.T).max() <= 1e-13 * np.abs(G).max()
+
+
+def test_oracle_assembly_reproduces_generator_enriched():
+    """The oracle's cell-matrix assembly (reinit's B^T diag(w) B plus the
+    kinetic part) reproduces the generator's enriched H: cells of two sizes
+    and two quadrature rules."""
+    import gbfe.enrichment as E
+
+    p = E.enriched_problem(4, 2, 16.0, 1, 4.0, 0.5, 108, keep_quadrature=True)
+    q = p.extra["quad_cells"]
+    assert len(np.unique(q["nq"])) == 2 and len(np.unique(p.nd_per_cell)) == 2
+    H = O.assemble_cells(p.nd_per_cell, q["nq"], q["B"], q["w"], p.K, 0.5)
+    assert np.abs(H - p.H).max() <= 1e-13 * np.abs(p.H).max()
