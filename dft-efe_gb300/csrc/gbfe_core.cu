@@ -865,6 +865,15 @@ int gbfe_ctx_check_wait_timeout(gbfe_ctx *ctx, double limit_s) {
   });
 }
 
+int gbfe_ctx_set_sm_budget(gbfe_ctx *ctx, int sms) {
+  if (!ctx || sms < 0) return GBFE_ERR_ARG;
+  return gbfe_guard(ctx, [&] {
+    int dev_sms = 0;
+    GBFE_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    ctx->sm_count = (sms == 0 || sms > dev_sms) ? dev_sms : sms;
+  });
+}
+
 int gbfe_ctx_set_split_groups(gbfe_ctx *ctx, int on) {
   if (!ctx) return GBFE_ERR_ARG;
   ctx->split_groups = on ? 1 : 0;

@@ -117,6 +117,23 @@ uint64_t poisson_footprint(const Request &r) {
   return r.K.size() * 8 + 8 * r.n_dofs * 8 + snd * 8 + snd * 12 + r.n_dofs * 16 + (16u << 20);
 }
 
+// Results are out (on the host, or the failure recorded): the requests are
+// done for their callers.  Called before the teardown of the requests'
+// device objects, whose frees synchronise the device and would otherwise
+// hold each result back until every other slot's queued kernels finished.
+// The slot, and the HBM budget the requests hold, stay taken until the
+// teardown is over (the worker releases them).
+void publish(gbfe_server *sv, const std::vector<Request *> &done) {
+  std::lock_guard<std::mutex> lk(sv->mu);
+  const double t = now_s();
+  for (Request *q : done) {
+    q->t_done = t;
+    q->state = RQ_DONE;
+    ++sv->completed;
+  }
+  sv->cv_done.notify_all();
+}
+
 // runs one request on a slot's context; every device object is freed on exit
 void run_request(gbfe_server *sv, gbfe_ctx *ctx, Request *r) {
   gbfe_mesh *me = nullptr;
@@ -190,6 +207,7 @@ void run_request(gbfe_server *sv, gbfe_ctx *ctx, Request *r) {
     } while (false);
     if (rc != GBFE_OK) fail(rc);
   }
+  publish(sv, std::vector<Request *>{r});
   gbfe_mv_destroy(X);
   gbfe_mv_destroy(bv);
   gbfe_op_destroy(A);
@@ -220,6 +238,7 @@ void run_poisson_batch(gbfe_server *sv, gbfe_ctx *ctx, const std::vector<Request
       r->status = rc;
       r->message = "injected allocation failure";
     }
+    publish(sv, batch);
     return;
   }
   std::vector<uint32_t> nd, ids, rows, rsz, cols, racc, c2m;
@@ -281,6 +300,7 @@ void run_poisson_batch(gbfe_server *sv, gbfe_ctx *ctx, const std::vector<Request
     r->iters = iters[i];
     r->x.assign(x.begin() + (ptrdiff_t)off[i], x.begin() + (ptrdiff_t)off[i + 1]);
   }
+  publish(sv, batch);
   gbfe_mv_destroy(X);
   gbfe_mv_destroy(bv);
   gbfe_op_destroy(A);
@@ -374,9 +394,11 @@ void worker(gbfe_server *sv, size_t slot_index) {
     const bool urgent = r->kind != 0 && slot.hi;
     if (urgent) gbfe_ctx_set_stream(slot.ctx, slot.hi);
     std::vector<Request *> done;
+    uint64_t footprint = 0;  // read now: a published request may be released by its caller
     {
       std::lock_guard<std::mutex> lk(sv->mu);
       done = slot.batch.empty() ? std::vector<Request *>{r} : slot.batch;
+      for (Request *q : done) footprint += q->footprint;
     }
     if (done.size() > 1)
       run_poisson_batch(sv, slot.ctx, done);
@@ -388,13 +410,7 @@ void worker(gbfe_server *sv, size_t slot_index) {
     }
     {
       std::lock_guard<std::mutex> lk(sv->mu);
-      const double t = now_s();
-      for (Request *q : done) {
-        q->t_done = t;
-        q->state = RQ_DONE;
-        sv->used -= q->footprint;
-        ++sv->completed;
-      }
+      sv->used -= footprint;
       slot.req = nullptr;
       slot.batch.clear();
       admit_locked(sv);

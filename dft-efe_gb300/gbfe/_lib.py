@@ -55,6 +55,7 @@ SIGNATURES = {
     "gbfe_ctx_check_wait_timeout": (i32, [p, f64]),
     "gbfe_ctx_set_tensor_cores": (i32, [p, i32]),
     "gbfe_ctx_set_split_groups": (i32, [p, i32]),
+    "gbfe_ctx_set_sm_budget": (i32, [p, i32]),
     "gbfe_ctx_set_profiling": (i32, [p, i32]),
     "gbfe_ctx_set_fp64_apply": (i32, [p, i32]),
     "gbfe_ctx_set_graphs": (i32, [p, i32]),

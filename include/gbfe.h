@@ -90,6 +90,11 @@ int gbfe_ctx_set_tensor_cores(gbfe_ctx *ctx, int mode);
  * does not read the enrichment rows computed just before (profiling off);
  * 0: one after the other on the context's stream. */
 int gbfe_ctx_set_split_groups(gbfe_ctx *ctx, int on);
+/* Size the grids of this context's kernels (persistent kernels: CTAs per SM x
+ * this count; strided kernels: their block counts) for `sms` multiprocessors
+ * instead of all of them (0: all).  Concurrent contexts on one GPU -- the
+ * serving slots -- then leave room on every SM for each other's kernels. */
+int gbfe_ctx_set_sm_budget(gbfe_ctx *ctx, int sms);
 /* ---- nonlocal pseudopotential part ---------------------------------------
  * Replaces basis::AtomCenterNonLocalOpContextFE
  * (basis/AtomCenterNonLocalOpContextFE.h:47-179): Y = sum_atoms C^T V C X.
