@@ -766,15 +766,20 @@ int gbfe_ctx_create(int device, gbfe_ctx **out) {
       ctx->tune_cache = cache;
       FILE *f = fopen(cache, "r");
       if (f) {
-        // "tc2 nd_max mtiles m N stages occupancy ms [tmem buffers]" (lines of other shapes are skipped)
+        // "tc2 nd_max mtiles m N stages occupancy ms [tmem buffers [prefetch [swapped]]]"
+        // (lines of other shapes are skipped)
         char line[256], kind[16];
-        unsigned nd, mt, mm, N, st, occ, nbuf = 0;
+        unsigned nd, mt, mm, N, st, occ, nbuf = 0, pf = 0, sw = 0;
         float ms;
         while (fgets(line, sizeof line, f)) {
           nbuf = 0;
-          const int got = sscanf(line, "%15s %u %u %u %u %u %u %f %u", kind, &nd, &mt, &mm, &N, &st, &occ, &ms, &nbuf);
+          pf = 0;
+          sw = 0;
+          const int got = sscanf(line, "%15s %u %u %u %u %u %u %f %u %u %u", kind, &nd, &mt, &mm, &N, &st, &occ, &ms,
+                                 &nbuf, &pf, &sw);
           if (got >= 8 && std::string(kind) == "tc2")
-            ctx->tc_tune[std::make_tuple(nd, mt, mm)] = TcTune{N, st, ms, occ, got == 9 ? nbuf : 0u};
+            ctx->tc_tune[std::make_tuple(nd, mt, mm)] = TcTune{
+                N, st, ms, occ, got >= 9 ? nbuf : 0u, got >= 10 ? std::min(pf, 3u) : 0u, got >= 11 && sw ? 1u : 0u};
         }
         fclose(f);
       }

@@ -156,6 +156,8 @@ struct TcTune {
   float ms = 0.f;
   uint32_t occ = 2;   // resident CTAs per SM the kernel is compiled for (2 or 3)
   uint32_t nbuf = 0;  // TMEM accumulator buffers: 0 two where they fit, 1 one (more CTAs per SM)
+  uint32_t pf = 0;    // X-row prefetch depth of the float4 gather (chunks, 0-3)
+  uint32_t swap = 0;  // 1: vectors on the MMA's M extent, cell rows on N
 };
 
 // Pinned host staging for small host-to-device copies issued inside a solve:

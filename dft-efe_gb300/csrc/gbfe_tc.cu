@@ -281,6 +281,17 @@ struct Tc2Args {
   // warps (a power of two, wpc * 32 lanes >= (KC / 8) * N / 4) each own every
   // (GATHER_WARPS / wpc)-th chunk; 0: one scalar row element per lane
   uint32_t wpc;
+  // float4 gather only: > 0 = the X rows of a group's next pf chunks are
+  // copied (cp.async) into lane-private shared staging ahead of use, so loads
+  // stay in flight through stage waits and epilogues; 0 = loads into registers
+  uint32_t pf;
+  uint32_t a_part;  // bytes of one A part (hi or lo) per stage: the group's largest cell, 8-row padded
+  // 0: cell rows on M (mtiles x 128), vectors on N; 1 (swapped): the 128
+  // vectors of the tile on M, the cell's rows on N (ncol = rows rounded up to
+  // 16): one MMA shape per K step whatever the cell size, and the epilogue
+  // writes each cell row's 128 vectors as whole 128-byte lines
+  uint32_t swap;
+  uint32_t ncol;  // TMEM columns of one accumulator buffer
 };
 
 // MINB: resident CTAs per SM the registers are budgeted for (2: 96 per thread;
@@ -290,9 +301,23 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t N = a.N, mtiles = a.mtiles, S = a.stages, nbuf = a.nbuf, m = a.m;
-  const uint32_t a_part = mtiles * 128 * KC * 2, b_part = N * KC * 2;
+  // A parts hold the group's largest cell (a.a_part bytes); the MMAs of the
+  // last M tile read up to mtiles * 128 rows, the rows past the cell's own
+  // coming from whatever follows (the allocation is padded for the last
+  // stage): they only feed accumulator rows >= nd, which are never stored
+  const uint32_t a_part = a.a_part, b_part = N * KC * 2;
   const uint32_t stage_bytes = 2 * a_part + 2 * b_part;
-  uint64_t *bars = (uint64_t *)(smem + S * stage_bytes);
+  // float4 gather: groups of wpc warps take ring chunks round robin.  A
+  // group's parity wait on a stage is only unambiguous when at most S chunks
+  // are in flight, so there are never more groups than stages.
+  uint32_t wpc = a.wpc;
+  if (wpc)
+    while (GATHER_WARPS / wpc > S) wpc *= 2;
+  const uint32_t P = wpc ? a.pf : 0;
+  const uint32_t stg_lanes = (KC / 8) * (N / 4);  // lanes of a group that gather (float4 mode)
+  const uint32_t stg_bytes = P ? (GATHER_WARPS / wpc) * (P + 1) * 8 * stg_lanes * 16 : 0;
+  const uint32_t pad = (a.swap ? a.ncol : mtiles * 128) * KC * 2 - a_part;  // rows the MMAs read past a_part
+  uint64_t *bars = (uint64_t *)(smem + S * stage_bytes + stg_bytes + pad);
   uint64_t *full_a = bars;
   uint64_t *full_b = bars + MAX_STAGES;
   uint64_t *empty = bars + 2 * MAX_STAGES;
@@ -305,12 +330,6 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
   const uint32_t tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
   const uint32_t n_items = a.ncells * a.vt;
 
-  // float4 gather: groups of wpc warps take ring chunks round robin.  A
-  // group's parity wait on a stage is only unambiguous when at most S chunks
-  // are in flight, so there are never more groups than stages.
-  uint32_t wpc = a.wpc;
-  if (wpc)
-    while (GATHER_WARPS / wpc > S) wpc *= 2;
   if (tid == 0) {
     for (uint32_t s = 0; s < MAX_STAGES; ++s) {
       mbar_init(&full_a[s], 1);
@@ -370,7 +389,7 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
   } else if (warp == MMA_WARP2) {
     // ---------------- MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = instr_desc(128, (int)N);
+      const uint32_t idesc = instr_desc(128, (int)(a.swap ? a.ncol : N));
       uint32_t q = 0, li = 0;
       for (uint32_t it = blockIdx.x; it < n_items && !*abort_flag; it += gridDim.x, ++li) {
         const uint32_t c = a.cells[it / a.vt];
@@ -389,16 +408,29 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           uint8_t *Ahi = smem + s * stage_bytes;
           const uint32_t ahi = smem_u32(Ahi), alo = ahi + a_part, bhi = alo + a_part, blo = bhi + b_part;
+          if (a.swap) {
+            // D[v][j] += X[v][k] A_c(k, j): the gathered tile is the M operand
+            const uint32_t d = tmem + b * a.ncol;
 #pragma unroll
-          for (uint32_t ks = 0; ks < KC / 16; ++ks) {
-            const uint64_t bdh = smem_desc(bhi + ks * 2 * LBO), bdl = smem_desc(blo + ks * 2 * LBO);
-            for (uint32_t t = 0; t < mtiles; ++t) {
-              const uint32_t aoff = t * 16 * SBO + ks * 2 * LBO;
-              const uint64_t adh = smem_desc(ahi + aoff), adl = smem_desc(alo + aoff);
-              const uint32_t d = tmem + (b * mtiles + t) * N;
-              umma(d, adh, bdh, idesc, (kc | ks) != 0);
-              umma(d, adh, bdl, idesc, 1);
-              umma(d, adl, bdh, idesc, 1);
+            for (uint32_t ks = 0; ks < KC / 16; ++ks) {
+              const uint64_t xdh = smem_desc(bhi + ks * 2 * LBO), xdl = smem_desc(blo + ks * 2 * LBO);
+              const uint64_t adh = smem_desc(ahi + ks * 2 * LBO), adl = smem_desc(alo + ks * 2 * LBO);
+              umma(d, xdh, adh, idesc, (kc | ks) != 0);
+              umma(d, xdl, adh, idesc, 1);
+              umma(d, xdh, adl, idesc, 1);
+            }
+          } else {
+#pragma unroll
+            for (uint32_t ks = 0; ks < KC / 16; ++ks) {
+              const uint64_t bdh = smem_desc(bhi + ks * 2 * LBO), bdl = smem_desc(blo + ks * 2 * LBO);
+              for (uint32_t t = 0; t < mtiles; ++t) {
+                const uint32_t aoff = t * 16 * SBO + ks * 2 * LBO;
+                const uint64_t adh = smem_desc(ahi + aoff), adl = smem_desc(alo + aoff);
+                const uint32_t d = tmem + b * a.ncol + t * N;
+                umma(d, adh, bdh, idesc, (kc | ks) != 0);
+                umma(d, adh, bdl, idesc, 1);
+                umma(d, adl, bdh, idesc, 1);
+              }
             }
           }
           umma_commit(&empty[s]);
@@ -423,11 +455,27 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
       if (!ok) return false;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t quad = warp % 4;
+      if (a.swap) {
+        // TMEM lane = vector of the tile, column = cell row: each store
+        // instruction writes 32 consecutive vectors of one row
+        const uint32_t v = quad * 32 + lane;
+        const bool vok = v0 + v < m;
+        for (uint32_t col = (warp / 4) * 16; col < a.ncol; col += 16 * (GATHER_WARPS / 4)) {
+          float val[16];
+          tmem_ld16(tmem + ((quad * 32) << 16) + b * a.ncol + col, val);
+          if (vok) {
+            float *dst = a.Yc + (uint64_t)(off + col) * m + v0 + v;
+#pragma unroll
+            for (uint32_t i = 0; i < 16; ++i)
+              if (col + i < nd) dst[(uint64_t)i * m] = val[i];
+          }
+        }
+      } else
       for (uint32_t t = 0; t < mtiles; ++t) {
         const uint32_t row = t * 128 + quad * 32 + lane;
         for (uint32_t col = (warp / 4) * 16; col < N; col += 32) {
           float v[16];
-          tmem_ld16(tmem + ((quad * 32) << 16) + (b * mtiles + t) * N + col, v);
+          tmem_ld16(tmem + ((quad * 32) << 16) + b * a.ncol + t * N + col, v);
           if (row < nd) {
             float *dst = a.Yc + (uint64_t)(off + row) * m + v0 + col;
             const uint32_t nvalid = min(16u, m - min(m, v0 + col));
@@ -455,12 +503,67 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
       // vectors (4*vq ..): 8 independent 16-byte row loads per lane, split and
       // stored as four 16-byte K-major rows of the B tile.  A group of wpc
       // warps covers one chunk; the G groups take chunks round robin, so G
-      // chunks are gathered concurrently (the loads are issued before the wait
-      // for the ring stage).
+      // chunks are gathered concurrently.  Without prefetch the loads are
+      // issued before the wait for the ring stage; with prefetch (P chunks
+      // ahead, cp.async into lane-private staging) they are issued P of the
+      // group's chunks earlier and stay in flight through the epilogues.
       const uint32_t G = GATHER_WARPS / wpc, grp = warp / wpc;
       const uint32_t nq = N / 4, L = (warp % wpc) * 32 + lane;
       const uint32_t kb = L / nq, vq = L % nq;
-      const bool active = L < (KC / 8) * nq;
+      const bool active = L < stg_lanes;
+      // store order rotated by (vq / 2) % 4: the eight lanes of each 16-byte
+      // store phase then write eight distinct rows of one core matrix, i.e.
+      // eight distinct bank groups
+      const uint32_t rot = (vq >> 1) & 3;
+      uint8_t *stg = smem + S * stage_bytes + grp * (P + 1) * 8 * stg_lanes * 16 + L * 16;
+      // prefetch cursor: the group's chunks in the order the loop below takes them
+      uint32_t p_it = blockIdx.x, p_kc = 0, p_q = 0, p_nk = 0, p_off = 0, p_nd = 0, p_v0 = 0;
+      auto p_load = [&]() {
+        if (p_it < n_items) {
+          const uint32_t c = a.cells[p_it / a.vt];
+          p_v0 = (p_it % a.vt) * N;
+          p_off = a.cell_off[c];
+          p_nd = a.cell_off[c + 1] - p_off;
+          p_nk = (p_nd + KC - 1) / KC;
+        }
+      };
+      auto p_step = [&]() {
+        if (++p_kc >= p_nk) {
+          p_kc = 0;
+          p_it += gridDim.x;
+          p_load();
+        }
+        ++p_q;
+      };
+      auto p_issue = [&](uint32_t slot) {  // one copy group per call, empty past the end
+        if (active && p_it < n_items) {
+          const bool vin = (p_v0 + 4 * vq) < m;
+          const uint32_t k0 = p_kc * KC + kb * 8;
+          uint8_t *dst = stg + slot * 8 * stg_lanes * 16;
+#pragma unroll
+          for (int kk = 0; kk < 8; ++kk) {
+            const float *src = a.X;
+            uint32_t bytes = 0;
+            if (vin && k0 + kk < p_nd) {
+              const uint32_t id = a.ids[p_off + k0 + kk];
+              const uint32_t e = id - a.sub_begin;
+              src = ((a.xsub && e < a.sub_n) ? a.xsub + (uint64_t)e * m : a.X + (uint64_t)id * m) + p_v0 + 4 * vq;
+              bytes = 16;
+            }
+            cp_async16(dst + kk * stg_lanes * 16, src, bytes);
+          }
+        }
+        cp_async_commit();
+      };
+      if (P) {
+        p_load();
+        while (p_it < n_items && p_q % G != grp) p_step();
+        for (uint32_t p = 0; p < P; ++p) {
+          p_issue(p);
+          do p_step(); while (p_it < n_items && p_q % G != grp);
+        }
+      }
+      uint32_t j = 0;  // the group's chunks consumed
       for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
         const uint32_t c = a.cells[it / a.vt];
         const uint32_t v0 = (it % a.vt) * N;
@@ -472,16 +575,30 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
           const uint32_t s = q % S;
           const uint32_t k0 = kc * KC + kb * 8;
           float4 xv[8];
+          if (P) {
+            p_issue((j + P) % (P + 1));
+            do p_step(); while (p_it < n_items && p_q % G != grp);
+            cp_async_wait(P);  // this chunk's copies (issued P groups ago) landed
+            const uint8_t *src = stg + (j % (P + 1)) * 8 * stg_lanes * 16;
 #pragma unroll
-          for (int kk = 0; kk < 8; ++kk)
-            xv[kk] = (vin && k0 + kk < nd)
-                         ? __ldg(reinterpret_cast<const float4 *>(a.X + (uint64_t)a.ids[off + k0 + kk] * m + v0 + 4 * vq))
-                         : make_float4(0.f, 0.f, 0.f, 0.f);
-          if (a.xsub && vin) {
+            for (int kk = 0; kk < 8; ++kk)
+              xv[kk] = active ? *reinterpret_cast<const float4 *>(src + kk * stg_lanes * 16)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+            ++j;
+          } else {
 #pragma unroll
-            for (int kk = 0; kk < 8; ++kk) {
-              const uint32_t e = (k0 + kk < nd ? a.ids[off + k0 + kk] : a.sub_begin + a.sub_n) - a.sub_begin;
-              if (e < a.sub_n) xv[kk] = __ldg(reinterpret_cast<const float4 *>(a.xsub + (uint64_t)e * m + v0 + 4 * vq));
+            for (int kk = 0; kk < 8; ++kk)
+              xv[kk] = (vin && k0 + kk < nd)
+                           ? __ldg(reinterpret_cast<const float4 *>(a.X + (uint64_t)a.ids[off + k0 + kk] * m + v0 +
+                                                                    4 * vq))
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (a.xsub && vin) {
+#pragma unroll
+              for (int kk = 0; kk < 8; ++kk) {
+                const uint32_t e = (k0 + kk < nd ? a.ids[off + k0 + kk] : a.sub_begin + a.sub_n) - a.sub_begin;
+                if (e < a.sub_n)
+                  xv[kk] = __ldg(reinterpret_cast<const float4 *>(a.xsub + (uint64_t)e * m + v0 + 4 * vq));
+              }
             }
           }
           if (q >= S) {
@@ -491,22 +608,27 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
           if (active) {
             uint8_t *Bhi = smem + s * stage_bytes + 2 * a_part;
             uint8_t *Blo = Bhi + b_part;
+            uint32_t ph[4][4], pl[4][4];  // [K pair j][vector w]: bf16 pairs (k0 + 2j, k0 + 2j + 1)
 #pragma unroll
             for (int w = 0; w < 4; ++w) {
-              uint32_t ph[4], pl[4];
 #pragma unroll
-              for (int j = 0; j < 4; ++j) {
-                const float4 &x0 = xv[2 * j], &x1 = xv[2 * j + 1];
+              for (int jj = 0; jj < 4; ++jj) {
+                const float4 &x0 = xv[2 * jj], &x1 = xv[2 * jj + 1];
                 __nv_bfloat16 h0, l0, h1, l1;
                 split_bf16(w == 0 ? x0.x : w == 1 ? x0.y : w == 2 ? x0.z : x0.w, h0, l0);
                 split_bf16(w == 0 ? x1.x : w == 1 ? x1.y : w == 2 ? x1.z : x1.w, h1, l1);
-                ph[j] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-                pl[j] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                ph[jj][w] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                pl[jj][w] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
               }
+            }
+            auto pick = [](const uint32_t(&r)[4], uint32_t w) { return w == 0 ? r[0] : w == 1 ? r[1] : w == 2 ? r[2] : r[3]; };
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const uint32_t w = (i + rot) & 3;
               const uint32_t v = 4 * vq + w;
               const uint32_t pos = (v / 8) * SBO + kb * LBO + (v % 8) * 16;
-              *(uint4 *)(Bhi + pos) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
-              *(uint4 *)(Blo + pos) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+              *(uint4 *)(Bhi + pos) = make_uint4(pick(ph[0], w), pick(ph[1], w), pick(ph[2], w), pick(ph[3], w));
+              *(uint4 *)(Blo + pos) = make_uint4(pick(pl[0], w), pick(pl[1], w), pick(pl[2], w), pick(pl[3], w));
             }
           }
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -519,6 +641,7 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
         prev_it = it;
       }
       if (ok && lag && li >= 1) epilogue(li - 1, prev_it);
+      if (P) cp_async_wait(0);  // no copy may land after the CTA leaves
     } else {
     for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
       const uint32_t c = a.cells[it / a.vt];
@@ -633,12 +756,17 @@ bool tc_supported(const gbfe_mesh *me) { return me->nd_max <= 256; }
 
 // v2 launch: persistent grid over (cell, vector tile) items of one M-tile group.
 // N_req / stages_req = 0: the tuned shape if one exists, else the heuristic.
-// returns the resident CTAs per SM the launch used
-static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg,
-                           uint32_t ncell, uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0,
-                           uint32_t stages_req = 0, const __nv_bfloat16 *tiles = nullptr, const float *xsub = nullptr,
-                           uint32_t sub_begin = 0, uint32_t sub_n = 0, uint32_t occ_req = 0,
-                           cudaStream_t stream = nullptr, uint32_t nbuf_req = 0) {
+// Returns the shape the launch used (stages and prefetch depth reduced until
+// the shared memory fits; CTAs per SM from shared memory, TMEM and registers).
+struct Tc2Used {
+  uint32_t per_sm, stages, pf, nbuf;
+};
+static Tc2Used launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, float *Yc, uint32_t cbeg,
+                          uint32_t ncell, uint32_t mtiles, double frac, uint32_t nd_max, uint32_t N_req = 0,
+                          uint32_t stages_req = 0, const __nv_bfloat16 *tiles = nullptr, const float *xsub = nullptr,
+                          uint32_t sub_begin = 0, uint32_t sub_n = 0, uint32_t occ_req = 0,
+                          cudaStream_t stream = nullptr, uint32_t nbuf_req = 0, uint32_t pf_req = 0,
+                          uint32_t swap_req = 0) {
   gbfe_mesh *me = op->mesh;
   const uint32_t m = X->m;
   if (!stream) stream = ctx->stream;
@@ -649,26 +777,52 @@ static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, f
       stages_req = it->second.stages;
       occ_req = it->second.occ;
       nbuf_req = it->second.nbuf;
+      pf_req = it->second.pf;
+      swap_req = it->second.swap;
     }
   }
   const uint32_t occ = occ_req >= 3 ? 3u : 2u;
+  const uint32_t swap = swap_req ? 1u : 0u;
   uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
   if (N_req) N = std::min<uint32_t>(N, N_req);
+  if (swap) N = 128;  // the vector tile is the M extent
   const uint32_t vt = (m + N - 1) / N;
-  N = ((m + vt - 1) / vt + 15) / 16 * 16;
-  const uint32_t a_part = mtiles * 128 * KC * 2, b_part = N * KC * 2;
+  if (!swap) N = ((m + vt - 1) / vt + 15) / 16 * 16;
+  // A parts sized for the group's largest cell; the rows the MMAs read past
+  // it (up to the M tiles, or to the 16-rounded N extent when swapped) stay
+  // inside the allocation (pad)
+  const uint32_t a_part = (nd_max + 7) / 8 * 8 * KC * 2, b_part = N * KC * 2;
+  const uint32_t ncol16 = (nd_max + 15) / 16 * 16;
+  GBFE_REQUIRE(a_part <= mtiles * 128 * KC * 2 && ncol16 <= 256, "tensor-core launch: cell larger than its M tiles");
+  const uint32_t pad = (swap ? ncol16 : mtiles * 128) * KC * 2 - a_part;
   const uint32_t stage_bytes = 2 * a_part + 2 * b_part;
+  // float4 gather when every row of X (and of xsub) starts on a 16-byte boundary
+  uint32_t wpc = 0;
+  if (m % 4 == 0 && ((uintptr_t)X->f.p % 16) == 0 && ((uintptr_t)xsub % 16) == 0 && ctx->tc_gather4) {
+    wpc = 1;
+    while (wpc * 32 < (KC / 8) * (N / 4)) wpc *= 2;
+  }
+  uint32_t pf = wpc ? std::min<uint32_t>(pf_req, 3) : 0;
+  auto stg_bytes = [&](uint32_t st, uint32_t p) -> uint32_t {
+    if (!p) return 0;
+    uint32_t w = wpc;
+    while (GATHER_WARPS / w > st) w *= 2;  // as the kernel: no more gather groups than stages
+    return (GATHER_WARPS / w) * (p + 1) * 8 * ((KC / 8) * (N / 4)) * 16;
+  };
   uint32_t stages = stages_req ? std::min<uint32_t>(stages_req, MAX_STAGES) : MAX_STAGES;
   const uint32_t reserve = 1024 + 512;
-  while (stages > 2 && stages * stage_bytes + reserve > 227 * 1024) --stages;
-  GBFE_REQUIRE(stages * stage_bytes + reserve <= 227 * 1024, "tensor-core tile does not fit in shared memory");
-  const uint32_t smem = stages * stage_bytes + reserve;
+  const uint32_t limit = 227 * 1024;
+  while (pf > 0 && stages * stage_bytes + stg_bytes(stages, pf) + pad + reserve > limit) --pf;
+  while (stages > 2 && stages * stage_bytes + stg_bytes(stages, pf) + pad + reserve > limit) --stages;
+  const uint32_t smem = stages * stage_bytes + stg_bytes(stages, pf) + pad + reserve;
+  GBFE_REQUIRE(smem <= limit, "tensor-core tile does not fit in shared memory");
   // two TMEM accumulators (the epilogue of one item overlaps the MMAs of the
   // next) where they fit, unless one was asked for (half the columns: room
   // for another CTA on the SM)
-  const uint32_t nbuf = (2 * mtiles * N <= 512 && nbuf_req != 1) ? 2 : 1;
+  const uint32_t ncol = swap ? ncol16 : mtiles * N;  // TMEM columns of one accumulator
+  const uint32_t nbuf = (2 * ncol <= 512 && nbuf_req != 1) ? 2 : 1;
   uint32_t cols = 32;
-  while (cols < nbuf * mtiles * N) cols *= 2;
+  while (cols < nbuf * ncol) cols *= 2;
   // CTAs per SM: shared memory (228 KB per SM, 1 KB of it reserved per CTA),
   // TMEM columns and the register budget of the instantiation
   const uint32_t per_sm =
@@ -680,15 +834,9 @@ static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, f
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
   });
-  // float4 gather when every row of X (and of xsub) starts on a 16-byte boundary
-  uint32_t wpc = 0;
-  if (m % 4 == 0 && ((uintptr_t)X->f.p % 16) == 0 && ((uintptr_t)xsub % 16) == 0 && ctx->tc_gather4) {
-    wpc = 1;
-    while (wpc * 32 < (KC / 8) * (N / 4)) wpc *= 2;
-  }
   Tc2Args args{X->f.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, vt, op->tc_aoff.p,
                tiles ? tiles : op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xsub, sub_begin,
-               sub_n, wpc};
+               sub_n, wpc, pf, a_part, swap, ncol};
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
   if (per_sm >= 3)
@@ -696,7 +844,7 @@ static uint32_t launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, f
   else
     k_cell_apply_tc2<2><<<grid, THREADS2, smem, stream>>>(args);
   check_launch(ctx, "cell_apply_tc2");
-  return per_sm;
+  return Tc2Used{per_sm, stages, pf, nbuf};
 }
 
 // Yc (FP32 cell-wise buffer) = split-BF16 tensor-core products, size-binned by
@@ -818,20 +966,24 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
     const uint32_t nd_max = me->bin_nd[b1 - 1];
     TcTune best;
     best.ms = 1e30f;
+    for (uint32_t sw : {0u, 1u})
     for (uint32_t N : {16u, 32u, 64u, 128u, 256u}) {
-      if (N > std::max<uint32_t>(16, (m + 15) / 16 * 16) && N != 16) continue;
+      if (sw ? N != 128 : (N > std::max<uint32_t>(16, (m + 15) / 16 * 16) && N != 16)) continue;
       for (uint32_t st : {2u, 3u, 4u})
       for (uint32_t occ : {2u, 3u})
-      for (uint32_t nb : {0u, 1u}) {
-        if (nb == 1 && 2 * mtiles * N > 512) continue;  // one buffer already
-        // warm; a shape that cannot hold 3 CTAs per SM runs as the 2-CTA one: not timed twice
-        const uint32_t used = launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st, nullptr,
-                                         nullptr, 0, 0, occ, ctx->stream, nb);
-        if (occ > 2 && used < occ) continue;
+      for (uint32_t nb : {0u, 1u})
+      for (uint32_t pf : {0u, 1u, 2u, 3u}) {
+        // warm; a shape that cannot hold 3 CTAs per SM runs as the 2-CTA one,
+        // one whose stages or prefetch were cut to fit, or that has room for
+        // one TMEM buffer only, as another shape: not timed twice
+        const Tc2Used used = launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st, nullptr,
+                                        nullptr, 0, 0, occ, ctx->stream, nb, pf, sw);
+        if ((occ > 2 && used.per_sm < occ) || used.stages != st || used.pf != pf || (nb == 0 && used.nbuf == 1))
+          continue;
         GBFE_CUDA(cudaEventRecord(e0, ctx->stream));
         for (int r = 0; r < 3; ++r)
           launch_tc2(ctx, op, &X, Yc.p, cbeg, ncell, mtiles, 0.0, nd_max, N, st, nullptr, nullptr, 0, 0, occ,
-                     ctx->stream, nb);
+                     ctx->stream, nb, pf, sw);
         GBFE_CUDA(cudaEventRecord(e1, ctx->stream));
         GBFE_CUDA(cudaEventSynchronize(e1));
         int st_word = 0;
@@ -849,13 +1001,16 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
           best.stages = st;
           best.occ = occ;
           best.nbuf = nb;
+          best.pf = pf;
+          best.swap = sw;
         }
       }
     }
     ctx->tc_tune[std::make_tuple(nd_max, mtiles, m)] = best;
     log.push_back("tc2 " + std::to_string(nd_max) + " " + std::to_string(mtiles) + " " + std::to_string(m) + " " +
                   std::to_string(best.N) + " " + std::to_string(best.stages) + " " + std::to_string(best.occ) + " " +
-                  std::to_string(best.ms) + " " + std::to_string(best.nbuf));
+                  std::to_string(best.ms) + " " + std::to_string(best.nbuf) + " " + std::to_string(best.pf) + " " +
+                  std::to_string(best.swap));
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -172,5 +172,25 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// 16-byte asynchronous global -> shared copy (L2 only); src_bytes 0 writes 16
+// zero bytes and reads nothing.  Both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// wait until at most n of this thread's copy groups are pending (n < 4); the
+// completed copies are then visible to this thread
+__device__ __forceinline__ void cp_async_wait(uint32_t n) {
+  if (n == 0)
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+  else if (n == 1)
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+  else if (n == 2)
+    asm volatile("cp.async.wait_group 2;" ::: "memory");
+  else
+    asm volatile("cp.async.wait_group 3;" ::: "memory");
+}
+
 }  // namespace tc
 }  // namespace gbfe

@@ -122,11 +122,15 @@ int gbfe_nonlocal_apply(const gbfe_nl *nl, const gbfe_cons *cons, gbfe_mv *X, gb
 int gbfe_op_attach_nonlocal(gbfe_op *op, const gbfe_nl *nl);
 
 /* Autotuner of the persistent split-BF16 tensor-core kernel: times every
- * (vector tile, pipeline stages) shape on `op` (built with GBFE_PREC_MIXED)
- * with m vectors, per launch group of cell sizes, and keeps the fastest on the
- * context.  `report` receives one line per group ("tc2 nd_max tiles m N
- * stages occupancy ms tmem_buffers"; tmem_buffers 1: one accumulator, which
- * leaves TMEM for another CTA per SM; 0: two where they fit).  With
+ * (vector tile, pipeline stages, CTAs per SM, TMEM buffers, X-row prefetch,
+ * orientation) shape on `op` (built with GBFE_PREC_MIXED) with m vectors, per
+ * launch group of cell sizes, and keeps the fastest on the context.  `report`
+ * receives one line per group ("tc2 nd_max tiles m N stages occupancy ms
+ * tmem_buffers prefetch swapped"; tmem_buffers 1: one accumulator, which
+ * leaves TMEM for another CTA per SM; 0: two where they fit; prefetch 0-3:
+ * chunks of X rows copied ahead into shared memory, 0 = gathered into
+ * registers; swapped 1: 128 vectors on the MMA's M extent and the cell's
+ * rows on N, 0: cell rows on M).  With
  * GBFE_AUTOTUNE_CACHE=<file> in the environment, new
  * contexts load earlier lines from that file and tuning appends to it. */
 int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len);

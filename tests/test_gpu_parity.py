@@ -407,7 +407,8 @@ def test_graph_replayed_filter_matches_eager(gpu_ctx, small_problem):
 
 
 def test_autotuned_tensor_core_shape(gpu_ctx, tmp_path, monkeypatch):
-    """The autotuner picks a (vector tile, stages, CTAs per SM, TMEM buffers) shape per cell-size group;
+    """The autotuner picks a (vector tile, stages, CTAs per SM, TMEM buffers, prefetch, orientation) shape per
+    cell-size group;
     every shape gives the split-BF16 result (TC_TOL against FP64), and the
     chosen shapes are written to and read back from the cache file."""
     from gbfe import api
@@ -426,8 +427,8 @@ def test_autotuned_tensor_core_shape(gpu_ctx, tmp_path, monkeypatch):
         Xf = api.MultiVector(basis, 40, dtype=np.float32, init=X0.astype(np.float32))
         Yf = api.MultiVector(basis, 40, dtype=np.float32)
         lines = api.autotune(H, 40)
-        # "tc2 nd_max tiles m N stages occupancy ms tmem_buffers"
-        assert lines and all(ln.split()[0] == "tc2" and len(ln.split()) == 9 for ln in lines)
+        # "tc2 nd_max tiles m N stages occupancy ms tmem_buffers prefetch swapped"
+        assert lines and all(ln.split()[0] == "tc2" and len(ln.split()) == 11 for ln in lines)
         H.apply(Xf, Yf)
         ctx.check_status()
         assert rel_maxnorm(Yf.numpy(), Y.numpy()) <= TC_TOL
