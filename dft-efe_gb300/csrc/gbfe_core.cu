@@ -568,11 +568,7 @@ void apply_pair_f64(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X, gbfe_mv *AX,
   const uint32_t m = X->m;
   constraints_p2c(ctx, A->cons, X);  // once: both applies read the same constrained X
   const int *xexp = oz_column_exponents(A, X);
-  if (!ctx->side_stream) {
-    GBFE_CUDA(cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
-    GBFE_CUDA(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
-    GBFE_CUDA(cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming));
-  }
+  ensure_side_stream(ctx);
   GBFE_CUDA(cudaEventRecord(ctx->fork_ev, ctx->stream));
   GBFE_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0));
   B->cellbuf.ensure((size_t)me->total_cell_dofs * m);

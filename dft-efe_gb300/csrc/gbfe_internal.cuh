@@ -381,6 +381,13 @@ inline unsigned grid_for(uint64_t n, unsigned block) {
 }
 
 inline void count_launch(gbfe_ctx *ctx, uint64_t n = 1) { ctx->launches += n; }
+// the context's side stream and its fork / join events, created on first use
+inline void ensure_side_stream(gbfe_ctx *ctx) {
+  if (ctx->side_stream) return;
+  GBFE_CUDA(cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
+  GBFE_CUDA(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
+  GBFE_CUDA(cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming));
+}
 inline void check_launch(gbfe_ctx *ctx, const char *name) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) throw Error(GBFE_ERR_CUDA, std::string(name) + ": " + cudaGetErrorString(e));
@@ -489,8 +496,10 @@ void oz_gram(gbfe_ctx *ctx, const double *const *A, uint32_t na, uint32_t ma, co
 // rows_ready: oz_rotate_rows already ran for these Y since they last changed
 void oz_rotate(gbfe_ctx *ctx, const double *T, uint32_t m, uint32_t mo, const double *const *Y, double *const *out,
                uint32_t nops, uint64_t N, bool rows_ready = false);
+// stream: where the launches go (default the context's stream; another
+// stream is not profiled)
 void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N,
-                    bool pair12 = false);
+                    bool pair12 = false, cudaStream_t stream = nullptr);
 // X = Y T and R = HY T - MY T diag(eps) in one launch (2m <= 512)
 bool oz_rotate_residual_supported(gbfe_ctx *ctx, uint32_t m);
 void oz_rotate_residual(gbfe_ctx *ctx, const double *T, const double *eps, uint32_t m, const double *Y,

@@ -37,6 +37,7 @@
 #include "gbfe_tc_ptx.cuh"
 
 #include <algorithm>
+#include <memory>
 
 using namespace gbfe;
 using namespace gbfe::tc;
@@ -743,23 +744,28 @@ static uint64_t rot_tiles_bytes(uint64_t N, uint32_t K) {
   return ((N + 127) / 128) * (uint64_t)((K + KC - 1) / KC) * oz::S * A_PART;
 }
 
-void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N, bool pair12) {
+void oz_rotate_rows(gbfe_ctx *ctx, const double *const *Y, uint32_t m, uint32_t nops, uint64_t N, bool pair12,
+                    cudaStream_t stream) {
   if (pair12) nops = 2;
+  const bool own = !stream || stream == ctx->stream;
+  if (!stream) stream = ctx->stream;
   ctx->oz_rexp.ensure((size_t)nops * N);
-  k_oz_rowexp<<<(unsigned)std::min<uint64_t>((nops * N + 7) / 8, (uint64_t)ctx->sm_count * 32), 256, 0,
-                ctx->stream>>>(Y[0], nops > 1 ? Y[1] : Y[0], (nops > 2 || pair12) ? Y[2] : Y[0], nops, m, N, pair12,
-                               ctx->oz_rexp.p);
+  k_oz_rowexp<<<(unsigned)std::min<uint64_t>((nops * N + 7) / 8, (uint64_t)ctx->sm_count * 32), 256, 0, stream>>>(
+      Y[0], nops > 1 ? Y[1] : Y[0], (nops > 2 || pair12) ? Y[2] : Y[0], nops, m, N, pair12, ctx->oz_rexp.p);
   count_launch(ctx, 1);
   uint64_t total = 0;
   for (uint32_t o = 0; o < nops; ++o) total += rot_tiles_bytes(N, (pair12 && o == 1) ? 2 * m : m);
   ctx->oz_dig.ensure(total);
-  ProfScope prof(ctx, "slice_f64_oz", 0.0, (double)N * m * 8.0 * (pair12 ? 3 : nops) + (double)total);
+  std::unique_ptr<ProfScope> prof;
+  if (own)
+    prof = std::make_unique<ProfScope>(ctx, "slice_f64_oz", 0.0,
+                                       (double)N * m * 8.0 * (pair12 ? 3 : nops) + (double)total);
   uint64_t off = 0;
   for (uint32_t o = 0; o < nops; ++o) {
     const bool two = pair12 && o == 1;
     const uint32_t K = two ? 2 * m : m, kchunks = (K + KC - 1) / KC;
     const uint64_t ntiles = ((N + 127) / 128) * (uint64_t)kchunks;
-    k_oz_slice_rows<<<(unsigned)std::min<uint64_t>(ntiles, (uint64_t)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+    k_oz_slice_rows<<<(unsigned)std::min<uint64_t>(ntiles, (uint64_t)ctx->sm_count * 8), 256, 0, stream>>>(
         Y[o], two ? Y[2] : Y[o], m, K, N, ctx->oz_rexp.p + (uint64_t)o * N, kchunks, ntiles, ctx->oz_dig.p + off);
     off += rot_tiles_bytes(N, K);
   }

@@ -858,6 +858,16 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
   bool rows_ready = false;
   // X and the residual R straight from Y, HY, MY (the rotated HY, MY are not kept)
   const bool oz_resid = oz_dense && oz_rotate_residual_supported(ctx, (uint32_t)m);
+  // the context stream waits for the side stream's work once armed
+  struct SideJoin {
+    gbfe_ctx *ctx;
+    bool armed = false;
+    void join() {
+      if (armed) cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0);
+      armed = false;
+    }
+    ~SideJoin() { join(); }
+  } side_join{ctx};
   // potrf, L^-1 S_H L^-T, syevd, L^-T V: the m x m stages, timed as one block
   auto eig_prof = std::make_unique<ProfScope>(ctx, "eig_small_f64", 0.0, 0.0);
   const bool host_eig = ctx->small_eig_host && m <= SMALL_EIG_HOST_MAX;
@@ -898,6 +908,19 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
     pool_arm.on = false;
     h2d_staged(ctx, ctx->pin_small, st.SH.p, hS.data(), hS.size() * 8);
   } else {
+    // the row digits of the rotation inputs depend on Y, HY, MY only: they are
+    // cut on the side stream while cuSOLVER works through the m x m block
+    // (short launches that leave most SMs idle); the guard joins the side
+    // stream back on every way out of this block
+    if (oz_dense && !ctx->profiling) {
+      ensure_side_stream(ctx);
+      GBFE_CUDA(cudaEventRecord(ctx->fork_ev, ctx->stream));
+      GBFE_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0));
+      oz_rotate_rows(ctx, rot_in, (uint32_t)m, 3, (uint64_t)N, oz_resid, ctx->side_stream);
+      GBFE_CUDA(cudaEventRecord(ctx->join_ev, ctx->side_stream));
+      side_join.armed = true;
+      rows_ready = true;
+    }
     int lwork = 0;
     GBFE_CUSOLVER(cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, m, st.SM.p, m, &lwork));
     ctx->lwork.ensure(std::max(lwork, 1));
@@ -934,6 +957,7 @@ int fused_pass(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, gbfe_mv 
     count_launch(ctx);
   }
   eig_prof.reset();
+  side_join.join();
   const double *T = st.SH.p;
   std::vector<double> nOnes(m, -1.0);
   DevVec d_no(ctx, m), d_e(ctx, m);

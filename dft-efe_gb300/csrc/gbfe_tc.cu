@@ -294,10 +294,13 @@ struct Tc2Args {
   uint32_t ncol;  // TMEM columns of one accumulator buffer
 };
 
+// GW gather / epilogue warps (8, or 16 for one CTA per SM).
 // MINB: resident CTAs per SM the registers are budgeted for (2: 96 per thread;
 // 3: 64, a few spilled) -- more CTAs keep more gather loads in flight
-template <int MINB>
-__global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args a) {
+template <int MINB, int GW>
+__global__ void __launch_bounds__((GW + 2) * 32, MINB) k_cell_apply_tc2(const Tc2Args a) {
+  constexpr int GATHER_WARPS = GW;
+  constexpr int TMA_WARP2 = GW, MMA_WARP2 = GW + 1;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t N = a.N, mtiles = a.mtiles, S = a.stages, nbuf = a.nbuf, m = a.m;
@@ -442,7 +445,7 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
     }
     __syncwarp();
   } else {
-    // ---------------- gather warps (0-7) + epilogue
+    // ---------------- gather warps (0 .. GW-1) + epilogue
     const uint32_t nvg = (N + 31) / 32;
     const uint32_t lag = nbuf - 1;  // with two TMEM buffers the epilogue trails by one cell
     auto epilogue = [&](uint32_t li, uint32_t it) -> bool {
@@ -473,7 +476,7 @@ __global__ void __launch_bounds__(THREADS2, MINB) k_cell_apply_tc2(const Tc2Args
       } else
       for (uint32_t t = 0; t < mtiles; ++t) {
         const uint32_t row = t * 128 + quad * 32 + lane;
-        for (uint32_t col = (warp / 4) * 16; col < N; col += 32) {
+        for (uint32_t col = (warp / 4) * 16; col < N; col += 16 * (GATHER_WARPS / 4)) {
           float v[16];
           tmem_ld16(tmem + ((quad * 32) << 16) + b * a.ncol + t * N + col, v);
           if (row < nd) {
@@ -781,7 +784,9 @@ static Tc2Used launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, fl
       swap_req = it->second.swap;
     }
   }
-  const uint32_t occ = occ_req >= 3 ? 3u : 2u;
+  // 1: one CTA per SM with 16 gather warps; 2, 3: CTAs per SM with 8
+  const uint32_t occ = occ_req >= 3 ? 3u : occ_req == 1 ? 1u : 2u;
+  const uint32_t gw = occ == 1 ? 16u : (uint32_t)GATHER_WARPS;
   const uint32_t swap = swap_req ? 1u : 0u;
   uint32_t N = std::min<uint32_t>(256, (m + 15) / 16 * 16);
   if (N_req) N = std::min<uint32_t>(N, N_req);
@@ -806,8 +811,8 @@ static Tc2Used launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, fl
   auto stg_bytes = [&](uint32_t st, uint32_t p) -> uint32_t {
     if (!p) return 0;
     uint32_t w = wpc;
-    while (GATHER_WARPS / w > st) w *= 2;  // as the kernel: no more gather groups than stages
-    return (GATHER_WARPS / w) * (p + 1) * 8 * ((KC / 8) * (N / 4)) * 16;
+    while (gw / w > st) w *= 2;  // as the kernel: no more gather groups than stages
+    return (gw / w) * (p + 1) * 8 * ((KC / 8) * (N / 4)) * 16;
   };
   uint32_t stages = stages_req ? std::min<uint32_t>(stages_req, MAX_STAGES) : MAX_STAGES;
   const uint32_t reserve = 1024 + 512;
@@ -831,18 +836,21 @@ static Tc2Used launch_tc2(gbfe_ctx *ctx, const gbfe_op *op, const gbfe_mv *X, fl
   const uint32_t grid = std::min<uint32_t>(items, per_sm * (uint32_t)ctx->sm_count);
   static PerDeviceOnce attr_once;
   attr_once.run(ctx->device, [&] {
-    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<3, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    GBFE_CUDA(cudaFuncSetAttribute(k_cell_apply_tc2<1, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
   });
   Tc2Args args{X->f.p, m, me->ids.p, me->cell_off.p, me->bin_cells.p + cbeg, ncell, vt, op->tc_aoff.p,
                tiles ? tiles : op->mats_hi.p, Yc, N, mtiles, cols, nbuf, stages, ctx->status.p, xsub, sub_begin,
                sub_n, wpc, pf, a_part, swap, ncol};
   ProfScope prof(ctx, "cell_apply_mixed", 2.0 * m * (double)me->total_mat * frac,
                  4.0 * (2.0 * (double)me->n_dofs * m + (double)me->total_mat) * frac);
-  if (per_sm >= 3)
-    k_cell_apply_tc2<3><<<grid, THREADS2, smem, stream>>>(args);
+  if (occ == 1)
+    k_cell_apply_tc2<1, 16><<<grid, (16 + 2) * 32, smem, stream>>>(args);
+  else if (per_sm >= 3)
+    k_cell_apply_tc2<3, 8><<<grid, THREADS2, smem, stream>>>(args);
   else
-    k_cell_apply_tc2<2><<<grid, THREADS2, smem, stream>>>(args);
+    k_cell_apply_tc2<2, 8><<<grid, THREADS2, smem, stream>>>(args);
   check_launch(ctx, "cell_apply_tc2");
   return Tc2Used{per_sm, stages, pf, nbuf};
 }
@@ -884,11 +892,7 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const __nv_bf
       for (size_t g = 0; g < groups.size() && side < 0; ++g)
         if (!groups[g].sub) side = (int)g;
     if (side >= 0) {
-      if (!ctx->side_stream) {
-        GBFE_CUDA(cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
-        GBFE_CUDA(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
-        GBFE_CUDA(cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming));
-      }
+      ensure_side_stream(ctx);
       if (!fork_recorded) GBFE_CUDA(cudaEventRecord(ctx->fork_ev, ctx->stream));
       GBFE_CUDA(cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0));
     }
@@ -970,7 +974,7 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
     for (uint32_t N : {16u, 32u, 64u, 128u, 256u}) {
       if (sw ? N != 128 : (N > std::max<uint32_t>(16, (m + 15) / 16 * 16) && N != 16)) continue;
       for (uint32_t st : {2u, 3u, 4u})
-      for (uint32_t occ : {2u, 3u})
+      for (uint32_t occ : {1u, 2u, 3u})
       for (uint32_t nb : {0u, 1u})
       for (uint32_t pf : {0u, 1u, 2u, 3u}) {
         // warm; a shape that cannot hold 3 CTAs per SM runs as the 2-CTA one,

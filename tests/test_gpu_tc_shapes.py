@@ -17,11 +17,14 @@ pytestmark = pytest.mark.gpu
 
 TC_TOL = 1e-4
 
-# (vector tile, ring stages, CTAs per SM asked, TMEM buffers flag, prefetch chunks, swapped)
+# (vector tile, ring stages, CTAs per SM asked (1: with 16 gather warps), TMEM buffers flag, prefetch chunks,
+#  swapped)
 SHAPES = [
     (32, 2, 2, 0, 0, 0), (32, 2, 2, 0, 1, 0), (32, 3, 2, 0, 3, 0),
     (64, 2, 2, 0, 0, 0), (64, 2, 2, 0, 2, 0), (64, 2, 2, 1, 3, 0), (64, 4, 2, 0, 1, 0),
     (128, 2, 2, 0, 0, 1), (128, 2, 2, 1, 0, 1), (128, 3, 2, 0, 2, 1), (128, 4, 2, 0, 0, 1),
+    # one CTA per SM with 16 gather warps
+    (32, 4, 1, 0, 0, 0), (64, 4, 1, 0, 1, 0), (128, 4, 1, 0, 0, 1), (128, 3, 1, 0, 1, 1),
 ]
 
 
