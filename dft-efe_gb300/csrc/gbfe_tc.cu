@@ -244,15 +244,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_cell_apply_tc(
 
 // ---------------------------------------------------------------------------
 // v2: persistent, warp-specialised, continuous chunk stream across cells.
-//   warps 0-7  gather X chunks into the B ring (one mbarrier arrive per warp per
-//              chunk) and run the epilogue of the previous cell (TMEM -> Yc;
-//              warp w reads the lanes of quadrant w % 4, every other 16 columns)
-//   warp 8     lane 0 issues the bulk TMA copies of A up to `stages` chunks ahead
-//   warp 9     allocates TMEM; lane 0 issues tcgen05.mma and the commits
-// Two CTAs per SM (registers capped by the launch bounds) keep 16 gather warps
-// in flight per SM: the gather's indirect row loads are the latency to hide.
-// TMEM holds `nbuf` accumulator buffers so one cell's epilogue overlaps the
-// next cell's MMAs.  The main loop synchronises through mbarriers only.
+//   warps 0..GW-1  gather X chunks into the B ring (one mbarrier arrive per
+//              warp per chunk) and run the epilogue of the previous cell (TMEM
+//              -> Yc; warp w reads the lanes of quadrant w % 4, every
+//              (GW / 4)-th block of 16 columns)
+//   warp GW    lane 0 issues the bulk TMA copies of A up to `stages` chunks ahead
+//   warp GW+1  allocates TMEM; lane 0 issues tcgen05.mma and the commits
+// Sixteen gather warps per SM -- two CTAs of 8 (registers capped by the
+// launch bounds) or one CTA of 16 -- keep the gather's indirect row loads in
+// flight: they are the latency to hide.  TMEM holds `nbuf` accumulator
+// buffers so one cell's epilogue overlaps the next cell's MMAs.  The main loop
+// synchronises through mbarriers only.
 // ---------------------------------------------------------------------------
 constexpr int MAX_STAGES = 4;
 constexpr int GATHER_WARPS = 8;
@@ -468,9 +470,14 @@ __global__ void __launch_bounds__((GW + 2) * 32, MINB) k_cell_apply_tc2(const Tc
           tmem_ld16(tmem + ((quad * 32) << 16) + b * a.ncol + col, val);
           if (vok) {
             float *dst = a.Yc + (uint64_t)(off + col) * m + v0 + v;
+            if (col + 16 <= nd) {
 #pragma unroll
-            for (uint32_t i = 0; i < 16; ++i)
-              if (col + i < nd) dst[(uint64_t)i * m] = val[i];
+              for (uint32_t i = 0; i < 16; ++i, dst += m) *dst = val[i];
+            } else {
+#pragma unroll
+              for (uint32_t i = 0; i < 16; ++i, dst += m)
+                if (col + i < nd) *dst = val[i];
+            }
           }
         }
       } else
@@ -514,10 +521,6 @@ __global__ void __launch_bounds__((GW + 2) * 32, MINB) k_cell_apply_tc2(const Tc
       const uint32_t nq = N / 4, L = (warp % wpc) * 32 + lane;
       const uint32_t kb = L / nq, vq = L % nq;
       const bool active = L < stg_lanes;
-      // store order rotated by (vq / 2) % 4: the eight lanes of each 16-byte
-      // store phase then write eight distinct rows of one core matrix, i.e.
-      // eight distinct bank groups
-      const uint32_t rot = (vq >> 1) & 3;
       uint8_t *stg = smem + S * stage_bytes + grp * (P + 1) * 8 * stg_lanes * 16 + L * 16;
       // prefetch cursor: the group's chunks in the order the loop below takes them
       uint32_t p_it = blockIdx.x, p_kc = 0, p_q = 0, p_nk = 0, p_off = 0, p_nd = 0, p_v0 = 0;
@@ -611,27 +614,25 @@ __global__ void __launch_bounds__((GW + 2) * 32, MINB) k_cell_apply_tc2(const Tc
           if (active) {
             uint8_t *Bhi = smem + s * stage_bytes + 2 * a_part;
             uint8_t *Blo = Bhi + b_part;
-            uint32_t ph[4][4], pl[4][4];  // [K pair j][vector w]: bf16 pairs (k0 + 2j, k0 + 2j + 1)
+            // (the four 16-byte stores of a lane hit two bank groups per
+            // 8-lane phase; rotating the store order per lane to spread them
+            // cost more select instructions than the conflicts cost time)
 #pragma unroll
             for (int w = 0; w < 4; ++w) {
+              uint32_t ph[4], pl[4];  // bf16 pairs (k0 + 2j, k0 + 2j + 1) of vector 4 vq + w
 #pragma unroll
               for (int jj = 0; jj < 4; ++jj) {
                 const float4 &x0 = xv[2 * jj], &x1 = xv[2 * jj + 1];
                 __nv_bfloat16 h0, l0, h1, l1;
                 split_bf16(w == 0 ? x0.x : w == 1 ? x0.y : w == 2 ? x0.z : x0.w, h0, l0);
                 split_bf16(w == 0 ? x1.x : w == 1 ? x1.y : w == 2 ? x1.z : x1.w, h1, l1);
-                ph[jj][w] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-                pl[jj][w] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                ph[jj] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                pl[jj] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
               }
-            }
-            auto pick = [](const uint32_t(&r)[4], uint32_t w) { return w == 0 ? r[0] : w == 1 ? r[1] : w == 2 ? r[2] : r[3]; };
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              const uint32_t w = (i + rot) & 3;
               const uint32_t v = 4 * vq + w;
               const uint32_t pos = (v / 8) * SBO + kb * LBO + (v % 8) * 16;
-              *(uint4 *)(Bhi + pos) = make_uint4(pick(ph[0], w), pick(ph[1], w), pick(ph[2], w), pick(ph[3], w));
-              *(uint4 *)(Blo + pos) = make_uint4(pick(pl[0], w), pick(pl[1], w), pick(pl[2], w), pick(pl[3], w));
+              *(uint4 *)(Bhi + pos) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+              *(uint4 *)(Blo + pos) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
             }
           }
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

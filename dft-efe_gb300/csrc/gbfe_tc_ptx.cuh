@@ -18,6 +18,7 @@ constexpr uint32_t SBO = (KC / 8) * CORE_BYTES;  // stride between 8-row groups
 constexpr uint32_t LBO = CORE_BYTES;             // stride between K-adjacent core matrices
 constexpr uint32_t WAIT_LIMIT = 1u << 24;        // bounded mbarrier polls
 constexpr uint64_t WAIT_NS = 2000000000ull;      // and at most 2 s per wait
+constexpr uint32_t WAIT_SUSPEND_NS = 20000;      // a poll may suspend the thread this long (woken at completion)
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -58,9 +59,9 @@ __device__ __forceinline__ bool mbar_wait_limited(uint64_t *bar, uint32_t parity
   for (uint32_t it = 0; it < max_polls; ++it) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(WAIT_SUSPEND_NS)
         : "memory");
     if (ok) return true;
     if ((it & 255u) == 255u) {
