@@ -281,11 +281,11 @@ def cpu_baseline_line(prob, cfg, deg, passes, procs) -> dict:
 #   cfg2: the two launches of one fused filter step of the workload itself
 #     (110.6 + 3.4 and 45.3 + 0.2 MB), averaged;
 #   cfg3: the split-BF16 product with the workload's tuned launch shape on an
-#     8^3-cell mesh of the same cells (216 dofs) and 512 vectors, 259.5 MB read
-#     + 171.1 MB written, scaled by the cells (13,824 / 512): every cell reads
+#     8^3-cell mesh of the same cells (216 dofs) and 512 vectors, 263.9 MB read
+#     + 168.5 MB written, scaled by the cells (13,824 / 512): every cell reads
 #     its own tiles and rows and writes its own cell-wise block
 NCU_TRAFFIC_PER_LAUNCH = {("cfg2", "cell_apply_mixed"): (110.6e6 + 3.4e6 + 45.3e6 + 0.2e6) / 2,
-                          ("cfg3", "cell_apply_mixed"): (259.5e6 + 171.1e6) * 13824 / 512}
+                          ("cfg3", "cell_apply_mixed"): (263.86e6 + 168.45e6) * 13824 / 512}
 
 # BF16 tensor-core products per FP64-accurate sliced product (8 x 8 digit
 # pairs with s + t <= 9)
