@@ -893,15 +893,16 @@ int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len
   if (!op) return GBFE_ERR_ARG;
   gbfe_ctx *ctx = op->mesh->ctx;
   return gbfe_guard(ctx, [&] {
-    std::vector<std::string> log;
-    autotune_tc(op, m, log);
-    std::string all;
+    std::vector<std::string> log, fresh;
+    autotune_tc(op, m, log, fresh);
+    std::string all, add;
     for (auto &l : log) all += l + "\n";
+    for (auto &l : fresh) add += l + "\n";
     if (report && report_len) snprintf(report, report_len, "%s", all.c_str());
-    if (!ctx->tune_cache.empty()) {
+    if (!ctx->tune_cache.empty() && !add.empty()) {
       FILE *f = fopen(ctx->tune_cache.c_str(), "a");
       if (f) {
-        fputs(all.c_str(), f);
+        fputs(add.c_str(), f);
         fclose(f);
       }
     }

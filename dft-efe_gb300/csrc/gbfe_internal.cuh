@@ -478,7 +478,7 @@ void assemble_cells(gbfe_mesh *me, const gbfe_cons *cons, int dtype, const void 
 void apply_pair_f64(const gbfe_op *A, const gbfe_op *B, gbfe_mv *X, gbfe_mv *AX, gbfe_mv *BX);
 void nonlocal_project(const gbfe_nl *nl, const gbfe_mv *X);
 void nonlocal_add(const gbfe_nl *nl, uint32_t m, int dtype, void *Yc);
-void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log);
+void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log, std::vector<std::string> &fresh);
 bool oz_supported(const gbfe_mesh *me);
 // dense symmetric eigen-decomposition on the host (gbfe_host_eig.cpp)
 int host_sym_eig(int n, double *a, double *w);

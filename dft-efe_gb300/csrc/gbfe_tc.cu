@@ -940,9 +940,11 @@ void cell_apply_tc(const gbfe_op *op, const gbfe_mv *X, float *Yc, const __nv_bf
   }
 }
 
-// Time every (vector tile, stages) shape of the persistent kernel on this
-// operator with m vectors and keep the fastest per launch group.
-void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
+// Time every launch shape of the persistent kernel on this operator with m
+// vectors and keep the fastest per launch group.  A group whose shape the
+// context already holds (tuned earlier, or loaded from the cache file) is not
+// timed again: its line is reported, not added to `fresh`.
+void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log, std::vector<std::string> &fresh) {
   gbfe_mesh *me = op->mesh;
   gbfe_ctx *ctx = me->ctx;
   GBFE_REQUIRE(op->tc_aoff.p, "autotune: operator has no tensor-core tiles (build it with GBFE_PREC_MIXED)");
@@ -969,6 +971,17 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
     if (b0 == UINT32_MAX) continue;
     const uint32_t cbeg = me->bin_begin[b0], ncell = me->bin_begin[b1] - cbeg;
     const uint32_t nd_max = me->bin_nd[b1 - 1];
+    auto line_of = [&](const TcTune &t) {
+      return "tc2 " + std::to_string(nd_max) + " " + std::to_string(mtiles) + " " + std::to_string(m) + " " +
+             std::to_string(t.N) + " " + std::to_string(t.stages) + " " + std::to_string(t.occ) + " " +
+             std::to_string(t.ms) + " " + std::to_string(t.nbuf) + " " + std::to_string(t.pf) + " " +
+             std::to_string(t.swap);
+    };
+    const auto known = ctx->tc_tune.find(std::make_tuple(nd_max, mtiles, m));
+    if (known != ctx->tc_tune.end()) {
+      log.push_back(line_of(known->second));
+      continue;
+    }
     TcTune best;
     best.ms = 1e30f;
     for (uint32_t sw : {0u, 1u})
@@ -1012,10 +1025,8 @@ void autotune_tc(const gbfe_op *op, uint32_t m, std::vector<std::string> &log) {
       }
     }
     ctx->tc_tune[std::make_tuple(nd_max, mtiles, m)] = best;
-    log.push_back("tc2 " + std::to_string(nd_max) + " " + std::to_string(mtiles) + " " + std::to_string(m) + " " +
-                  std::to_string(best.N) + " " + std::to_string(best.stages) + " " + std::to_string(best.occ) + " " +
-                  std::to_string(best.ms) + " " + std::to_string(best.nbuf) + " " + std::to_string(best.pf) + " " +
-                  std::to_string(best.swap));
+    log.push_back(line_of(best));
+    fresh.push_back(log.back());
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -132,7 +132,8 @@ int gbfe_op_attach_nonlocal(gbfe_op *op, const gbfe_nl *nl);
  * registers; swapped 1: 128 vectors on the MMA's M extent and the cell's
  * rows on N, 0: cell rows on M).  With
  * GBFE_AUTOTUNE_CACHE=<file> in the environment, new
- * contexts load earlier lines from that file and tuning appends to it. */
+ * contexts load earlier lines from that file and tuning appends to it; a
+ * group whose shape the context already holds is reported, not re-timed. */
 int gbfe_autotune(const gbfe_op *op, uint32_t m, char *report, size_t report_len);
 /* 1 (default): inside gbfe_ks_eigen_solve the d-1 steps of the Chebyshev
  * recurrence are captured once into a CUDA graph (second pass) and replayed
