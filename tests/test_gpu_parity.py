@@ -445,6 +445,11 @@ def test_autotuned_tensor_core_shape(gpu_ctx, tmp_path, monkeypatch):
         H.apply(Xf, Yf2)
         ctx2.check_status()
         assert np.array_equal(Yf2.numpy(), tuned)
+        # the cached shapes are reported again, not re-timed or re-appended
+        again = api.autotune(H, 40)
+        drop_ms = lambda ln: ln.split()[:7] + ln.split()[8:]
+        assert [drop_ms(ln) for ln in again] == [drop_ms(ln) for ln in lines]
+        assert cache.read_text().strip().splitlines() == lines
     finally:
         ctx2.close()
 
