@@ -94,6 +94,53 @@ struct PerDeviceOnce {
   }
 };
 
+// Device blocks kept for reuse by a thread that installs a cache (the serving
+// workers): a block freed there is parked instead of handed to cudaFree,
+// whose device-wide synchronisation would hold up the other slots' work.
+// Parked blocks become reusable only at mark_safe(), which the owner calls
+// once every stream that may still read them has been synchronised; blocks
+// are reused by exact size.  Past `cap` parked bytes a free goes to cudaFree.
+struct DevCache {
+  std::multimap<size_t, void *> ready, parked;
+  size_t bytes = 0, cap = 0;
+  void mark_safe() {
+    ready.insert(parked.begin(), parked.end());
+    parked.clear();
+  }
+  void release() {
+    for (auto &kv : ready) cudaFree(kv.second);
+    for (auto &kv : parked) cudaFree(kv.second);
+    ready.clear();
+    parked.clear();
+    bytes = 0;
+  }
+};
+inline DevCache *&thread_dev_cache() {
+  static thread_local DevCache *cache = nullptr;
+  return cache;
+}
+inline cudaError_t dev_alloc(void **p, size_t bytes) {
+  if (DevCache *c = thread_dev_cache()) {
+    auto it = c->ready.find(bytes);
+    if (it != c->ready.end()) {
+      *p = it->second;
+      c->ready.erase(it);
+      c->bytes -= bytes;
+      return cudaSuccess;
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
+inline void dev_free(void *p, size_t bytes) {
+  DevCache *c = thread_dev_cache();
+  if (c && c->bytes + bytes <= c->cap) {
+    c->parked.emplace(bytes, p);
+    c->bytes += bytes;
+    return;
+  }
+  cudaFree(p);
+}
+
 // owning device buffer
 template <class T>
 struct DBuf {
@@ -105,7 +152,7 @@ struct DBuf {
   DBuf &operator=(const DBuf &) = delete;
   ~DBuf() { reset(); }
   void reset() {
-    if (p && !borrowed) cudaFree(p);
+    if (p && !borrowed) dev_free(p, sizeof(T) * n);
     p = nullptr;
     n = 0;
     borrowed = false;
@@ -119,7 +166,11 @@ struct DBuf {
   void alloc(size_t count) {
     if (count == n && p) return;
     reset();
-    if (count) GBFE_CUDA(cudaMalloc(&p, sizeof(T) * count));
+    if (count) {
+      void *q = nullptr;
+      GBFE_CUDA(dev_alloc(&q, sizeof(T) * count));
+      p = static_cast<T *>(q);
+    }
     n = count;
   }
   // grow-only scratch
@@ -222,6 +273,7 @@ struct gbfe_ctx {
   std::vector<std::unique_ptr<gbfe::DBuf<double>>> vec_pool;  // scoped m-vectors of a pass (LIFO)
   std::vector<std::unique_ptr<PinnedSlot>> vec_pin;            // their host staging
   PinnedSlot pin_small;                                        // m x m eigenvectors
+  PinnedSlot pin_tab, pin_coef;  // the filter's coefficient tables (kept: cudaFreeHost synchronises the device)
   size_t vec_top = 0;
   gbfe::DBuf<double> oz_part;       // per-item Gram partials
   gbfe::DBuf<__nv_bfloat16> oz_tdig;  // slices of the rotation factor

@@ -383,6 +383,19 @@ void admit_locked(gbfe_server *sv) {
 void worker(gbfe_server *sv, size_t slot_index) {
   Slot &slot = sv->slots[slot_index];
   cudaSetDevice(sv->device);
+  // device blocks of finished requests are reused by the next ones on this
+  // slot (no cudaFree, and its device-wide synchronisation, between requests)
+  struct CacheScope {
+    DevCache cache;
+    explicit CacheScope(size_t cap) {
+      cache.cap = cap;
+      thread_dev_cache() = &cache;
+    }
+    ~CacheScope() {
+      thread_dev_cache() = nullptr;
+      cache.release();
+    }
+  } scope(std::max<uint64_t>(sv->budget / std::max<size_t>(1, sv->slots.size()), 1ull << 30));
   for (;;) {
     Request *r = nullptr;
     {
@@ -404,10 +417,9 @@ void worker(gbfe_server *sv, size_t slot_index) {
       run_poisson_batch(sv, slot.ctx, done);
     else
       run_request(sv, slot.ctx, r);
-    if (urgent) {
-      gbfe_ctx_synchronize(slot.ctx);  // nothing of this request left on the priority stream
-      gbfe_ctx_set_stream(slot.ctx, nullptr);
-    }
+    gbfe_ctx_synchronize(slot.ctx);  // nothing of this request left on the slot's streams
+    scope.cache.mark_safe();
+    if (urgent) gbfe_ctx_set_stream(slot.ctx, nullptr);
     {
       std::lock_guard<std::mutex> lk(sv->mu);
       sv->used -= footprint;

@@ -462,7 +462,6 @@ void launch_cheb_step<float>(gbfe_ctx *ctx, uint64_t n, uint32_t m, double alpha
 struct FilterWork {
   std::unique_ptr<gbfe_mv> s1, s2, R, RN, Yf;
   DBuf<double> tab, coef;
-  PinnedSlot pin_tab, pin_coef;
   cudaGraphExec_t exec = nullptr;
   gbfe_ctx *owner = nullptr;  // the context whose pool takes exec back
   std::vector<GraphProf> prof;
@@ -550,8 +549,8 @@ void residual_filter(const gbfe_op *A, const gbfe_op *B, const gbfe_op *BInv, co
   std::vector<double> ones(m, 1.0);
   d_ones.set(ctx, ones.data(), m);
   d_eig.set(ctx, eig_h, m);
-  h2d_staged(ctx, w.pin_tab, w.tab.p, s.eF2.data(), s.eF2.size() * 8);
-  h2d_staged(ctx, w.pin_coef, w.coef.p, coef.data(), coef.size() * 8);
+  h2d_staged(ctx, ctx->pin_tab, w.tab.p, s.eF2.data(), s.eF2.size() * 8);
+  h2d_staged(ctx, ctx->pin_coef, w.coef.p, coef.data(), coef.size() * 8);
   gbfe_mv *s1 = w.s1.get(), *s2 = w.s2.get();
   std::unique_ptr<gbfe_mv> &R = w.R, &RN = w.RN;
   const gbfe_mv *Yr = Y;
